@@ -1,0 +1,233 @@
+/*
+ * radar_graph.h -- C ABI of the GB300 frontier engine (librg.so).
+ *
+ * The library replaces the data-parallel hot path of RADAR-Graph: the
+ * Ligra-style edgeMap/vertexMap engine (sparse push, dense push, pull) and the
+ * PageRank, BFS, BC and Radii apps that drive it, in their push, push-pull,
+ * DegreeSorting, HUBDUP and RADAR variants.  Paths below are relative to the
+ * reference project root (RADAR variant unless another is named).
+ *
+ * Conventions
+ *  - Every call returns rg_status; RG_OK is 0.  Nothing aborts the process
+ *    (the reference abort()s / exit()s, e.g. ligra.h:285-288, IO.h:95-115).
+ *    rg_last_error() gives a one-line message for the calling thread.
+ *  - Vertex ids and edge offsets are uint32_t (Ligra's uintE/uintT without
+ *    -DLONG/-DEDGELONG, parallel.h:100-123); graphs with >= 2^32 directed
+ *    edges are refused with RG_EUNSUPPORTED.
+ *  - Pointers named h_* are host memory, d_* device memory.  `stream` is a
+ *    cudaStream_t passed as void* (NULL = the library's own stream).
+ *  - Ids passed to and returned from the app entry points are ORIGINAL ids:
+ *    when the graph was degree-sorted the library maps inputs (roots, sources)
+ *    and outputs through new_ids exactly as the reference apps do
+ *    (BFS.C:126-129, Radii.C:163-165, writeOutputToFile in every app), except
+ *    BFS parent VALUES, which stay in the graph's internal id space as in the
+ *    reference.
+ */
+#ifndef RADAR_GRAPH_H
+#define RADAR_GRAPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rg_status {
+  RG_OK = 0,
+  RG_EINVAL = 1,        /* bad argument: null pointer, id out of range, size mismatch */
+  RG_ENOMEM = 2,        /* device or host allocation failed */
+  RG_ECUDA = 3,         /* a CUDA call failed */
+  RG_EIO = 4,           /* a file could not be opened or read */
+  RG_EFORMAT = 5,       /* malformed input ("Bad input file", IO.h:235-248) */
+  RG_EUNSUPPORTED = 6,  /* option or size the engine does not implement */
+  RG_ETIMEOUT = 7,      /* a bounded device-side wait ran out */
+  RG_ENODEV = 8         /* no usable CUDA device */
+} rg_status;
+
+/* The five reference variants (src/<variant>/). */
+typedef enum rg_variant {
+  RG_PUSH = 0,       /* push-new-orig: every app pushes (dense_forward) */
+  RG_PUSH_PULL = 1,  /* push-pull: dense iterations pull (edgeMapDense) */
+  RG_DEGSORT = 2,    /* degree-sorting: push on a degree-sorted graph */
+  RG_HUBDUP = 3,     /* hubdup: push, hub accumulators privatised (bitmap + index map) */
+  RG_RADAR = 4       /* RADAR: degree sort + hubs privatised, hub <=> id < numHubs */
+} rg_variant;
+
+typedef struct rg_graph rg_graph;       /* device-resident CSR image (+ permutation) */
+typedef struct rg_frontier rg_frontier; /* device frontier: id queue + bitmap */
+
+const char* rg_last_error(void);
+const char* rg_status_str(rg_status s);
+/* Library version string, e.g. "radar-graph-gb300 0.1 sm_103a". */
+const char* rg_version(void);
+
+/* ------------------------------------------------------------------------
+ * Input formats and graph construction (host side; IO.h:207-632)
+ * ------------------------------------------------------------------------ */
+
+/* Seeded R-MAT (uniform=0: a=0.57 b=0.19 c=0.19) or Erdos-Renyi (uniform=1)
+ * edge list of 2^scale vertices and edge_factor * 2^scale edges, following
+ * the GAP generator (GAP/src/generator.h:52-114): 2^18-edge blocks, block b
+ * draws from mt19937 seeded with seed+b, then ids are permuted with an
+ * mt19937(seed) shuffle.  h_src/h_dst hold edge_factor<<scale entries. */
+rg_status rg_generate_edges(int scale, int edge_factor, uint64_t seed, int uniform,
+                            uint32_t* h_src, uint32_t* h_dst);
+
+/* Symmetric CSR from an edge list: both directions of every edge, then per
+ * vertex sort + unique + self-loop removal exactly like the symmetric text
+ * loader (IO.h:429-474).  *h_off_out (n+1) and *h_adj_out are malloc'ed by
+ * the library; release them with rg_host_free. */
+rg_status rg_csr_from_edges(int64_t n, int64_t num_edges, const uint32_t* h_src,
+                            const uint32_t* h_dst, uint32_t** h_off_out,
+                            uint32_t** h_adj_out, int64_t* m_out);
+
+/* Ligra AdjacencyGraph text: "AdjacencyGraph\n n\n m\n offsets[n]\n edges[m]"
+ * (IO.h:231-268).  write: h_off has n+1 entries. */
+rg_status rg_write_adjacency(const char* path, int64_t n, int64_t m, const uint32_t* h_off,
+                             const uint32_t* h_adj);
+/* Reads a Ligra text graph (binary=0) or the binary .config/.adj/.idx triple
+ * (binary=1, IO.h:477-626) and applies the same clean-up as the reference
+ * loader for symmetric graphs (text only; the binary reader does no clean-up
+ * in the reference either).  Result arrays as in rg_csr_from_edges. */
+rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_out,
+                        int64_t* m_out, uint32_t** h_off_out, uint32_t** h_adj_out);
+void rg_host_free(void* p);
+
+/* ------------------------------------------------------------------------
+ * Device graph (graph.h:57-87 / vertex.h:188-274)
+ * ------------------------------------------------------------------------ */
+
+/* Uploads a symmetric CSR (h_off: n+1, h_adj: m) to the current device. */
+rg_status rg_graph_create(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                          rg_graph** out);
+/* Uploads from arrays already on the device (copied; caller keeps ownership). */
+rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
+                                 const uint32_t* d_adj, rg_graph** out);
+/* Degree sort on the device (preprocessGraph, IO.h:843-895): rank vertices by
+ * (degree desc, id desc), relabel every neighbour list (order kept).  The new
+ * graph remembers new_ids; h_new_ids (n entries, may be NULL) receives it. */
+rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids);
+rg_status rg_graph_info(const rg_graph* g, int64_t* n, int64_t* m, int* degree_sorted);
+/* Copies the device CSR back (h_off: n+1, h_adj: m) -- for checking. */
+rg_status rg_graph_download(const rg_graph* g, uint32_t* h_off, uint32_t* h_adj,
+                            uint32_t* h_new_ids);
+rg_status rg_graph_free(rg_graph* g);
+
+/* ------------------------------------------------------------------------
+ * Apps: Compute(graph, P) of each reference app.  Outputs are indexed by
+ * ORIGINAL vertex id (arr[new_ids[v]] as writeOutputToFile does).
+ * ------------------------------------------------------------------------ */
+
+/* PageRank (PageRank.C:120-189): damping 0.85, stop at L1 < 1e-7 or
+ * max_iters.  h_ranks: n doubles. */
+rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks,
+                      int64_t* iters_out, double* l1_out);
+
+/* BFS (BFS.C:122-188) from ORIGINAL id `root` (-r).  h_parents (n, may be
+ * NULL): parent in internal id space, UINT32_MAX if unreached.  h_depth (n,
+ * may be NULL): BFS depth, -1 if unreached (bit-exact across variants). */
+rg_status rg_bfs(rg_graph* g, rg_variant variant, uint32_t root, uint32_t* h_parents,
+                 int32_t* h_depth, int64_t* rounds_out, int64_t* reached_out);
+
+/* BC (BC-manyiter-v2.C:205-367): max_iters sources drawn like the reference
+ * (mt19937(27491095), uniform over [0,n-1], redrawn on degree 0).  h_deps:
+ * n doubles, chained across sources as the reference does (NaN where a
+ * source left a vertex unreached). */
+rg_status rg_bc(rg_graph* g, rg_variant variant, int max_iters, double* h_deps,
+                int64_t* levels_out);
+/* Same with an explicit source list (ORIGINAL ids). */
+rg_status rg_bc_sources(rg_graph* g, rg_variant variant, const uint32_t* h_sources, int nsrc,
+                        double* h_deps, int64_t* levels_out);
+/* The sources rg_bc would use (ORIGINAL ids). */
+rg_status rg_bc_pick_sources(const rg_graph* g, int k, uint32_t* h_sources);
+
+/* Radii (Radii.C:140-218): min(n,64) seeds hashInt(i) % n.  h_radii: n int32
+ * (-1 unreached, 0 seed, else last round the vertex's mask grew). */
+rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* rounds_out);
+/* Radii with explicit seeds (ORIGINAL ids, bit i for seeds[i], k <= 64). */
+rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k,
+                         int32_t* h_radii, int64_t* rounds_out);
+
+/* ------------------------------------------------------------------------
+ * Engine (ligra.h:277-354 edgeMap, 461-493 vertexMap).  The functor of the
+ * reference (update/updateAtomic/cond/mergeDuplicates, utils.h:62-79) cannot
+ * cross a C ABI, so the operator is a closed enum of device functors that
+ * act on caller-owned device arrays.
+ * ------------------------------------------------------------------------ */
+
+typedef enum rg_op {
+  RG_OP_PAGERANK = 0,  /* p_next[d] += p_curr[s]/deg(s)          (PR_F)        */
+  RG_OP_BFS = 1,       /* parents[d] CAS UINT32_MAX -> s           (BFS_F)       */
+  RG_OP_BC_FWD = 2,    /* num_paths[d] += num_paths[s] if !visited (BC_F)        */
+  RG_OP_BC_BWD = 3,    /* deps[d] += deps[s] if !visited           (BC_Back_F)   */
+  RG_OP_RADII = 4      /* next_visited[d] |= visited[s] ...        (Radii_F)     */
+} rg_op;
+
+typedef enum rg_vop {
+  RG_VOP_PR_DAMP = 0,       /* p_next[i] = 0.85*p_next[i] + 0.15/n  (PR_Vertex_F)      */
+  RG_VOP_BC_VISIT = 1,      /* visited[i] = 1                       (BC_Vertex_F)      */
+  RG_VOP_BC_BACK = 2,       /* visited[i] = 1; deps[i] += inv[i]    (BC_Back_Vertex_F) */
+  RG_VOP_RADII_SYNC = 3     /* visited[i] = next_visited[i]          (Radii_Vertex_F)   */
+} rg_vop;
+
+/* Device arrays an operator reads and writes (unused ones may be NULL). */
+typedef struct rg_op_args {
+  double* p_curr;           /* PR: n */
+  double* p_next;           /* PR: n */
+  uint32_t* parents;        /* BFS: n */
+  double* num_paths;        /* BC forward: n (inverse path counts for RG_VOP_BC_BACK) */
+  double* deps;             /* BC backward: n */
+  uint32_t* visited_bits;   /* BC: (n+31)/32 words, bit i = visited */
+  int64_t* visited;         /* Radii: n masks */
+  int64_t* next_visited;    /* Radii: n masks */
+  int32_t* radii;           /* Radii: n */
+  int32_t round;            /* Radii: current round */
+} rg_op_args;
+
+/* edgeMap flags (ligra.h:51-57). */
+#define RG_NO_OUTPUT 1u
+#define RG_DENSE_FORWARD 8u
+
+rg_status rg_frontier_create(const rg_graph* g, rg_frontier** out);
+rg_status rg_frontier_free(rg_frontier* f);
+/* Sets the frontier to the given INTERNAL ids (host array, duplicates kept
+ * like vertexSubset(n, m, indices)). */
+rg_status rg_frontier_set(rg_frontier* f, const uint32_t* h_ids, int64_t k);
+rg_status rg_frontier_set_all(rg_frontier* f);
+rg_status rg_frontier_count(const rg_frontier* f, int64_t* count);
+/* Copies the frontier as a byte map (n bytes, 1 = member). */
+rg_status rg_frontier_get(const rg_frontier* f, uint8_t* h_member);
+
+/* One edgeMap over `in`.  out == NULL or flags & RG_NO_OUTPUT: no output.
+ * threshold -1 = m/20 (ligra.h:283).  Dense iterations push when flags has
+ * RG_DENSE_FORWARD and pull otherwise, as in ligra.h:302-307. */
+rg_status rg_edgemap(rg_graph* g, rg_frontier* in, rg_op op, const rg_op_args* args,
+                     rg_frontier* out, uint32_t flags, int64_t threshold, void* stream);
+rg_status rg_vertexmap(rg_graph* g, rg_frontier* f, rg_vop op, const rg_op_args* args,
+                       void* stream);
+
+/* Device buffers for rg_op_args (cudaMalloc'ed, zero-filled). */
+rg_status rg_device_alloc(size_t bytes, void** d_ptr);
+rg_status rg_device_free(void* d_ptr);
+rg_status rg_copy_to_device(void* d_dst, const void* h_src, size_t bytes);
+rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes);
+rg_status rg_synchronize(void);
+
+/* ------------------------------------------------------------------------
+ * Timing of the last app call (CUDA events on the launching stream).
+ * ------------------------------------------------------------------------ */
+typedef struct rg_timing {
+  double total_ms;          /* whole app call on the device */
+  double edge_ms;           /* time inside edge kernels */
+  int64_t edges_traversed;  /* GTEPS numerator (SURVEY-style edge count) */
+  int64_t algorithmic_bytes;/* compulsory bytes of the app's byte model */
+  int64_t edge_launches;    /* launches of the dominant edge kernel */
+  int64_t kernel_launches;  /* all kernel launches of the call */
+} rg_timing;
+rg_status rg_last_timing(rg_timing* t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RADAR_GRAPH_H */

@@ -1,0 +1,748 @@
+// Oracle: a CPU restatement of RADAR-Graph's edgeMap/vertexMap frontier engine
+// and of the PageRank, BFS, BC and Radii apps that drive it.
+//
+// This file is TEST INFRASTRUCTURE.  Only the tests, the smoke check and the
+// CPU-baseline leg of the benchmark load it, and only as the checker or as the
+// timed CPU reference arm.  The product (the CUDA library) never calls it.
+//
+// Parity is pinned: the outputs of this restatement are compared against the
+// reference's own OpenMP binaries (built from the reference sources by
+// oracle/Makefile into oracle/_ref/) on seeded graphs; the resulting golden
+// vectors live in tests/golden/ together with the script that made them.
+//
+// Every function cites the reference file:line it follows (paths are relative
+// to the reference project root, RADAR variant unless another is named).
+//
+// Variants (argument `variant`):
+//   0 push        src/push-new-orig : every app pushes (dense_forward)
+//   1 push-pull   src/push-pull     : dense iterations pull (edgeMapDense)
+//   2 degsort     src/degree-sorting: same as push; caller passes a sorted graph
+//   3 hubdup      src/hubdup        : push + thread-private hub accumulators,
+//                                     hubs found through a bitmap + index map
+//   4 radar       src/RADAR         : push + thread-private hubs = ids < numHubs
+//                                     (caller passes a degree-sorted graph)
+// All variants compute the same results (depths/radii exactly, doubles within
+// rounding), which is what the reference does too.
+
+#include <omp.h>
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+#include <algorithm>
+#include <atomic>
+#include <functional>
+#include <random>
+#include <utility>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;  // UINT_E_MAX in Ligra (parallel.h:113-123)
+
+enum Variant { kPush = 0, kPushPull = 1, kDegSort = 2, kHubDup = 3, kRadar = 4 };
+
+struct Csr {
+  int64_t n, m;
+  const uint32_t* off;  // n+1
+  const uint32_t* adj;  // m
+  uint32_t deg(int64_t v) const { return off[v + 1] - off[v]; }
+};
+
+// ---------------------------------------------------------------------------
+// Atomics.  The reference uses __sync CAS (utils.h:311-324) and a CAS loop for
+// double addition (utils.h:334-339) and 64-bit OR (Radii.C:30-35).
+// ---------------------------------------------------------------------------
+inline bool cas_u32(uint32_t* p, uint32_t o, uint32_t nv) {
+  return __atomic_compare_exchange_n(p, &o, nv, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+}
+inline bool cas_i32(int32_t* p, int32_t o, int32_t nv) {
+  return __atomic_compare_exchange_n(p, &o, nv, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+}
+inline void add_f64(double* p, double v) {
+  uint64_t* q = reinterpret_cast<uint64_t*>(p);
+  uint64_t old = __atomic_load_n(q, __ATOMIC_RELAXED);
+  for (;;) {
+    double o; memcpy(&o, &old, 8);
+    double nv = o + v;
+    uint64_t nb; memcpy(&nb, &nv, 8);
+    if (__atomic_compare_exchange_n(q, &old, nb, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return;
+  }
+}
+// Returns the value before the add (the BC forward functor needs oldV, BC-manyiter-v2.C:63-68).
+inline double add_f64_old(double* p, double v) {
+  uint64_t* q = reinterpret_cast<uint64_t*>(p);
+  uint64_t old = __atomic_load_n(q, __ATOMIC_RELAXED);
+  for (;;) {
+    double o; memcpy(&o, &old, 8);
+    double nv = o + v;
+    uint64_t nb; memcpy(&nb, &nv, 8);
+    if (__atomic_compare_exchange_n(q, &old, nb, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return o;
+  }
+}
+inline void or_i64(int64_t* p, int64_t b) {
+  int64_t old = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while ((old | b) != old &&
+         !__atomic_compare_exchange_n(p, &old, old | b, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+  }
+}
+
+// Parallel pack of the indices of set bytes, in increasing order (the
+// reference's pack_index, sequence.h, and the SlidingQueue compaction of
+// ligra.h:161-192 produce the same set).
+std::vector<uint32_t> pack_indices(const uint8_t* bits, int64_t n) {
+  int T = omp_get_max_threads();
+  std::vector<int64_t> cnt(T + 1, 0);
+  std::vector<uint32_t> out;
+#pragma omp parallel num_threads(T)
+  {
+    int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    int64_t b = n * t / nt, e = n * (t + 1) / nt, c = 0;
+    for (int64_t i = b; i < e; i++) c += bits[i] != 0;
+    cnt[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (int i = 0; i < nt; i++) cnt[i + 1] += cnt[i];
+      out.resize(cnt[nt]);
+    }
+    int64_t o = cnt[t];
+    for (int64_t i = b; i < e; i++) if (bits[i]) out[o++] = (uint32_t)i;
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Frontier (vertexSubset.h:111-229): sparse id list or dense byte map.
+// ---------------------------------------------------------------------------
+struct Frontier {
+  int64_t n = 0;
+  int64_t count = 0;
+  bool is_dense = false;
+  std::vector<uint32_t> ids;   // sparse form
+  std::vector<uint8_t> bits;   // dense form (one byte per vertex, like bool[n])
+  bool has_ids = false, has_bits = false;
+
+  static Frontier single(int64_t n, uint32_t v) {
+    Frontier f; f.n = n; f.count = 1; f.ids = {v}; f.has_ids = true; return f;
+  }
+  static Frontier all(int64_t n) {
+    Frontier f; f.n = n; f.count = n; f.bits.assign(n, 1); f.has_bits = true; f.is_dense = true;
+    return f;
+  }
+  static Frontier from_ids(int64_t n, std::vector<uint32_t> v) {
+    Frontier f; f.n = n; f.count = (int64_t)v.size(); f.ids = std::move(v); f.has_ids = true;
+    return f;
+  }
+  static Frontier from_bits(int64_t n, std::vector<uint8_t> b) {
+    Frontier f; f.n = n; f.bits = std::move(b); f.has_bits = true; f.is_dense = true;
+    int64_t c = 0;
+#pragma omp parallel for reduction(+ : c)
+    for (int64_t i = 0; i < n; i++) c += f.bits[i];
+    f.count = c;
+    return f;
+  }
+  // toSparse (vertexSubset.h:196-211): pack the indices of set bytes in order.
+  void to_sparse() {
+    if (!has_ids && count > 0) {
+      ids = pack_indices(bits.data(), n);
+      has_ids = true;
+    }
+    is_dense = false;
+  }
+  // toDense (vertexSubset.h:214-221).
+  void to_dense() {
+    if (!has_bits) {
+      bits.assign(n, 0);
+#pragma omp parallel for
+      for (int64_t i = 0; i < (int64_t)ids.size(); i++) bits[ids[i]] = 1;
+      has_bits = true;
+    }
+    is_dense = true;
+  }
+  bool in(int64_t v) const { return bits[v] != 0; }
+  template <class Fn> void for_each(Fn fn) {  // vertexMap (ligra.h:478-493)
+    if (is_dense) {
+#pragma omp parallel for
+      for (int64_t i = 0; i < n; i++) if (bits[i]) fn((uint32_t)i);
+    } else {
+#pragma omp parallel for
+      for (int64_t i = 0; i < (int64_t)ids.size(); i++) fn(ids[i]);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// edgeMap (ligra.h:277-316 mode switch; 130-196 sparse push; 90-128 dense
+// push; 61-88 dense pull with vertex.h:12-41 early exit).
+//
+// The functor F provides:
+//   bool cond(uint32_t d)
+//   void update(uint32_t s, uint32_t d)              pull, non-atomic
+//   void update_atomic(uint32_t s, uint32_t d, int tid)  push
+//   void merge()                                     mergeDuplicates
+//   uint8_t* next                                    next byte map or nullptr
+// ---------------------------------------------------------------------------
+template <class F>
+Frontier edge_map(const Csr& g, Frontier& fr, F& f, int64_t threshold, bool output,
+                  bool dense_forward) {
+  const int64_t n = g.n;
+  if (threshold == -1) threshold = g.m / 20;  // ligra.h:283
+  if (fr.count == 0) return Frontier::from_ids(n, {});
+  fr.to_sparse();
+  int64_t k = (int64_t)fr.ids.size();
+  int64_t out_deg = 0;
+#pragma omp parallel for reduction(+ : out_deg)
+  for (int64_t i = 0; i < k; i++) out_deg += g.deg(fr.ids[i]);
+  if (out_deg == 0) return Frontier::from_ids(n, {});  // ligra.h:301
+  if (k + out_deg > threshold) {
+    fr.to_dense();
+    if (output) {
+#pragma omp parallel for
+      for (int64_t i = 0; i < n; i++) f.next[i] = 0;
+    }
+    if (dense_forward) {  // edgeMapDenseForward
+#pragma omp parallel for schedule(dynamic, 64)
+      for (int64_t s = 0; s < n; s++) {
+        if (!fr.in(s)) continue;
+        int tid = omp_get_thread_num();
+        for (uint32_t j = g.off[s]; j < g.off[s + 1]; j++) {
+          uint32_t d = g.adj[j];
+          if (f.cond(d)) f.update_atomic((uint32_t)s, d, tid);
+        }
+      }
+      f.merge();
+    } else {  // edgeMapDense (pull); symmetric graphs: in-edges == out-edges
+#pragma omp parallel for schedule(dynamic, 64)
+      for (int64_t v = 0; v < n; v++) {
+        if (!f.cond((uint32_t)v)) continue;
+        for (uint32_t j = g.off[v]; j < g.off[v + 1]; j++) {
+          uint32_t u = g.adj[j];
+          if (fr.in(u)) f.update(u, (uint32_t)v);
+          if (!f.cond((uint32_t)v)) break;
+        }
+      }
+    }
+  } else {  // edgeMapSparse
+    if (output) {
+#pragma omp parallel for
+      for (int64_t i = 0; i < n; i++) f.next[i] = 0;
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < k; i++) {
+      uint32_t s = fr.ids[i];
+      int tid = omp_get_thread_num();
+      for (uint32_t j = g.off[s]; j < g.off[s + 1]; j++) {
+        uint32_t d = g.adj[j];
+        if (f.cond(d)) f.update_atomic(s, d, tid);
+      }
+    }
+    f.merge();
+    if (output) {  // compact the next byte map into an id list (ligra.h:161-192)
+      return Frontier::from_ids(n, pack_indices(f.next, n));
+    }
+    return Frontier::from_ids(n, {});
+  }
+  if (output) return Frontier::from_bits(n, std::vector<uint8_t>(f.next, f.next + n));
+  return Frontier::from_ids(n, {});
+}
+
+// ---------------------------------------------------------------------------
+// Hub duplication (RADAR: hub <=> d < numHubs, PageRank.C:42-53; hubdup:
+// hub <=> bit set in a bitmap, index through idxMap, hubdup/.../IO.h:720-804).
+// numHubs = llcCap / (T*elem [+extra]) with llcCap = 1<<25 (PageRank.C:148-149,
+// BFS.C:144-145, BC-manyiter-v2.C:232-233, Radii.C:172-173).  The reference
+// reads and writes out of bounds when numHubs > n; this restatement caps it.
+// ---------------------------------------------------------------------------
+struct Hubs {
+  int64_t count = 0;                 // number of hub slots
+  std::vector<int32_t> slot_of;      // hubdup only: vertex -> slot or -1
+  std::vector<uint32_t> vertex_of;   // slot -> vertex
+  bool by_map = false;
+  int32_t slot(uint32_t d) const {
+    if (by_map) return slot_of[d];
+    return (int64_t)d < count ? (int32_t)d : -1;
+  }
+};
+
+Hubs make_hubs(const Csr& g, int variant, int nthreads, size_t elem, size_t extra) {
+  Hubs h;
+  if (variant != kHubDup && variant != kRadar) return h;
+  const int64_t llc = 1 << 25;
+  int64_t num = llc / (int64_t)(nthreads * elem + extra);
+  if (variant == kRadar) {
+    h.count = std::min<int64_t>(num, g.n);
+    h.vertex_of.resize(h.count);
+    for (int64_t i = 0; i < h.count; i++) h.vertex_of[i] = (uint32_t)i;
+    return h;
+  }
+  // hubdup identifyHubs: threshold = sorted_degree[numHubs]; hubs are deg > thresh.
+  std::vector<uint32_t> degs(g.n);
+  for (int64_t v = 0; v < g.n; v++) degs[v] = g.deg(v);
+  std::sort(degs.begin(), degs.end(), std::greater<uint32_t>());
+  num = std::min<int64_t>(num, g.n - 1);
+  uint32_t thresh = num >= 0 ? degs[num] : 0;
+  h.by_map = true;
+  h.slot_of.assign(g.n, -1);
+  for (int64_t v = 0; v < g.n; v++) {
+    if (g.deg(v) > thresh) {
+      h.slot_of[v] = (int32_t)h.vertex_of.size();
+      h.vertex_of.push_back((uint32_t)v);
+    }
+  }
+  h.count = (int64_t)h.vertex_of.size();
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// PageRank (PageRank.C:29-189).
+// ---------------------------------------------------------------------------
+struct PrF {
+  const Csr* g; double* p_curr; double* p_next; uint8_t* next = nullptr;
+  const Hubs* hubs; std::vector<std::vector<double>>* dup;
+  bool cond(uint32_t) const { return true; }
+  void update(uint32_t s, uint32_t d) { p_next[d] += p_curr[s] / g->deg(s); }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int32_t h = hubs->slot(d);
+    if (h >= 0) (*dup)[tid][h] += p_curr[s] / g->deg(s);
+    else add_f64(&p_next[d], p_curr[s] / g->deg(s));
+  }
+  void merge() {
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      uint32_t d = hubs->vertex_of[h];
+      for (int t = 0; t < T; t++) { p_next[d] += (*dup)[t][h]; (*dup)[t][h] = 0.0; }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// BFS (BFS.C:28-188; push-pull variant src/push-pull/Ligra/apps/BFS.C:28-48).
+// ---------------------------------------------------------------------------
+struct BfsF {
+  uint32_t* parents; uint8_t* next;
+  const Hubs* hubs; std::vector<std::vector<uint32_t>>* dup;
+  std::vector<uint8_t>* do_merge; bool pull_cond;
+  bool cond(uint32_t d) const { return pull_cond ? parents[d] == kNone : true; }
+  void update(uint32_t s, uint32_t d) {
+    if (parents[d] == kNone) { parents[d] = s; next[d] = 1; }
+  }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int32_t h = hubs->slot(d);
+    if (h >= 0) {
+      if ((*dup)[tid][h] == kNone) {
+        (*dup)[tid][h] = s;
+        __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+      }
+    } else if (parents[d] == kNone) {
+      if (cas_u32(&parents[d], kNone, s)) next[d] = 1;
+    }
+  }
+  void merge() {  // BFS.C:69-94: first non-MAX private copy wins
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      if (!(*do_merge)[h]) continue;
+      (*do_merge)[h] = 0;
+      uint32_t d = hubs->vertex_of[h];
+      if (parents[d] != kNone) continue;
+      for (int t = 0; t < T; t++) {
+        if ((*dup)[t][h] != kNone) { parents[d] = (*dup)[t][h]; next[d] = 1; break; }
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// BC (BC-manyiter-v2.C:32-183).
+// ---------------------------------------------------------------------------
+struct BcF {
+  double* num_paths; uint8_t* visited; uint8_t* next;
+  const Hubs* hubs; std::vector<std::vector<double>>* dup; std::vector<uint8_t>* do_merge;
+  bool cond(uint32_t d) const { return visited[d] == 0; }
+  void update(uint32_t s, uint32_t d) {
+    double o = num_paths[d];
+    num_paths[d] += num_paths[s];
+    if (o == 0.0) next[d] = 1;
+  }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int32_t h = hubs->slot(d);
+    if (h >= 0) {
+      (*dup)[tid][h] += num_paths[s];
+      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+    } else {
+      double o = add_f64_old(&num_paths[d], num_paths[s]);
+      if (o == 0.0) next[d] = 1;
+    }
+  }
+  void merge() {
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      if (!(*do_merge)[h]) continue;
+      (*do_merge)[h] = 0;
+      uint32_t d = hubs->vertex_of[h];
+      bool upd = false;
+      for (int t = 0; t < T; t++) {
+        num_paths[d] += (*dup)[t][h];
+        if ((*dup)[t][h] != 0.0) { upd = true; (*dup)[t][h] = 0.0; }
+      }
+      if (upd) next[d] = 1;
+    }
+  }
+};
+
+struct BcBackF {
+  double* deps; uint8_t* visited; uint8_t* next = nullptr;
+  const Hubs* hubs; std::vector<std::vector<double>>* dup; std::vector<uint8_t>* do_merge;
+  bool cond(uint32_t d) const { return visited[d] == 0; }
+  void update(uint32_t s, uint32_t d) { deps[d] += deps[s]; }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int32_t h = hubs->slot(d);
+    if (h >= 0) {
+      (*dup)[tid][h] += deps[s];
+      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+    } else {
+      add_f64(&deps[d], deps[s]);
+    }
+  }
+  void merge() {
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      if (!(*do_merge)[h]) continue;
+      (*do_merge)[h] = 0;
+      uint32_t d = hubs->vertex_of[h];
+      for (int t = 0; t < T; t++) { deps[d] += (*dup)[t][h]; (*dup)[t][h] = 0.0; }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Radii (Radii.C:37-117).
+// ---------------------------------------------------------------------------
+struct RadiiF {
+  int64_t* visited; int64_t* next_visited; int32_t* radii; int32_t round; uint8_t* next;
+  const Hubs* hubs; std::vector<std::vector<int64_t>>* dup; std::vector<uint8_t>* do_merge;
+  bool cond(uint32_t) const { return true; }
+  void update(uint32_t s, uint32_t d) {
+    int64_t w = visited[d] | visited[s];
+    if (visited[d] != w) {
+      next_visited[d] |= w;
+      if (radii[d] != round) { radii[d] = round; next[d] = 1; }
+    }
+  }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int64_t w = visited[d] | visited[s];
+    if (visited[d] == w) return;
+    int32_t h = hubs->slot(d);
+    if (h >= 0) {
+      (*dup)[tid][h] |= w;
+      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+    } else {
+      or_i64(&next_visited[d], w);
+    }
+    int32_t old = radii[d];
+    if (old != round && cas_i32(&radii[d], old, round)) next[d] = 1;
+  }
+  void merge() {
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      if (!(*do_merge)[h]) continue;
+      (*do_merge)[h] = 0;
+      uint32_t d = hubs->vertex_of[h];
+      for (int t = 0; t < T; t++) {
+        if ((*dup)[t][h]) { next_visited[d] |= (*dup)[t][h]; (*dup)[t][h] = 0; }
+      }
+    }
+  }
+};
+
+struct ThreadScope {
+  int saved;
+  explicit ThreadScope(int t) : saved(omp_get_max_threads()) { if (t > 0) omp_set_num_threads(t); }
+  ~ThreadScope() { omp_set_num_threads(saved); }
+};
+
+// Ligra's 64-bit hashInt (utils.h:350-358); a published integer mixing hash
+// whose constants decide which vertices Radii samples, so they must match.
+inline uint64_t hash_u64(uint64_t a) {
+  a = (a + 0x7ed55d166bef7a1dULL) + (a << 12);
+  a = (a ^ 0xc761c23c510fa2ddULL) ^ (a >> 9);
+  a = (a + 0x165667b183a9c0e1ULL) + (a << 59);
+  a = (a + 0xd3a2646cab3487e3ULL) ^ (a << 49);
+  a = (a + 0xfd7046c5ef9ab54cULL) + (a << 3);
+  a = (a ^ 0xb55a4f090dd4a67bULL) ^ (a >> 32);
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Symmetric-graph clean-up of the Ligra text loader (IO.h:429-474): for every
+// vertex sort its neighbour list, drop duplicates and self-loops, repack.
+// `off` has n entries (start offsets, as in the AdjacencyGraph file).
+// Returns the new edge count; out_off has n+1 entries.
+int64_t orc_dedup_symmetric(int64_t n, int64_t m, const uint32_t* off, const uint32_t* adj,
+                            uint32_t* out_off, uint32_t* out_adj) {
+  std::vector<uint32_t> tmp(adj, adj + m);
+  std::vector<uint32_t> nd(n);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; i++) {
+    uint32_t b = off[i], e = (i == n - 1) ? (uint32_t)m : off[i + 1];
+    uint32_t* s = tmp.data() + b;
+    std::sort(s, tmp.data() + e);
+    uint32_t* ne = std::unique(s, tmp.data() + e);
+    ne = std::remove(s, ne, (uint32_t)i);
+    nd[i] = (uint32_t)(ne - s);
+  }
+  uint64_t acc = 0;
+  for (int64_t i = 0; i < n; i++) { out_off[i] = (uint32_t)acc; acc += nd[i]; }
+  out_off[n] = (uint32_t)acc;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; i++) memcpy(out_adj + out_off[i], tmp.data() + off[i], 4ull * nd[i]);
+  return (int64_t)acc;
+}
+
+// Degree sort of a symmetric graph (IO.h:843-895): sort (degree, id) pairs with
+// std::greater -- degree descending, ties by DEScending original id -- and give
+// rank r to the r-th pair.  Neighbour lists are relabelled but keep their order.
+void orc_degree_sort(int64_t n, const uint32_t* off, const uint32_t* adj, uint32_t* new_ids,
+                     uint32_t* new_off, uint32_t* new_adj) {
+  std::vector<std::pair<uint32_t, uint32_t>> p(n);
+  for (int64_t v = 0; v < n; v++) p[v] = {off[v + 1] - off[v], (uint32_t)v};
+  std::sort(p.begin(), p.end(), std::greater<std::pair<uint32_t, uint32_t>>());
+  for (int64_t r = 0; r < n; r++) new_ids[p[r].second] = (uint32_t)r;
+  uint64_t acc = 0;
+  for (int64_t r = 0; r < n; r++) { new_off[r] = (uint32_t)acc; acc += p[r].first; }
+  new_off[n] = (uint32_t)acc;
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < n; v++) {
+    uint32_t r = new_ids[v];
+    uint32_t o = new_off[r];
+    for (uint32_t j = off[v]; j < off[v + 1]; j++) new_adj[o + (j - off[v])] = new_ids[adj[j]];
+  }
+}
+
+// PageRank Compute (PageRank.C:120-189).  push-pull passes threshold 0 and no
+// dense_forward (src/push-pull/Ligra/apps/PageRank.C:122), i.e. always pull.
+// `ranks` receives the final rank vector: p_curr after a run that used all
+// max_iters iterations (the last swap leaves the ranks there), p_next after an
+// L1 < 1e-7 break.
+int orc_pagerank(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
+                 int64_t max_iters, int nthreads, double* ranks, int64_t* iters_out,
+                 double* l1_out) {
+  ThreadScope ts(nthreads);
+  Csr g{n, (int64_t)off[n], off, adj};
+  const double damping = 0.85, eps = 0.0000001;
+  std::vector<double> a(n, 1.0 / (double)n), b(n, 0.0);
+  double* p_curr = a.data();
+  double* p_next = b.data();
+  int T = omp_get_max_threads();
+  Hubs hubs = make_hubs(g, variant, T, sizeof(double), variant == kHubDup ? 5 : 0);
+  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  Frontier fr = Frontier::all(n);
+  const double added = (1 - damping) * (1 / (double)n);
+  int64_t iter = 0;
+  double l1 = 0.0;
+  bool broke = false;
+  while (iter++ < max_iters) {
+    PrF f{&g, p_curr, p_next, nullptr, &hubs, &dup};
+    if (variant == kPushPull) edge_map(g, fr, f, 0, false, false);
+    else edge_map(g, fr, f, -1, false, true);
+    fr.for_each([&](uint32_t i) { p_next[i] = damping * p_next[i] + added; });
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) p_curr[i] = fabs(p_curr[i] - p_next[i]);
+    l1 = 0.0;
+#pragma omp parallel for reduction(+ : l1)
+    for (int64_t i = 0; i < n; i++) l1 += p_curr[i];
+    if (l1 < eps) { broke = true; break; }
+    fr.for_each([&](uint32_t i) { p_curr[i] = 0.0; });
+    std::swap(p_curr, p_next);
+  }
+  memcpy(ranks, broke ? p_next : p_curr, 8 * n);
+  if (iters_out) *iters_out = iter;
+  if (l1_out) *l1_out = l1;
+  return 0;
+}
+
+// BFS Compute (BFS.C:122-188).  `root` is an internal id.  Parents are internal
+// ids, UINT32_MAX for unreached.  rounds_out = number of edgeMap calls.
+int orc_bfs(int64_t n, const uint32_t* off, const uint32_t* adj, int variant, uint32_t root,
+            int nthreads, uint32_t* parents, int64_t* rounds_out) {
+  ThreadScope ts(nthreads);
+  Csr g{n, (int64_t)off[n], off, adj};
+  for (int64_t i = 0; i < n; i++) parents[i] = kNone;
+  parents[root] = root;
+  int T = omp_get_max_threads();
+  Hubs hubs = make_hubs(g, variant, T, sizeof(uint32_t), 1 + (variant == kHubDup ? 5 : 0));
+  std::vector<std::vector<uint32_t>> dup(hubs.count ? T : 0,
+                                         std::vector<uint32_t>(hubs.count, kNone));
+  // RADAR seeds the private copies from Parents (BFS.C:154-156); with hub
+  // slot == vertex id that marks the root's slot as already set, which is
+  // harmless because the root already has its parent.
+  std::vector<uint8_t> do_merge(hubs.count, 0);
+  std::vector<uint8_t> next(n, 0);
+  Frontier fr = Frontier::single(n, root);
+  int64_t rounds = 0;
+  while (fr.count > 0) {
+    BfsF f{parents, next.data(), &hubs, &dup, &do_merge, variant == kPushPull};
+    fr = edge_map(g, fr, f, -1, true, variant != kPushPull);
+    rounds++;
+  }
+  if (rounds_out) *rounds_out = rounds;
+  return 0;
+}
+
+// BC Compute (BC-manyiter-v2.C:205-352) over the given source list (internal
+// ids, already picked).  `deps` is zeroed once and chained across sources,
+// exactly as the reference does: each source's final transform
+// D = (D - 1/sigma) / (1/sigma) feeds the next source's backward phase.
+int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
+           const uint32_t* sources, int nsrc, int nthreads, double* deps, int64_t* levels_out) {
+  ThreadScope ts(nthreads);
+  Csr g{n, (int64_t)off[n], off, adj};
+  int T = omp_get_max_threads();
+  Hubs hubs = make_hubs(g, variant, T, sizeof(double), 1 + (variant == kHubDup ? 5 : 0));
+  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  std::vector<uint8_t> do_merge(hubs.count, 0);
+  std::vector<double> num_paths(n);
+  std::vector<uint8_t> visited(n), next(n);
+  for (int64_t i = 0; i < n; i++) deps[i] = 0.0;
+  int64_t total_levels = 0;
+  for (int it = 0; it < nsrc; it++) {
+    uint32_t start = sources[it];
+    std::fill(num_paths.begin(), num_paths.end(), 0.0);
+    num_paths[start] = 1.0;
+    std::fill(visited.begin(), visited.end(), 0);
+    visited[start] = 1;
+    std::vector<Frontier> levels;
+    Frontier fr = Frontier::single(n, start);
+    levels.push_back(fr);
+    int64_t round = 0;
+    while (fr.count > 0) {
+      round++;
+      BcF f{num_paths.data(), visited.data(), next.data(), &hubs, &dup, &do_merge};
+      Frontier out = edge_map(g, fr, f, -1, true, variant != kPushPull);
+      out.for_each([&](uint32_t i) { visited[i] = 1; });
+      levels.push_back(out);
+      fr = out;
+    }
+    total_levels += round;
+    std::vector<double>& inv = num_paths;  // inverted in place (BC-manyiter-v2.C:324-325)
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) inv[i] = 1 / inv[i];
+    std::fill(visited.begin(), visited.end(), 0);
+    auto back_vertex = [&](uint32_t i) { visited[i] = 1; deps[i] += inv[i]; };
+    Frontier cur = levels[round - 1];
+    cur.for_each(back_vertex);
+    for (int64_t r = round - 2; r >= 0; r--) {
+      BcBackF f{deps, visited.data(), nullptr, &hubs, &dup, &do_merge};
+      edge_map(g, cur, f, -1, false, variant != kPushPull);
+      cur = levels[r];
+      cur.for_each(back_vertex);
+    }
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) deps[i] = (deps[i] - inv[i]) / inv[i];
+  }
+  if (levels_out) *levels_out = total_levels;
+  return 0;
+}
+
+// Radii Compute (Radii.C:140-218).  seeds[i] is the internal id that gets bit i
+// (hashInt(i) % n mapped through new_ids).  When two seeds collide the seeding
+// loop's plain store leaves one bit; this restatement keeps the bit of the
+// larger i, which is what the reference does with one thread.
+int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
+              const uint32_t* seeds, int nseeds, int nthreads, int32_t* radii,
+              int64_t* rounds_out) {
+  ThreadScope ts(nthreads);
+  Csr g{n, (int64_t)off[n], off, adj};
+  std::vector<int64_t> visited(n, 0), next_visited(n, 0);
+  for (int64_t i = 0; i < n; i++) radii[i] = -1;
+  std::vector<uint32_t> starts(nseeds);
+  for (int i = 0; i < nseeds; i++) {
+    uint32_t v = seeds[i];
+    radii[v] = 0;
+    starts[i] = v;
+    next_visited[v] = (int64_t)(1ULL << i);
+  }
+  int T = omp_get_max_threads();
+  Hubs hubs = make_hubs(g, variant, T, sizeof(int64_t), 1 + (variant == kHubDup ? 5 : 0));
+  std::vector<std::vector<int64_t>> dup(hubs.count ? T : 0, std::vector<int64_t>(hubs.count, 0));
+  std::vector<uint8_t> do_merge(hubs.count, 0);
+  std::vector<uint8_t> next(n, 0);
+  Frontier fr = Frontier::from_ids(n, starts);
+  int32_t round = 0;
+  while (fr.count > 0) {
+    round++;
+    fr.for_each([&](uint32_t i) { visited[i] = next_visited[i]; });
+    RadiiF f{visited.data(), next_visited.data(), radii, round, next.data(), &hubs, &dup,
+             &do_merge};
+    fr = edge_map(g, fr, f, -1, true, variant != kPushPull);
+  }
+  if (rounds_out) *rounds_out = round;
+  return 0;
+}
+
+// BC source selection (BC-manyiter-v2.C:253-271, 279-280): mt19937 seeded with
+// 27491095, uniform_int_distribution<long>(0, n-1), redrawn while the vertex has
+// degree 0; draws are original ids, mapped through new_ids when the graph was
+// degree-sorted.  `deg_orig` is the degree by ORIGINAL id.
+void orc_bc_sources(int64_t n, const uint32_t* deg_orig, int k, uint32_t* out_orig) {
+  std::mt19937 rng(27491095);
+  std::uniform_int_distribution<long> ud(0, n - 1);
+  for (int i = 0; i < k; i++) {
+    long s;
+    do { s = ud(rng); } while (deg_orig[s] == 0);
+    out_orig[i] = (uint32_t)s;
+  }
+}
+
+// Radii seeds (Radii.C:159-169): vertex hashInt((ulong)i) % n for i < min(n,64).
+int orc_radii_seeds(int64_t n, uint32_t* out_orig) {
+  int k = (int)std::min<int64_t>(n, 64);
+  for (int i = 0; i < k; i++) out_orig[i] = (uint32_t)(hash_u64((uint64_t)i) % (uint64_t)n);
+  return k;
+}
+
+// BFS depths from a parent array (used to compare BFS results bit-exactly).
+void orc_depths_from_parents(int64_t n, const uint32_t* parents, int32_t* depth) {
+  for (int64_t i = 0; i < n; i++) depth[i] = -2;
+  for (int64_t i = 0; i < n; i++) {
+    if (parents[i] == kNone) { depth[i] = -1; continue; }
+    // walk up until a known depth or the root
+    int64_t v = i, steps = 0;
+    while (depth[v] == -2 && parents[v] != (uint32_t)v && steps <= n) { v = parents[v]; steps++; }
+    int32_t base = depth[v] >= 0 ? depth[v] : (parents[v] == (uint32_t)v ? 0 : -3);
+    if (depth[v] == -2) depth[v] = base;
+    // second pass assigns depths along the path
+    int64_t u = i; int32_t d = base + (int32_t)steps;
+    while (u != v) { depth[u] = d--; u = parents[u]; }
+  }
+}
+
+// Reference BFS depths by a plain serial level-synchronous BFS (textbook), the
+// bit-exact quantity all variants agree on.
+void orc_bfs_depths(int64_t n, const uint32_t* off, const uint32_t* adj, uint32_t root,
+                    int32_t* depth) {
+  for (int64_t i = 0; i < n; i++) depth[i] = -1;
+  std::vector<uint32_t> q; q.reserve(n);
+  depth[root] = 0; q.push_back(root);
+  for (size_t h = 0; h < q.size(); h++) {
+    uint32_t u = q[h];
+    for (uint32_t j = off[u]; j < off[u + 1]; j++) {
+      uint32_t v = adj[j];
+      if (depth[v] < 0) { depth[v] = depth[u] + 1; q.push_back(v); }
+    }
+  }
+}
+
+}  // extern "C"

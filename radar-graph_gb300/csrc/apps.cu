@@ -1,0 +1,1038 @@
+// App drivers (Compute of PageRank.C, BFS.C, BC-manyiter-v2.C, Radii.C) on
+// the device engine, and the engine-level C ABI (rg_edgemap/rg_vertexmap).
+//
+// Every app keeps its arrays resident in HBM for the whole call, reads back
+// only the per-level frontier size (one 16-byte copy per level, the same
+// information the reference's edgeMapData gathers to choose a mode), and
+// copies the result to the host once at the end.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <functional>
+#include <random>
+#include <vector>
+
+#include "engine.cuh"
+#include "rg_device.cuh"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// per-call timing and launch accounting
+// ---------------------------------------------------------------------------
+static thread_local rg_timing g_timing;
+
+struct CallTimer {
+  rg_graph* g;
+  explicit CallTimer(rg_graph* gr) : g(gr) {
+    memset(&g_timing, 0, sizeof g_timing);
+    cudaEventRecord(g->ev0, g->stream);
+  }
+  rg_status stop() {
+    RG_CUDA(cudaEventRecord(g->ev1, g->stream));
+    RG_CUDA(cudaEventSynchronize(g->ev1));
+    float ms = 0;
+    RG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+    g_timing.total_ms = ms;
+    return RG_OK;
+  }
+};
+
+static int device_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+static int max_dyn_smem() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// hubs (RADAR: ids < H after degree sort; HUBDUP: identifyHubs,
+// hubdup/Ligra/ligra/IO.h:720-804, threshold = sorted_degree[H], hub iff
+// degree > threshold)
+// ---------------------------------------------------------------------------
+struct HubCache {
+  const rg_graph* g = nullptr;
+  uint32_t requested = 0;  // H asked for
+  uint32_t H = 0;          // hubs found (degree > sorted_degree[requested])
+  DevBuf bits, slot, vertex;
+};
+static std::vector<HubCache*> g_hub_cache;
+
+// Hub slots that fit the shared-memory budget for an element of `elem` bytes
+// next to the push kernel's static staging arrays.
+static uint32_t hub_budget(size_t elem, int64_t n) {
+  size_t static_bytes = 3 * sizeof(uint32_t) * (kHubPushThreads * kPushItems + 1) + 64;
+  size_t dyn = (size_t)max_dyn_smem() - static_bytes - 1024;
+  uint64_t h = dyn / elem;
+  return (uint32_t)std::min<uint64_t>(h, (uint64_t)n);
+}
+
+static rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
+  HubCache* hc = nullptr;
+  for (HubCache* c : g_hub_cache) if (c->g == g && c->requested == H) hc = c;
+  if (!hc) {
+    std::vector<uint32_t> d(g->h_deg);
+    std::sort(d.begin(), d.end(), std::greater<uint32_t>());
+    uint32_t thresh = H < (uint32_t)g->n ? d[H] : 0;
+    int64_t nwords = (g->n + 31) / 32;
+    std::vector<uint32_t> bits(nwords, 0), slot(g->n, 0), vert;
+    for (int64_t v = 0; v < g->n; v++) {
+      if (g->h_deg[v] > thresh) {
+        bits[v >> 5] |= 1u << (v & 31);
+        slot[v] = (uint32_t)vert.size();
+        vert.push_back((uint32_t)v);
+      }
+    }
+    hc = new HubCache();
+    hc->g = g;
+    hc->requested = H;
+    hc->H = (uint32_t)vert.size();
+    rg_status s;
+    if ((s = hc->bits.reserve(4 * nwords)) != RG_OK || (s = hc->slot.reserve(4 * g->n)) != RG_OK ||
+        (s = hc->vertex.reserve(4 * (vert.size() + 1))) != RG_OK) {
+      delete hc;
+      return s;
+    }
+    RG_CUDA(cudaMemcpy(hc->bits.p, bits.data(), 4 * nwords, cudaMemcpyHostToDevice));
+    RG_CUDA(cudaMemcpy(hc->slot.p, slot.data(), 4 * g->n, cudaMemcpyHostToDevice));
+    if (!vert.empty()) RG_CUDA(cudaMemcpy(hc->vertex.p, vert.data(), 4 * vert.size(), cudaMemcpyHostToDevice));
+    g_hub_cache.push_back(hc);
+  }
+  info.H = hc->H;
+  info.bits = hc->bits.as<uint32_t>();
+  info.slot = hc->slot.as<uint32_t>();
+  info.vertex = hc->vertex.as<uint32_t>();
+  return RG_OK;
+}
+
+void drop_hub_cache(const rg_graph* g) {
+  for (auto it = g_hub_cache.begin(); it != g_hub_cache.end();) {
+    if ((*it)->g == g) { delete *it; it = g_hub_cache.erase(it); }
+    else ++it;
+  }
+}
+
+static int hub_mode_of(int variant) {
+  return variant == RG_RADAR ? kHubPrefix : variant == RG_HUBDUP ? kHubMap : kHubNone;
+}
+
+// ---------------------------------------------------------------------------
+// frontier views and the edgeMap driver (edgeMapData, ligra.h:277-316)
+// ---------------------------------------------------------------------------
+struct FView {
+  uint32_t* queue = nullptr;
+  uint32_t* qoff = nullptr;
+  uint32_t* bits = nullptr;
+  int64_t count = 0, degsum = 0;
+};
+
+static FView view_of(Frontier& f) {
+  return FView{f.queue.as<uint32_t>(), f.qoff.as<uint32_t>(), f.bits.as<uint32_t>(), f.count, f.degsum};
+}
+
+struct EmOpts {
+  int variant = RG_PUSH;
+  bool dense_forward = true;
+  int64_t threshold = -1;
+  uint32_t hub_h = 0;  // 0 = budget
+};
+
+// Frontiers below this many edges skip hub privatisation: the shared-memory
+// set-up and merge would cost more than the atomics they save.  Results do not
+// depend on it.
+constexpr int64_t kHubMinEdges = 1 << 16;
+
+template <class Op, int kHub>
+static rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo& hub, uint32_t* next_bits,
+                             cudaStream_t st) {
+  constexpr int kT = kHub == kHubNone ? kPushThreads : kHubPushThreads;
+  constexpr int kTile = kT * kPushItems;
+  auto kern = push_lbs<Op, kHub, kT>;
+  const int64_t tiles = (in.degsum + kTile - 1) / kTile;
+  size_t dyn = kHub == kHubNone ? 0 : sizeof(typename Op::HubT) * hub.H;
+  int grid;
+  if (kHub == kHubNone) {
+    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * 8);
+  } else {
+    static bool attr_set = false;
+    if (!attr_set) {
+      RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   max_dyn_smem() - 3 * 4 * (kTile + 1) - 64));
+      attr_set = true;
+    }
+    int per_sm = 0;
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kT, dyn));
+    if (per_sm < 1) per_sm = 1;
+    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * per_sm);
+  }
+  if (grid < 1) grid = 1;
+  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, (uint32_t)in.count, (uint32_t)in.degsum, op, hub,
+                              next_bits);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  g_timing.edge_launches++;
+  return RG_OK;
+}
+
+// One edgeMap.  `out` (may be null for no_output ops) receives the next
+// frontier: its bitmap is cleared, filled, then compacted (which syncs).
+template <class Op>
+static rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const EmOpts& o, cudaStream_t st,
+                          int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr) {
+  const int64_t nwords = (g->n + 31) / 32;
+  if (out) RG_CUDA(cudaMemsetAsync(out->bits, 0, 4 * nwords, st));
+  int64_t threshold = o.threshold == -1 ? g->m / 20 : o.threshold;
+  if (in.count > 0 && in.degsum > 0) {
+    g_timing.edges_traversed += in.degsum;
+    const bool dense = in.count + in.degsum > threshold;
+    uint32_t* nb = out ? out->bits : nullptr;
+    if (dense && !o.dense_forward) {
+      const int64_t groups_per_block = 256 / 8;
+      int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
+      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), in.bits, op, nb);
+      RG_CUDA(cudaGetLastError());
+      g_timing.kernel_launches++;
+      g_timing.edge_launches++;
+    } else {
+      int hm = in.degsum >= kHubMinEdges ? hub_mode_of(o.variant) : kHubNone;
+      HubInfo hub;
+      if (hm == kHubPrefix) {
+        hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
+                        : hub_budget(sizeof(typename Op::HubT), g->n);
+        RG_TRY(launch_push<Op, kHubPrefix>(g, in, op, hub, nb, st));
+      } else if (hm == kHubMap) {
+        uint32_t H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
+                             : hub_budget(sizeof(typename Op::HubT), g->n);
+        RG_TRY(hub_map(g, H, hub));
+        RG_TRY(launch_push<Op, kHubMap>(g, in, op, hub, nb, st));
+      } else {
+        RG_TRY(launch_push<Op, kHubNone>(g, in, op, hub, nb, st));
+      }
+    }
+  }
+  if (out) {
+    Frontier tmp;  // non-owning shell for compact_bits
+    tmp.bits.p = out->bits;
+    RG_TRY(compact_bits(g, tmp, st, true, depth, level, or_into, out->queue, out->qoff));
+    tmp.bits.p = nullptr;
+    out->count = tmp.count;
+    out->degsum = tmp.degsum;
+    g_timing.kernel_launches += 3;
+  }
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small vertex kernels
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void fill_kernel(T* a, int64_t n, T v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+template <class T>
+static void fill(T* a, int64_t n, T v, cudaStream_t st) {
+  int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
+  fill_kernel<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(a, n, v);
+  g_timing.kernel_launches++;
+}
+
+// out[v] = in[new_ids[v]]: results in original-id order (writeOutputToFile).
+template <class T>
+__global__ void gather_kernel(const T* __restrict__ in, const uint32_t* __restrict__ new_ids, int64_t n,
+                              T* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = in[new_ids[i]];
+}
+
+template <class T>
+static rg_status download_orig(rg_graph* g, const T* d_arr, T* h_out, DevBuf& tmp, cudaStream_t st) {
+  if (!h_out) return RG_OK;
+  const T* src = d_arr;
+  if (g->sorted) {
+    RG_TRY(tmp.reserve(sizeof(T) * g->n));
+    int64_t blocks = std::min<int64_t>((g->n + 255) / 256, (int64_t)device_sms() * 32);
+    gather_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(d_arr, g->new_ids.as<uint32_t>(), g->n, tmp.as<T>());
+    RG_CUDA(cudaGetLastError());
+    g_timing.kernel_launches++;
+    src = tmp.as<T>();
+  }
+  RG_CUDA(cudaMemcpyAsync(h_out, src, sizeof(T) * g->n, cudaMemcpyDeviceToHost, st));
+  return RG_OK;
+}
+
+static uint32_t to_internal(const rg_graph* g, uint32_t orig) {
+  return g->sorted ? g->h_new_ids[orig] : orig;
+}
+
+// ---------------------------------------------------------------------------
+// PageRank (PageRank.C:120-189)
+// ---------------------------------------------------------------------------
+constexpr double kDamping = 0.85;
+constexpr int kSweepThreads = 1024;
+constexpr double kEpsilon = 0.0000001;
+
+__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p_curr, double* acc, double* contrib,
+                        double one_over_n) {
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    p_curr[v] = one_over_n;
+    acc[v] = 0.0;
+    uint32_t d = off[v + 1] - off[v];
+    contrib[v] = d ? one_over_n / (double)d : 0.0;
+  }
+}
+
+__device__ __forceinline__ bool pr_converged(const double* l1_prev) {
+  return l1_prev != nullptr && *l1_prev < kEpsilon;
+}
+
+// Dense push over every edge (edgeMapDenseForward with a full frontier):
+// acc[d] += contrib[s].  Each warp owns kSweepChunk consecutive edges read as
+// 16-byte vectors; chunk_v gives the chunk's first source so a lane finds its
+// source with a short search.
+template <int kHub>
+__global__ void __launch_bounds__(1024) pr_push_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                     uint32_t nchunks, const double* __restrict__ contrib,
+                                                     double* acc, HubInfo hub, const double* l1_prev) {
+  if (pr_converged(l1_prev)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* hs = reinterpret_cast<double*>(smem_raw);
+  if (kHub != kHubNone) {
+    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = 0.0;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / 128; r++) {
+      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+      if (e < g.m) {
+        const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+        uint32_t s = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[s + 1];
+        double cs = contrib[s];
+        const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {
+            do { s++; nxt = g.off[s + 1]; } while (ee >= nxt);
+            cs = contrib[s];
+          }
+          const uint32_t d = dd[i];
+          uint32_t slot;
+          if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) atomicAdd(hs + slot, cs);
+          else atomicAdd(acc + d, cs);
+        }
+      }
+    }
+  }
+  if (kHub != kHubNone) {
+    __syncthreads();
+    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) {
+      const double x = hs[h];
+      if (x != 0.0) atomicAdd(acc + hub_vertex<kHub>(hub, h), x);
+    }
+  }
+}
+
+// Dense pull over every vertex (edgeMapDense with a full frontier, push-pull
+// variant): acc[v] = sum over in-neighbours u of contrib[u].  Edge-balanced
+// like the push sweep; partial sums of a row are combined across the warp by
+// a segmented scan (rows are non-decreasing across lanes) and added once per
+// row piece.
+__global__ void __launch_bounds__(256) pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                     uint32_t nchunks, const double* __restrict__ contrib,
+                                                     double* acc, const double* l1_prev) {
+  if (pr_converged(l1_prev)) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / 128; r++) {
+      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+      uint32_t row = 0xFFFFFFFFu;
+      double part = 0.0;
+      if (e < g.m) {
+        const uint4 u4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+        uint32_t v = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[v + 1];
+        const uint32_t uu[4] = {u4.x, u4.y, u4.z, u4.w};
+        row = v;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {
+            atomicAdd(acc + row, part);  // a row piece that ends inside this lane
+            part = 0.0;
+            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+            row = v;
+          }
+          part += contrib[uu[i]];
+        }
+      }
+      // segmented inclusive scan of the lanes' last row pieces
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, part, o);
+        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
+        if (lane >= o && tr == row) part += t;
+      }
+      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
+      if (row != 0xFFFFFFFFu && (lane == 31 || next_row != row)) atomicAdd(acc + row, part);
+    }
+  }
+}
+
+// vertexMap(PR_Vertex_F) + the L1 step + reset, fused:
+//   p' = 0.85*acc + 0.15/n;  l1 += |p_curr - p'|;  acc = p';  p_curr = 0;
+//   contrib = p'/deg  (for the next iteration's edge pass)
+__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, double* acc,
+                                                   double* p_curr, double* contrib, double added, double* l1_out,
+                                                   const double* l1_prev) {
+  if (pr_converged(l1_prev)) return;
+  double local = 0.0;
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const double pn = kDamping * acc[v] + added;
+    local += fabs(p_curr[v] - pn);
+    acc[v] = pn;
+    p_curr[v] = 0.0;
+    const uint32_t d = off[v + 1] - off[v];
+    contrib[v] = d ? pn / (double)d : 0.0;
+  }
+  local = warp_sum(local);
+  __shared__ double ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < 8 ? ws[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) atomicAdd(l1_out, t);
+  }
+}
+
+struct PrState {
+  DevBuf a, b, contrib, l1, tmp;
+};
+
+rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
+                       double* l1_out, uint32_t hub_h, bool use_graph) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
+  if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
+  cudaStream_t st = g->stream;
+  const int64_t n = g->n;
+  static thread_local PrState S;
+  RG_TRY(S.a.reserve(8 * n));
+  RG_TRY(S.b.reserve(8 * n));
+  RG_TRY(S.contrib.reserve(8 * n));
+  RG_TRY(S.l1.reserve(8 * (max_iters + 1)));
+  CallTimer timer(g);
+  double* A = S.a.as<double>();
+  double* B = S.b.as<double>();
+  double* C = S.contrib.as<double>();
+  double* L1 = S.l1.as<double>();
+  RG_CUDA(cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st));
+  const int sms = device_sms();
+  const int vblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16);
+  pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, 1 / (double)n);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  const double added = (1 - kDamping) * (1 / (double)n);
+  // hub set-up
+  int hm = hub_mode_of(variant);
+  HubInfo hub;
+  size_t dyn = 0;
+  if (hm != kHubNone) {
+    uint32_t budget = hub_budget(sizeof(double), n);
+    uint32_t H = hub_h ? std::min(hub_h, budget) : budget;
+    if (hm == kHubPrefix) hub.H = H;
+    else RG_TRY(hub_map(g, H, hub));
+    dyn = sizeof(double) * hub.H;
+  }
+  auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
+                  : hm == kHubMap  ? pr_push_sweep<kHubMap>
+                                   : pr_push_sweep<kHubNone>;
+  int sweep_grid;
+  if (variant == RG_PUSH_PULL) {
+    int per_sm = 0;
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pr_pull_sweep, 256, 0));
+    sweep_grid = sms * std::max(per_sm, 1);
+  } else {
+    if (dyn) RG_CUDA(cudaFuncSetAttribute(sweep_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int per_sm = 0;
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_fn, kSweepThreads, dyn));
+    sweep_grid = sms * std::max(per_sm, 1);
+  }
+  const int sweep_threads = variant == RG_PUSH_PULL ? 256 : kSweepThreads;
+  sweep_grid = (int)std::min<int64_t>(sweep_grid,
+                                      std::max<int64_t>((g->nchunks * 32 + sweep_threads - 1) / sweep_threads, 1));
+  // iterations: acc alternates B, A, B, ... ; kernels of iteration i return at
+  // once when iteration i-1 already reached L1 < 1e-7 (device-side break)
+  double* acc = B;
+  double* cur = A;
+  for (int64_t it = 0; it < max_iters; it++) {
+    const double* prev = it ? L1 + it - 1 : nullptr;
+    if (g->m > 0) {
+      if (variant == RG_PUSH_PULL) {
+        pr_pull_sweep<<<sweep_grid, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C,
+                                                  acc, prev);
+      } else {
+        sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C, acc,
+                                               hub, prev);
+      }
+      RG_CUDA(cudaGetLastError());
+      g_timing.kernel_launches++;
+      g_timing.edge_launches++;
+    }
+    pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added, L1 + it, prev);
+    RG_CUDA(cudaGetLastError());
+    g_timing.kernel_launches++;
+    std::swap(acc, cur);
+  }
+  (void)use_graph;
+  std::vector<double> l1h(max_iters + 1, 0.0);
+  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, 8 * (max_iters + 1), cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  int64_t done = max_iters;
+  bool broke = false;
+  for (int64_t it = 0; it < max_iters; it++) {
+    if (l1h[it] < kEpsilon) { done = it; broke = true; break; }
+  }
+  // the ranks are the acc buffer of the last executed iteration
+  int64_t last = broke ? done : max_iters - 1;
+  const double* ranks = max_iters == 0 ? A : ((last % 2 == 0) ? B : A);
+  RG_TRY(download_orig<double>(g, ranks, h_ranks, S.tmp, st));
+  RG_TRY(timer.stop());
+  g_timing.edges_traversed = g->m * (broke ? done + 1 : max_iters);
+  g_timing.algorithmic_bytes = (4 * g->m + 4 * (n + 1) + 16 * n) * (broke ? done + 1 : max_iters);
+  if (iters_out) *iters_out = broke ? done + 1 : max_iters + 1;
+  if (l1_out) *l1_out = max_iters ? l1h[last] : 0.0;
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BFS (BFS.C:122-188)
+// ---------------------------------------------------------------------------
+__global__ void set_u32(uint32_t* a, uint32_t i, uint32_t v) { a[i] = v; }
+__global__ void set_i32(int32_t* a, uint32_t i, int32_t v) { a[i] = v; }
+
+struct BfsState {
+  DevBuf parents, depth, tmp;
+  Frontier f[2];
+};
+
+rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_parents, int32_t* h_depth,
+                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
+  if (root_orig >= (uint64_t)g->n) return fail(RG_EINVAL, "root %u >= n", root_orig);
+  cudaStream_t st = g->stream;
+  const int64_t n = g->n;
+  static thread_local BfsState S;
+  RG_TRY(S.parents.reserve(4 * n));
+  RG_TRY(S.depth.reserve(4 * n));
+  RG_TRY(frontier_alloc(g, S.f[0]));
+  RG_TRY(frontier_alloc(g, S.f[1]));
+  const uint32_t root = to_internal(g, root_orig);
+  CallTimer timer(g);
+  uint32_t* parents = S.parents.as<uint32_t>();
+  int32_t* depth = S.depth.as<int32_t>();
+  RG_CUDA(cudaMemsetAsync(parents, 0xFF, 4 * n, st));
+  RG_CUDA(cudaMemsetAsync(depth, 0xFF, 4 * n, st));
+  set_u32<<<1, 1, 0, st>>>(parents, root, root);
+  set_i32<<<1, 1, 0, st>>>(depth, root, 0);
+  g_timing.kernel_launches += 2;
+  RG_TRY(frontier_from_host(g, S.f[0], &root, 1, st));
+  FView cur = view_of(S.f[0]), nxt = view_of(S.f[1]);
+  EmOpts o;
+  o.variant = variant;
+  o.dense_forward = variant != RG_PUSH_PULL;
+  o.hub_h = hub_h;
+  int64_t rounds = 0, reached = 1;
+  OpBfs op{parents};
+  while (cur.count > 0) {
+    rounds++;
+    RG_TRY(edge_map(g, cur, op, &nxt, o, st, depth, (int32_t)rounds));
+    reached += nxt.count;
+    std::swap(cur, nxt);
+  }
+  RG_TRY(download_orig<uint32_t>(g, parents, h_parents, S.tmp, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  RG_TRY(download_orig<int32_t>(g, depth, h_depth, S.tmp, st));
+  RG_TRY(timer.stop());
+  // edges examined: the out-edges of every reached vertex (SURVEY byte model)
+  g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 4 * (n + 1) + 4 * n + 2 * ((n + 7) / 8) * rounds;
+  if (rounds_out) *rounds_out = rounds;
+  if (reached_out) *reached_out = reached;
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BC (BC-manyiter-v2.C:205-367)
+// ---------------------------------------------------------------------------
+__global__ void bc_invert(double* p, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = 1 / p[i];
+}
+// BC_Back_Vertex_F over a level queue: visited[i] = 1; deps[i] += inv[i].
+__global__ void bc_back_vertex(const uint32_t* __restrict__ q, int64_t k, uint32_t* visited, double* deps,
+                               const double* __restrict__ inv) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) {
+    uint32_t i = q[j];
+    atomicOr(visited + (i >> 5), 1u << (i & 31));
+    deps[i] += inv[i];
+  }
+}
+// Final transform (BC-manyiter-v2.C:347-349): D = (D - 1/sigma) / (1/sigma).
+__global__ void bc_final(double* deps, const double* __restrict__ inv, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) deps[i] = (deps[i] - inv[i]) / inv[i];
+}
+__global__ void set_f64(double* a, uint32_t i, double v) { a[i] = v; }
+
+struct BcState {
+  DevBuf num_paths, deps, visited, levels_q, levels_qo, bits0, bits1, tmp;
+};
+
+rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
+                 uint32_t hub_h) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
+  if (nsrc < 0 || (nsrc > 0 && !src_orig)) return fail(RG_EINVAL, "bad source list");
+  for (int i = 0; i < nsrc; i++) {
+    if (src_orig[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "source %u >= n", src_orig[i]);
+  }
+  cudaStream_t st = g->stream;
+  const int64_t n = g->n;
+  const int64_t nwords = (n + 31) / 32;
+  static thread_local BcState S;
+  RG_TRY(S.num_paths.reserve(8 * n));
+  RG_TRY(S.deps.reserve(8 * n));
+  RG_TRY(S.visited.reserve(4 * (nwords + 8)));
+  RG_TRY(S.levels_q.reserve(4 * (n + 64)));
+  RG_TRY(S.levels_qo.reserve(4 * (2 * n + 66)));
+  RG_TRY(S.bits0.reserve(4 * (nwords + 8)));
+  RG_TRY(S.bits1.reserve(4 * (nwords + 8)));
+  CallTimer timer(g);
+  double* np = S.num_paths.as<double>();
+  double* deps = S.deps.as<double>();
+  uint32_t* visited = S.visited.as<uint32_t>();
+  uint32_t* LQ = S.levels_q.as<uint32_t>();
+  uint32_t* LQO = S.levels_qo.as<uint32_t>();
+  RG_CUDA(cudaMemsetAsync(deps, 0, 8 * n, st));
+  EmOpts o;
+  o.variant = variant;
+  o.dense_forward = variant != RG_PUSH_PULL;
+  o.hub_h = hub_h;
+  const int vblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 16);
+  int64_t total_levels = 0;
+  std::vector<int64_t> lstart, lcount, ldeg;
+  for (int it = 0; it < nsrc; it++) {
+    const uint32_t start = to_internal(g, src_orig[it]);
+    RG_CUDA(cudaMemsetAsync(np, 0, 8 * n, st));
+    set_f64<<<1, 1, 0, st>>>(np, start, 1.0);
+    RG_CUDA(cudaMemsetAsync(visited, 0, 4 * nwords, st));
+    set_u32<<<1, 1, 0, st>>>(visited, start >> 5, 1u << (start & 31));
+    g_timing.kernel_launches += 2;
+    // level 0 = {start}
+    uint32_t q0[2] = {start, 0};
+    uint32_t qo0[2] = {0, g->h_deg[start]};
+    RG_CUDA(cudaMemcpyAsync(LQ, q0, 4, cudaMemcpyHostToDevice, st));
+    RG_CUDA(cudaMemcpyAsync(LQO, qo0, 8, cudaMemcpyHostToDevice, st));
+    RG_CUDA(cudaMemsetAsync(S.bits0.p, 0, 4 * nwords, st));
+    set_u32<<<1, 1, 0, st>>>(S.bits0.as<uint32_t>(), start >> 5, 1u << (start & 31));
+    RG_CUDA(cudaStreamSynchronize(st));  // q0/qo0 live on this stack frame
+    lstart.assign(1, 0);
+    lcount.assign(1, 1);
+    ldeg.assign(1, g->h_deg[start]);
+    FView cur{LQ, LQO, S.bits0.as<uint32_t>(), 1, (int64_t)g->h_deg[start]};
+    uint32_t* spare_bits = S.bits1.as<uint32_t>();
+    int64_t round = 0, qpos = 1;
+    OpBcFwd fop{np, visited};
+    while (cur.count > 0) {
+      round++;
+      FView nxt{LQ + qpos, LQO + qpos + round, spare_bits, 0, 0};
+      RG_TRY(edge_map(g, cur, fop, &nxt, o, st, nullptr, 0, visited));
+      spare_bits = cur.bits;
+      lstart.push_back(qpos);
+      lcount.push_back(nxt.count);
+      ldeg.push_back(nxt.degsum);
+      qpos += nxt.count;
+      cur = nxt;
+    }
+    total_levels += round;
+    bc_invert<<<vblocks, 256, 0, st>>>(np, n);
+    RG_CUDA(cudaMemsetAsync(visited, 0, 4 * nwords, st));
+    g_timing.kernel_launches++;
+    auto level_view = [&](int64_t r) {
+      return FView{LQ + lstart[r], LQO + lstart[r] + r, S.bits0.as<uint32_t>(), lcount[r], ldeg[r]};
+    };
+    auto back_vertex = [&](int64_t r) {
+      if (lcount[r] > 0) {
+        bc_back_vertex<<<(unsigned)((lcount[r] + 255) / 256), 256, 0, st>>>(LQ + lstart[r], lcount[r], visited, deps,
+                                                                          np);
+        g_timing.kernel_launches++;
+      }
+    };
+    back_vertex(round - 1);
+    OpBcBwd bop{deps, visited};
+    for (int64_t r = round - 2; r >= 0; r--) {
+      FView lv = level_view(r + 1);
+      const int64_t threshold = g->m / 20;
+      if (variant == RG_PUSH_PULL && lv.count + lv.degsum > threshold) {
+        // the pull path reads the level as a bitmap
+        Frontier shell;
+        shell.queue.p = lv.queue;
+        shell.bits.p = lv.bits;
+        shell.count = lv.count;
+        RG_TRY(frontier_bits_from_queue(g, shell, st));
+        shell.queue.p = nullptr;
+        shell.bits.p = nullptr;
+      }
+      RG_TRY(edge_map(g, lv, bop, nullptr, o, st));
+      back_vertex(r);
+    }
+    bc_final<<<vblocks, 256, 0, st>>>(deps, np, n);
+    RG_CUDA(cudaGetLastError());
+    g_timing.kernel_launches++;
+  }
+  RG_TRY(download_orig<double>(g, deps, h_deps, S.tmp, st));
+  RG_TRY(timer.stop());
+  g_timing.algorithmic_bytes =
+      4 * g_timing.edges_traversed + (int64_t)nsrc * (8 * (n + 1) + 8 * n + n + 16 * n + 8 * n);
+  if (levels_out) *levels_out = total_levels;
+  return RG_OK;
+}
+
+// BC source selection (BC-manyiter-v2.C:253-271): mt19937(27491095),
+// uniform_int_distribution<long>(0, n-1), redrawn while the vertex (original
+// id) has degree 0.
+rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
+  if (!g || k < 0 || (k > 0 && !out)) return fail(RG_EINVAL, "bad arguments");
+  bool any = false;
+  for (int64_t v = 0; v < g->n && !any; v++) any = g->h_deg[v] > 0;
+  if (!any && k > 0) return fail(RG_EINVAL, "graph has no edges; no BC source can be drawn");
+  std::mt19937 rng(27491095);
+  std::uniform_int_distribution<long> ud(0, g->n - 1);
+  for (int i = 0; i < k; i++) {
+    long s;
+    do { s = ud(rng); } while (g->h_deg[to_internal(g, (uint32_t)s)] == 0);
+    out[i] = (uint32_t)s;
+  }
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Radii (Radii.C:140-218)
+// ---------------------------------------------------------------------------
+__global__ void radii_sync(const uint32_t* __restrict__ q, int64_t k, unsigned long long* visited,
+                           const unsigned long long* __restrict__ next_visited) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) {
+    uint32_t i = q[j];
+    visited[i] = next_visited[i];
+  }
+}
+__global__ void radii_seed(const uint32_t* __restrict__ v, const unsigned long long* __restrict__ mask, int k,
+                           unsigned long long* next_visited, int32_t* radii) {
+  int j = threadIdx.x;
+  if (j < k) {
+    next_visited[v[j]] = mask[j];
+    radii[v[j]] = 0;
+  }
+}
+
+struct RadiiState {
+  DevBuf visited, next_visited, radii, seedv, seedm, tmp;
+  Frontier f[2];
+};
+
+rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k, int32_t* h_radii,
+                    int64_t* rounds_out, uint32_t hub_h) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
+  if (k < 0 || k > 64 || (k > 0 && !seeds_orig)) return fail(RG_EINVAL, "need 0..64 seeds");
+  cudaStream_t st = g->stream;
+  const int64_t n = g->n;
+  static thread_local RadiiState S;
+  RG_TRY(S.visited.reserve(8 * n));
+  RG_TRY(S.next_visited.reserve(8 * n));
+  RG_TRY(S.radii.reserve(4 * n));
+  RG_TRY(S.seedv.reserve(4 * 64));
+  RG_TRY(S.seedm.reserve(8 * 64));
+  RG_TRY(frontier_alloc(g, S.f[0]));
+  RG_TRY(frontier_alloc(g, S.f[1]));
+  // seeding loop (Radii.C:162-169): NextVisited[v] = 1<<i is a plain store, so
+  // on a collision the largest i wins (the single-thread order)
+  std::vector<uint32_t> starts(k), uv;
+  std::vector<unsigned long long> um;
+  for (int i = 0; i < k; i++) {
+    if (seeds_orig[i] >= (uint64_t)n) return fail(RG_EINVAL, "seed %u >= n", seeds_orig[i]);
+    uint32_t v = to_internal(g, seeds_orig[i]);
+    starts[i] = v;
+    auto it = std::find(uv.begin(), uv.end(), v);
+    if (it == uv.end()) { uv.push_back(v); um.push_back(1ull << i); }
+    else um[it - uv.begin()] = 1ull << i;
+  }
+  CallTimer timer(g);
+  unsigned long long* vis = S.visited.as<unsigned long long>();
+  unsigned long long* nvis = S.next_visited.as<unsigned long long>();
+  int32_t* radii = S.radii.as<int32_t>();
+  RG_CUDA(cudaMemsetAsync(vis, 0, 8 * n, st));
+  RG_CUDA(cudaMemsetAsync(nvis, 0, 8 * n, st));
+  RG_CUDA(cudaMemsetAsync(radii, 0xFF, 4 * n, st));
+  if (!uv.empty()) {
+    RG_CUDA(cudaMemcpyAsync(S.seedv.p, uv.data(), 4 * uv.size(), cudaMemcpyHostToDevice, st));
+    RG_CUDA(cudaMemcpyAsync(S.seedm.p, um.data(), 8 * um.size(), cudaMemcpyHostToDevice, st));
+    radii_seed<<<1, 64, 0, st>>>(S.seedv.as<uint32_t>(), S.seedm.as<unsigned long long>(), (int)uv.size(), nvis,
+                                 radii);
+    g_timing.kernel_launches++;
+  }
+  RG_TRY(frontier_from_host(g, S.f[0], starts.data(), k, st));  // keeps duplicates, like vertexSubset(n,64,starts)
+  FView cur = view_of(S.f[0]), nxt = view_of(S.f[1]);
+  EmOpts o;
+  o.variant = variant;
+  o.dense_forward = variant != RG_PUSH_PULL;
+  o.hub_h = hub_h;
+  int32_t round = 0;
+  while (cur.count > 0) {
+    round++;
+    radii_sync<<<(unsigned)((cur.count + 255) / 256), 256, 0, st>>>(cur.queue, cur.count, vis, nvis);
+    g_timing.kernel_launches++;
+    OpRadii op{vis, nvis, radii, round};
+    RG_TRY(edge_map(g, cur, op, &nxt, o, st));
+    std::swap(cur, nxt);
+  }
+  RG_TRY(download_orig<int32_t>(g, radii, h_radii, S.tmp, st));
+  RG_TRY(timer.stop());
+  g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 16 * n + 4 * n;
+  if (rounds_out) *rounds_out = round;
+  return RG_OK;
+}
+
+}  // namespace rg
+
+using namespace rg;
+
+extern "C" {
+
+rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
+                      double* l1_out) {
+  return pagerank_run(g, variant, max_iters, h_ranks, iters_out, l1_out, 0, false);
+}
+
+rg_status rg_bfs(rg_graph* g, rg_variant variant, uint32_t root, uint32_t* h_parents, int32_t* h_depth,
+                 int64_t* rounds_out, int64_t* reached_out) {
+  return bfs_run(g, variant, root, h_parents, h_depth, rounds_out, reached_out, 0);
+}
+
+rg_status rg_bc_pick_sources(const rg_graph* g, int k, uint32_t* h_sources) { return bc_pick(g, k, h_sources); }
+
+rg_status rg_bc(rg_graph* g, rg_variant variant, int max_iters, double* h_deps, int64_t* levels_out) {
+  if (!g || max_iters < 0) return fail(RG_EINVAL, "bad arguments");
+  std::vector<uint32_t> src(max_iters);
+  RG_TRY(bc_pick(g, max_iters, src.data()));
+  return bc_run(g, variant, src.data(), max_iters, h_deps, levels_out, 0);
+}
+
+rg_status rg_bc_sources(rg_graph* g, rg_variant variant, const uint32_t* h_sources, int nsrc, double* h_deps,
+                        int64_t* levels_out) {
+  return bc_run(g, variant, h_sources, nsrc, h_deps, levels_out, 0);
+}
+
+rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* rounds_out) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  int k = (int)std::min<int64_t>(g->n, 64);
+  std::vector<uint32_t> seeds(k);
+  for (int i = 0; i < k; i++) seeds[i] = (uint32_t)(hash_u64((uint64_t)i) % (uint64_t)g->n);
+  return radii_run(g, variant, seeds.data(), k, h_radii, rounds_out, 0);
+}
+
+rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k, int32_t* h_radii,
+                         int64_t* rounds_out) {
+  return radii_run(g, variant, h_seeds, k, h_radii, rounds_out, 0);
+}
+
+rg_status rg_last_timing(rg_timing* t) {
+  if (!t) return fail(RG_EINVAL, "null");
+  *t = g_timing;
+  return RG_OK;
+}
+
+// ---- engine-level API ------------------------------------------------------
+
+rg_status rg_frontier_create(const rg_graph* g, rg_frontier** out) {
+  if (!g || !out) return fail(RG_EINVAL, "null argument");
+  rg_frontier* f = new (std::nothrow) rg_frontier();
+  if (!f) return fail(RG_ENOMEM, "host allocation failed");
+  f->g = g;
+  rg_status s = frontier_alloc(g, f->f);
+  if (s != RG_OK) { delete f; return s; }
+  RG_CUDA(cudaMemsetAsync(f->f.bits.p, 0, f->f.bits.bytes, g->stream));
+  RG_CUDA(cudaMemsetAsync(f->f.qoff.p, 0, 4, g->stream));
+  RG_CUDA(cudaStreamSynchronize(g->stream));
+  *out = f;
+  return RG_OK;
+}
+
+rg_status rg_frontier_free(rg_frontier* f) {
+  delete f;
+  return RG_OK;
+}
+
+rg_status rg_frontier_set(rg_frontier* f, const uint32_t* h_ids, int64_t k) {
+  if (!f || k < 0 || (k > 0 && !h_ids)) return fail(RG_EINVAL, "bad arguments");
+  return frontier_from_host(f->g, f->f, h_ids, k, f->g->stream);
+}
+
+rg_status rg_frontier_set_all(rg_frontier* f) {
+  if (!f) return fail(RG_EINVAL, "null frontier");
+  return frontier_set_all(f->g, f->f, f->g->stream);
+}
+
+rg_status rg_frontier_count(const rg_frontier* f, int64_t* count) {
+  if (!f || !count) return fail(RG_EINVAL, "null argument");
+  *count = f->f.count;
+  return RG_OK;
+}
+
+rg_status rg_frontier_get(const rg_frontier* f, uint8_t* h_member) {
+  if (!f || !h_member) return fail(RG_EINVAL, "null argument");
+  const int64_t n = f->g->n, nwords = (n + 31) / 32;
+  std::vector<uint32_t> bits(nwords);
+  RG_CUDA(cudaMemcpy(bits.data(), f->f.bits.p, 4 * nwords, cudaMemcpyDeviceToHost));
+  for (int64_t v = 0; v < n; v++) h_member[v] = (bits[v >> 5] >> (v & 31)) & 1u;
+  return RG_OK;
+}
+
+__global__ void contrib_kernel(uint32_t n, const uint32_t* __restrict__ off, const double* __restrict__ p,
+                               double* __restrict__ c) {
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t d = off[v + 1] - off[v];
+    c[v] = d ? p[v] / (double)d : 0.0;
+  }
+}
+
+rg_status rg_edgemap(rg_graph* g, rg_frontier* in, rg_op op, const rg_op_args* a, rg_frontier* out, uint32_t flags,
+                     int64_t threshold, void* stream) {
+  if (!g || !in || !a || in->g != g || (out && out->g != g)) return fail(RG_EINVAL, "bad arguments");
+  if (in->f.count > g->n + 64) return fail(RG_EINVAL, "edgeMap: Sizes Don't match");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+  memset(&g_timing, 0, sizeof g_timing);
+  FView iv = view_of(in->f);
+  const bool want_out = out && !(flags & RG_NO_OUTPUT);
+  FView ov;
+  if (want_out) ov = view_of(out->f);
+  EmOpts o;
+  o.variant = RG_PUSH;
+  o.dense_forward = (flags & RG_DENSE_FORWARD) != 0;
+  o.threshold = threshold;
+  // the pull path reads the input bitmap; make sure it matches the queue
+  if (!in->f.bits_valid) RG_TRY(frontier_bits_from_queue(g, in->f, st));
+  rg_status s = RG_OK;
+  switch (op) {
+    case RG_OP_PAGERANK: {
+      if (!a->p_curr || !a->p_next) return fail(RG_EINVAL, "PAGERANK needs p_curr, p_next");
+      static thread_local DevBuf contrib;
+      RG_TRY(contrib.reserve(8 * g->n));
+      contrib_kernel<<<(unsigned)std::min<int64_t>((g->n + 255) / 256, 4096), 256, 0, st>>>(
+          (uint32_t)g->n, g->off.as<uint32_t>(), a->p_curr, contrib.as<double>());
+      s = edge_map(g, iv, OpPr{contrib.as<double>(), a->p_next}, nullptr, o, st);
+      break;
+    }
+    case RG_OP_BFS:
+      if (!a->parents) return fail(RG_EINVAL, "BFS needs parents");
+      s = edge_map(g, iv, OpBfs{a->parents}, want_out ? &ov : nullptr, o, st);
+      break;
+    case RG_OP_BC_FWD:
+      if (!a->num_paths || !a->visited_bits) return fail(RG_EINVAL, "BC_FWD needs num_paths, visited_bits");
+      s = edge_map(g, iv, OpBcFwd{a->num_paths, a->visited_bits}, want_out ? &ov : nullptr, o, st);
+      break;
+    case RG_OP_BC_BWD:
+      if (!a->deps || !a->visited_bits) return fail(RG_EINVAL, "BC_BWD needs deps, visited_bits");
+      s = edge_map(g, iv, OpBcBwd{a->deps, a->visited_bits}, nullptr, o, st);
+      break;
+    case RG_OP_RADII:
+      if (!a->visited || !a->next_visited || !a->radii) return fail(RG_EINVAL, "RADII needs visited, next_visited, radii");
+      s = edge_map(g, iv,
+                   OpRadii{(const unsigned long long*)a->visited, (unsigned long long*)a->next_visited, a->radii,
+                           a->round},
+                   want_out ? &ov : nullptr, o, st);
+      break;
+    default:
+      return fail(RG_EINVAL, "unknown op %d", (int)op);
+  }
+  if (s != RG_OK) return s;
+  if (want_out) {
+    out->f.count = ov.count;
+    out->f.degsum = ov.degsum;
+    out->f.queue_valid = true;
+    out->f.bits_valid = true;
+  }
+  RG_CUDA(cudaStreamSynchronize(st));
+  return RG_OK;
+}
+
+__global__ void vertexmap_kernel(const uint32_t* __restrict__ q, int64_t k, int vop, rg_op_args a, double c) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  uint32_t i = q[j];
+  switch (vop) {
+    case RG_VOP_PR_DAMP: a.p_next[i] = kDamping * a.p_next[i] + c; break;
+    case RG_VOP_BC_VISIT: atomicOr(a.visited_bits + (i >> 5), 1u << (i & 31)); break;
+    case RG_VOP_BC_BACK:
+      atomicOr(a.visited_bits + (i >> 5), 1u << (i & 31));
+      a.deps[i] += a.num_paths[i];
+      break;
+    case RG_VOP_RADII_SYNC: a.visited[i] = a.next_visited[i]; break;
+  }
+}
+
+rg_status rg_vertexmap(rg_graph* g, rg_frontier* f, rg_vop vop, const rg_op_args* a, void* stream) {
+  if (!g || !f || !a || f->g != g) return fail(RG_EINVAL, "bad arguments");
+  if ((int)vop < 0 || (int)vop > 3) return fail(RG_EINVAL, "unknown vertex op");
+  if ((vop == RG_VOP_PR_DAMP && !a->p_next) || (vop == RG_VOP_BC_VISIT && !a->visited_bits) ||
+      (vop == RG_VOP_BC_BACK && (!a->visited_bits || !a->deps || !a->num_paths)) ||
+      (vop == RG_VOP_RADII_SYNC && (!a->visited || !a->next_visited))) {
+    return fail(RG_EINVAL, "vertex op is missing an array");
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+  if (!f->f.queue_valid) RG_TRY(compact_bits(g, f->f, st, true));
+  if (f->f.count > 0) {
+    vertexmap_kernel<<<(unsigned)((f->f.count + 255) / 256), 256, 0, st>>>(
+        f->f.queue.as<uint32_t>(), f->f.count, (int)vop, *a, (1 - kDamping) * (1 / (double)g->n));
+    RG_CUDA(cudaGetLastError());
+  }
+  RG_CUDA(cudaStreamSynchronize(st));
+  return RG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,656 @@
+// Device graph image, scans, frontier compaction and the degree-sort relabel.
+//
+// Degree sort (preprocessGraph, IO.h:843-895): the reference sorts
+// pair<degree, id> with std::greater, i.e. degree descending and ties by
+// DEScending original id, and gives rank r to the r-th pair.  Here a stable
+// LSD radix sort on the 32-bit key ~degree runs over ids laid out in
+// descending order, which yields exactly that order (the sort is stable, so
+// equal degrees keep the descending-id input order).  Neighbour lists are then
+// relabelled in place order (IO.h:877-895 keeps the order, it does not
+// re-sort).
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "rg_device.cuh"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+rg_status fail(rg_status s, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return s;
+}
+void clear_error() { g_err[0] = 0; }
+const char* last_error() { return g_err; }
+
+rg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  const char* f = strrchr(file, '/');
+  fail(e == cudaErrorMemoryAllocation ? RG_ENOMEM : RG_ECUDA, "%s: %s (%s:%d)",
+       cudaGetErrorString(e), what, f ? f + 1 : file, line);
+  cudaGetLastError();  // clear a sticky-free error so the context stays usable
+  return e == cudaErrorMemoryAllocation ? RG_ENOMEM : RG_ECUDA;
+}
+
+rg_status DevBuf::reserve(size_t b) {
+  if (b <= bytes && p) return RG_OK;
+  release();
+  size_t want = b < 256 ? 256 : b;
+  RG_CUDA(cudaMalloc(&p, want));
+  bytes = want;
+  return RG_OK;
+}
+
+Workspace::~Workspace() {
+  if (h_info) cudaFreeHost(h_info);
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of uint32 (three kernels: tile sums, scan of sums, apply)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <int kThreads>
+__device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_tot[kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < kThreads / 32 ? warp_tot[lane] : 0;
+    uint32_t ti = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t u = __shfl_up_sync(0xffffffffu, ti, o);
+      if (lane >= o) ti += u;
+    }
+    if (lane < kThreads / 32) warp_tot[lane] = ti - t;
+    if (lane == kThreads / 32 - 1) *total = ti;
+  }
+  __syncthreads();
+  uint32_t r = warp_tot[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void scan_tile_sums(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ sums) {
+  int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t s = 0;
+  for (int i = 0; i < kScanItems; i++) {
+    int64_t idx = base + (int64_t)i * kScanThreads + threadIdx.x;
+    if (idx < n) s += in[idx];
+  }
+  __shared__ uint32_t tot;
+  block_exclusive_sum<kScanThreads>(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// One block scans `nt` tile sums in place (exclusive) and writes the total.
+__global__ void scan_sums(uint32_t* sums, int64_t nt, uint32_t* total_out) {
+  __shared__ uint32_t carry_s, tot;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nt; base += kScanThreads) {
+    int64_t i = base + threadIdx.x;
+    uint32_t v = i < nt ? sums[i] : 0;
+    uint32_t ex = block_exclusive_sum<kScanThreads>(v, &tot);
+    uint32_t c = carry_s;
+    if (i < nt) sums[i] = c + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s = c + tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry_s;
+}
+
+__global__ void scan_apply(const uint32_t* __restrict__ in, int64_t n, const uint32_t* __restrict__ sums,
+                           uint32_t* __restrict__ out) {
+  // each thread scans kScanItems consecutive elements
+  int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    int64_t idx = base + i;
+    v[i] = idx < n ? in[idx] : 0;
+    s += v[i];
+  }
+  __shared__ uint32_t tot;
+  uint32_t ex = block_exclusive_sum<kScanThreads>(s, &tot) + sums[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    int64_t idx = base + i;
+    if (idx < n) out[idx] = ex;
+    ex += v[i];
+  }
+}
+
+rg_status scan_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st) {
+  int64_t nt = (n + kScanTile - 1) / kScanTile;
+  if (nt == 0) nt = 1;
+  RG_TRY(ws.scan_tmp.reserve(sizeof(uint32_t) * (nt + 1)));
+  uint32_t* sums = ws.scan_tmp.as<uint32_t>();
+  if (n > 0) scan_tile_sums<<<(unsigned)nt, kScanThreads, 0, st>>>(in, n, sums);
+  else RG_CUDA(cudaMemsetAsync(sums, 0, 4, st));
+  scan_sums<<<1, kScanThreads, 0, st>>>(sums, nt, out + n);
+  if (n > 0) scan_apply<<<(unsigned)nt, kScanThreads, 0, st>>>(in, n, sums, out);
+  RG_CUDA(cudaGetLastError());
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// bitmap -> ascending queue + degree scan (ligra.h:161-192 compaction,
+// vertexSubset.h:196-211 toSparse)
+// ---------------------------------------------------------------------------
+constexpr int kCompThreads = 256;
+constexpr int kCompWords = 8;  // words per thread
+constexpr int kCompTile = kCompThreads * kCompWords;
+
+struct CountDeg {
+  uint32_t c, d;
+};
+
+__device__ __forceinline__ CountDeg count_words(const uint32_t* __restrict__ bits, int64_t nwords,
+                                                const uint32_t* __restrict__ off, int64_t w0) {
+  CountDeg r{0, 0};
+#pragma unroll
+  for (int i = 0; i < kCompWords; i++) {
+    int64_t w = w0 + i;
+    if (w >= nwords) break;
+    uint32_t x = bits[w];
+    r.c += __popc(x);
+    while (x) {
+      int b = __ffs(x) - 1;
+      x &= x - 1;
+      uint32_t v = (uint32_t)(w * 32 + b);
+      r.d += off[v + 1] - off[v];
+    }
+  }
+  return r;
+}
+
+__global__ void comp_count(const uint32_t* __restrict__ bits, int64_t nwords, const uint32_t* __restrict__ off,
+                           uint32_t* __restrict__ part_c, uint32_t* __restrict__ part_d) {
+  int64_t w0 = ((int64_t)blockIdx.x * kCompThreads + threadIdx.x) * kCompWords;
+  CountDeg r = count_words(bits, nwords, off, w0);
+  __shared__ uint32_t tc, td;
+  block_exclusive_sum<kCompThreads>(r.c, &tc);
+  block_exclusive_sum<kCompThreads>(r.d, &td);
+  if (threadIdx.x == 0) {
+    part_c[blockIdx.x] = tc;
+    part_d[blockIdx.x] = td;
+  }
+}
+
+__global__ void comp_scan(uint32_t* part_c, uint32_t* part_d, int64_t nt, uint64_t* info,
+                          uint32_t* qoff_total_slot_base) {
+  __shared__ uint32_t cc, cd, tc, td;
+  if (threadIdx.x == 0) { cc = 0; cd = 0; }
+  __syncthreads();
+  for (int64_t base = 0; base < nt; base += kCompThreads) {
+    int64_t i = base + threadIdx.x;
+    uint32_t vc = i < nt ? part_c[i] : 0, vd = i < nt ? part_d[i] : 0;
+    uint32_t ec = block_exclusive_sum<kCompThreads>(vc, &tc);
+    uint32_t ed = block_exclusive_sum<kCompThreads>(vd, &td);
+    uint32_t c0 = cc, d0 = cd;
+    if (i < nt) { part_c[i] = c0 + ec; part_d[i] = d0 + ed; }
+    __syncthreads();
+    if (threadIdx.x == 0) { cc = c0 + tc; cd = d0 + td; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    info[0] = cc;
+    info[1] = cd;
+    // qoff[count] = degsum: the slot sits right after the last queue entry
+    if (qoff_total_slot_base) qoff_total_slot_base[cc] = cd;
+  }
+}
+
+__global__ void comp_emit(const uint32_t* __restrict__ bits, int64_t nwords, const uint32_t* __restrict__ off,
+                          const uint32_t* __restrict__ part_c, const uint32_t* __restrict__ part_d,
+                          uint32_t* __restrict__ queue, uint32_t* __restrict__ qoff, int32_t* depth,
+                          int32_t level, uint32_t* or_into) {
+  int64_t w0 = ((int64_t)blockIdx.x * kCompThreads + threadIdx.x) * kCompWords;
+  CountDeg r = count_words(bits, nwords, off, w0);
+  __shared__ uint32_t tc, td;
+  uint32_t pc = block_exclusive_sum<kCompThreads>(r.c, &tc) + part_c[blockIdx.x];
+  uint32_t pd = block_exclusive_sum<kCompThreads>(r.d, &td) + part_d[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kCompWords; i++) {
+    int64_t w = w0 + i;
+    if (w >= nwords) break;
+    uint32_t x = bits[w];
+    if (or_into && x) or_into[w] |= x;
+    while (x) {
+      int b = __ffs(x) - 1;
+      x &= x - 1;
+      uint32_t v = (uint32_t)(w * 32 + b);
+      queue[pc] = v;
+      qoff[pc] = pd;
+      if (depth) depth[v] = level;
+      pc++;
+      pd += off[v + 1] - off[v];
+    }
+  }
+}
+
+rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool sync, int32_t* depth,
+                       int32_t level, uint32_t* or_into, uint32_t* queue_out, uint32_t* qoff_out) {
+  Workspace& ws = const_cast<rg_graph*>(g)->ws;
+  const int64_t nwords = (g->n + 31) / 32;
+  const int64_t nt = (nwords + kCompTile - 1) / kCompTile;
+  RG_TRY(ws.scan_partials.reserve(sizeof(uint32_t) * 2 * (nt + 1)));
+  uint32_t* pc = ws.scan_partials.as<uint32_t>();
+  uint32_t* pd = pc + nt + 1;
+  uint32_t* q = queue_out ? queue_out : f.queue.as<uint32_t>();
+  uint32_t* qo = qoff_out ? qoff_out : f.qoff.as<uint32_t>();
+  uint64_t* info = ws.counters.as<uint64_t>();
+  comp_count<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, g->off.as<uint32_t>(), pc, pd);
+  comp_scan<<<1, kCompThreads, 0, st>>>(pc, pd, nt, info, qo);
+  comp_emit<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, g->off.as<uint32_t>(), pc,
+                                                   pd, q, qo, depth, level, or_into);
+  RG_CUDA(cudaGetLastError());
+  RG_CUDA(cudaMemcpyAsync(ws.h_info, info, 16, cudaMemcpyDeviceToHost, st));
+  f.queue_valid = (queue_out == nullptr);
+  f.bits_valid = true;
+  if (sync) {
+    RG_CUDA(cudaStreamSynchronize(st));
+    f.count = (int64_t)ws.h_info[0];
+    f.degsum = (int64_t)ws.h_info[1];
+  }
+  return RG_OK;
+}
+
+rg_status frontier_alloc(const rg_graph* g, Frontier& f) {
+  const int64_t nwords = (g->n + 31) / 32;
+  RG_TRY(f.queue.reserve(sizeof(uint32_t) * (g->n + 64)));
+  RG_TRY(f.qoff.reserve(sizeof(uint32_t) * (g->n + 65)));
+  RG_TRY(f.bits.reserve(sizeof(uint32_t) * (nwords + 8)));
+  return RG_OK;
+}
+
+__global__ void set_bits_from_queue(const uint32_t* __restrict__ q, int64_t k, uint32_t* bits) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) atomicOr(bits + (q[i] >> 5), 1u << (q[i] & 31));
+}
+
+rg_status frontier_bits_from_queue(const rg_graph* g, Frontier& f, cudaStream_t st) {
+  const int64_t nwords = (g->n + 31) / 32;
+  RG_CUDA(cudaMemsetAsync(f.bits.p, 0, sizeof(uint32_t) * nwords, st));
+  if (f.count > 0) {
+    set_bits_from_queue<<<(unsigned)((f.count + 255) / 256), 256, 0, st>>>(f.queue.as<uint32_t>(), f.count,
+                                                                          f.bits.as<uint32_t>());
+  }
+  RG_CUDA(cudaGetLastError());
+  f.bits_valid = true;
+  return RG_OK;
+}
+
+rg_status frontier_from_host(const rg_graph* g, Frontier& f, const uint32_t* ids, int64_t k,
+                             cudaStream_t st) {
+  RG_TRY(frontier_alloc(g, f));
+  if (k > g->n + 64) return fail(RG_EINVAL, "frontier larger than n+64 entries");
+  std::vector<uint32_t> qo(k + 1);
+  uint64_t acc = 0;
+  for (int64_t i = 0; i < k; i++) {
+    if (ids[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "frontier id %u >= n", ids[i]);
+    qo[i] = (uint32_t)acc;
+    acc += g->h_deg[ids[i]];
+  }
+  qo[k] = (uint32_t)acc;
+  if (k) RG_CUDA(cudaMemcpyAsync(f.queue.p, ids, 4 * k, cudaMemcpyHostToDevice, st));
+  RG_CUDA(cudaMemcpyAsync(f.qoff.p, qo.data(), 4 * (k + 1), cudaMemcpyHostToDevice, st));
+  f.count = k;
+  f.degsum = (int64_t)acc;
+  f.queue_valid = true;
+  RG_TRY(frontier_bits_from_queue(g, f, st));
+  // the host vector must outlive the async copy
+  RG_CUDA(cudaStreamSynchronize(st));
+  return RG_OK;
+}
+
+__global__ void fill_all_bits(uint32_t* bits, int64_t n) {
+  int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t nwords = (n + 31) / 32;
+  if (w < nwords) {
+    int64_t rem = n - w * 32;
+    bits[w] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+  }
+}
+
+rg_status frontier_set_all(const rg_graph* g, Frontier& f, cudaStream_t st) {
+  RG_TRY(frontier_alloc(g, f));
+  const int64_t nwords = (g->n + 31) / 32;
+  fill_all_bits<<<(unsigned)((nwords + 255) / 256), 256, 0, st>>>(f.bits.as<uint32_t>(), g->n);
+  RG_CUDA(cudaGetLastError());
+  f.bits_valid = true;
+  return compact_bits(g, f, st, true);
+}
+
+// ---------------------------------------------------------------------------
+// graph image
+// ---------------------------------------------------------------------------
+
+// chunk_v[c] = source vertex of edge min(c*kSweepChunk, m-1), c = 0..nchunks.
+__global__ void build_chunk_starts(const uint32_t* __restrict__ off, uint32_t n, uint32_t m, int64_t nchunks,
+                                   uint32_t* __restrict__ chunk_v) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > nchunks) return;
+  uint64_t e = (uint64_t)c * kSweepChunk;
+  if (e >= m) e = m - 1;
+  chunk_v[c] = upper_index(off, 0u, n - 1, (uint32_t)e);
+}
+
+static rg_status finish_graph(rg_graph* g) {
+  cudaStream_t st = g->stream;
+  if (g->m > 0) {
+    g->nchunks = (g->m + kSweepChunk - 1) / kSweepChunk;
+    RG_TRY(g->chunk_v.reserve(sizeof(uint32_t) * (g->nchunks + 1)));
+    build_chunk_starts<<<(unsigned)((g->nchunks + 1 + 255) / 256), 256, 0, st>>>(
+        g->off.as<uint32_t>(), (uint32_t)g->n, (uint32_t)g->m, g->nchunks, g->chunk_v.as<uint32_t>());
+    RG_CUDA(cudaGetLastError());
+  }
+  RG_TRY(g->ws.counters.reserve(4096));
+  RG_CUDA(cudaMemsetAsync(g->ws.counters.p, 0, 4096, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  return RG_OK;
+}
+
+static rg_status new_graph(rg_graph** out) {
+  rg_graph* g = new (std::nothrow) rg_graph();
+  if (!g) return fail(RG_ENOMEM, "host allocation failed");
+  cudaError_t e = cudaGetDevice(&g->device);
+  if (e != cudaSuccess) {
+    delete g;
+    cudaGetLastError();
+    return fail(RG_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
+      cudaHostAlloc((void**)&g->ws.h_info, 64, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    delete g;
+    return fail(RG_ECUDA, "stream/event/pinned allocation failed");
+  }
+  *out = g;
+  return RG_OK;
+}
+
+}  // namespace rg
+
+rg_graph::~rg_graph() {
+  if (stream) cudaStreamSynchronize(stream);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+using namespace rg;
+
+static rg_status graph_create_common(int64_t n, int64_t m, const uint32_t* off, const uint32_t* adj,
+                                     cudaMemcpyKind kind, rg_graph** out) {
+  if (!out || n <= 0 || m < 0 || !off || (m > 0 && !adj)) {
+    return fail(RG_EINVAL, "rg_graph_create: bad arguments");
+  }
+  if (m >= 0xFFFFFFFFll || n >= 0xFFFFFFFFll) {
+    return fail(RG_EUNSUPPORTED, "rg_graph_create: >= 2^32 edges or vertices");
+  }
+  std::vector<uint32_t> h_off(n + 1);
+  if (kind == cudaMemcpyHostToDevice) {
+    memcpy(h_off.data(), off, 4 * (n + 1));
+  } else {
+    RG_CUDA(cudaMemcpy(h_off.data(), off, 4 * (n + 1), cudaMemcpyDeviceToHost));
+  }
+  if (h_off[0] != 0 || h_off[n] != (uint32_t)m) return fail(RG_EINVAL, "offsets must start at 0 and end at m");
+  rg_graph* g = nullptr;
+  RG_TRY(new_graph(&g));
+  g->n = n;
+  g->m = m;
+  g->h_deg.resize(n);
+  uint32_t mx = 0;
+  for (int64_t v = 0; v < n; v++) {
+    if (h_off[v + 1] < h_off[v]) { delete g; return fail(RG_EINVAL, "offsets not monotone at %lld", (long long)v); }
+    g->h_deg[v] = h_off[v + 1] - h_off[v];
+    mx = std::max(mx, g->h_deg[v]);
+  }
+  g->max_deg = mx;
+  rg_status s;
+  if ((s = g->off.reserve(4 * (n + 1))) != RG_OK || (s = g->adj.reserve(4 * (m + 8))) != RG_OK) {
+    delete g;
+    return s;
+  }
+  cudaError_t e = cudaMemcpyAsync(g->off.p, h_off.data(), 4 * (n + 1), cudaMemcpyHostToDevice, g->stream);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(g->adj.p, adj, 4 * m, kind, g->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->adj.as<uint32_t>() + m, 0, 32, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  if (e != cudaSuccess) {
+    delete g;
+    return cuda_fail(e, "graph upload", __FILE__, __LINE__);
+  }
+  if ((s = finish_graph(g)) != RG_OK) { delete g; return s; }
+  *out = g;
+  return RG_OK;
+}
+
+extern "C" rg_status rg_graph_create(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                                     rg_graph** out) {
+  return graph_create_common(n, m, h_off, h_adj, cudaMemcpyHostToDevice, out);
+}
+
+extern "C" rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
+                                            const uint32_t* d_adj, rg_graph** out) {
+  return graph_create_common(n, m, d_off, d_adj, cudaMemcpyDeviceToDevice, out);
+}
+
+extern "C" rg_status rg_graph_free(rg_graph* g) {
+  delete g;
+  return RG_OK;
+}
+
+extern "C" rg_status rg_graph_info(const rg_graph* g, int64_t* n, int64_t* m, int* sorted) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (n) *n = g->n;
+  if (m) *m = g->m;
+  if (sorted) *sorted = g->sorted ? 1 : 0;
+  return RG_OK;
+}
+
+extern "C" rg_status rg_graph_download(const rg_graph* g, uint32_t* h_off, uint32_t* h_adj, uint32_t* h_new_ids) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (h_off) RG_CUDA(cudaMemcpy(h_off, g->off.p, 4 * (g->n + 1), cudaMemcpyDeviceToHost));
+  if (h_adj && g->m) RG_CUDA(cudaMemcpy(h_adj, g->adj.p, 4 * g->m, cudaMemcpyDeviceToHost));
+  if (h_new_ids) {
+    if (g->sorted) memcpy(h_new_ids, g->h_new_ids.data(), 4 * g->n);
+    else for (int64_t i = 0; i < g->n; i++) h_new_ids[i] = (uint32_t)i;
+  }
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// degree sort
+// ---------------------------------------------------------------------------
+namespace rg {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortSub = 16;  // sub-tiles per block
+constexpr int kSortTile = kSortThreads * kSortSub;
+
+// key[i] = ~deg(id), val[i] = id with ids laid out in DESCENDING order.
+__global__ void sort_init(const uint32_t* __restrict__ off, uint32_t n, uint32_t* key, uint32_t* val) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    uint32_t v = n - 1 - (uint32_t)i;
+    key[i] = ~(off[v + 1] - off[v]);
+    val[i] = v;
+  }
+}
+
+__global__ void sort_hist(const uint32_t* __restrict__ key, int64_t n, int shift, int64_t nblocks,
+                          uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  int64_t base = (int64_t)blockIdx.x * kSortTile;
+  for (int s = 0; s < kSortSub; s++) {
+    int64_t i = base + (int64_t)s * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(key[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter: sub-tiles in order, threads in order within a sub-tile.
+__global__ void sort_scatter(const uint32_t* __restrict__ key, const uint32_t* __restrict__ val, int64_t n,
+                             int shift, int64_t nblocks, const uint32_t* __restrict__ hist_scan,
+                             uint32_t* __restrict__ key_out, uint32_t* __restrict__ val_out) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t running[256];
+  __shared__ uint32_t wcount[kWarps][257];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  running[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  int64_t base = (int64_t)blockIdx.x * kSortTile;
+  for (int s = 0; s < kSortSub; s++) {
+    for (int d = threadIdx.x; d < kWarps * 257; d += kSortThreads) (&wcount[0][0])[d] = 0;
+    __syncthreads();
+    int64_t i = base + (int64_t)s * kSortThreads + threadIdx.x;
+    bool valid = i < n;
+    uint32_t k = valid ? key[i] : 0, v = valid ? val[i] : 0;
+    uint32_t digit = valid ? ((k >> shift) & 255u) : 256u;
+    uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    if (rank == 0) wcount[w][digit] = __popc(peers);
+    __syncthreads();
+    uint32_t pos = 0;
+    if (valid) {
+      pos = running[digit] + rank;
+      for (int ww = 0; ww < w; ww++) pos += wcount[ww][digit];
+    }
+    __syncthreads();
+    {
+      uint32_t t = 0;
+      for (int ww = 0; ww < kWarps; ww++) t += wcount[ww][threadIdx.x];
+      running[threadIdx.x] += t;
+    }
+    if (valid) {
+      key_out[pos] = k;
+      val_out[pos] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void rank_to_ids(const uint32_t* __restrict__ sorted_ids, const uint32_t* __restrict__ off, uint32_t n,
+                            uint32_t* __restrict__ new_ids, uint32_t* __restrict__ new_deg) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) {
+    uint32_t v = sorted_ids[r];
+    new_ids[v] = (uint32_t)r;
+    new_deg[r] = off[v + 1] - off[v];
+  }
+}
+
+// One warp per original vertex: copy its list to the new position, relabelled.
+__global__ void relabel_lists(const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj, uint32_t n,
+                              const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ new_off,
+                              uint32_t* __restrict__ new_adj) {
+  int64_t wv = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = wv; v < n; v += nw) {
+    uint32_t b = off[v], e = off[v + 1];
+    uint32_t o = new_off[new_ids[v]];
+    for (uint32_t j = b + lane; j < e; j += 32) new_adj[o + (j - b)] = new_ids[adj[j]];
+  }
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids) {
+  if (!g || !out) return fail(RG_EINVAL, "rg_graph_degree_sort: null argument");
+  const int64_t n = g->n, m = g->m;
+  cudaStream_t st = g->stream;
+  Workspace& ws = const_cast<rg_graph*>(g)->ws;
+  DevBuf k0, v0, k1, v1, hist, new_deg;
+  const int64_t nblocks = (n + kSortTile - 1) / kSortTile;
+  RG_TRY(k0.reserve(4 * n)); RG_TRY(v0.reserve(4 * n));
+  RG_TRY(k1.reserve(4 * n)); RG_TRY(v1.reserve(4 * n));
+  RG_TRY(hist.reserve(4 * (256 * nblocks + 1)));
+  sort_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->off.as<uint32_t>(), (uint32_t)n, k0.as<uint32_t>(),
+                                                        v0.as<uint32_t>());
+  // ~deg differs from 0xFFFFFFFF only in the low bits that max_deg spans
+  int bits = 0;
+  while (bits < 32 && (g->max_deg >> bits) != 0) bits++;
+  int passes = (bits + 7) / 8;
+  uint32_t *ka = k0.as<uint32_t>(), *va = v0.as<uint32_t>(), *kb = k1.as<uint32_t>(), *vb = v1.as<uint32_t>();
+  for (int p = 0; p < passes; p++) {
+    int shift = 8 * p;
+    sort_hist<<<(unsigned)nblocks, kSortThreads, 0, st>>>(ka, n, shift, nblocks, hist.as<uint32_t>());
+    RG_TRY(scan_u32(ws, hist.as<uint32_t>(), hist.as<uint32_t>(), 256 * nblocks, st));
+    sort_scatter<<<(unsigned)nblocks, kSortThreads, 0, st>>>(ka, va, n, shift, nblocks, hist.as<uint32_t>(), kb,
+                                                             vb);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  RG_CUDA(cudaGetLastError());
+  rg_graph* ng = nullptr;
+  RG_TRY(new_graph(&ng));
+  ng->n = n;
+  ng->m = m;
+  rg_status s;
+  if ((s = ng->off.reserve(4 * (n + 1))) != RG_OK || (s = ng->adj.reserve(4 * (m + 8))) != RG_OK ||
+      (s = ng->new_ids.reserve(4 * n)) != RG_OK || (s = new_deg.reserve(4 * n)) != RG_OK) {
+    delete ng;
+    return s;
+  }
+  rank_to_ids<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(va, g->off.as<uint32_t>(), (uint32_t)n,
+                                                          ng->new_ids.as<uint32_t>(), new_deg.as<uint32_t>());
+  if ((s = scan_u32(ws, new_deg.as<uint32_t>(), ng->off.as<uint32_t>(), n, st)) != RG_OK) {
+    delete ng;
+    return s;
+  }
+  relabel_lists<<<(unsigned)std::min<int64_t>((n * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(
+      g->off.as<uint32_t>(), g->adj.as<uint32_t>(), (uint32_t)n, ng->new_ids.as<uint32_t>(),
+      ng->off.as<uint32_t>(), ng->adj.as<uint32_t>());
+  cudaError_t e = cudaMemsetAsync(ng->adj.as<uint32_t>() + m, 0, 32, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    delete ng;
+    return cuda_fail(e, "degree sort", __FILE__, __LINE__);
+  }
+  ng->sorted = true;
+  ng->h_new_ids.resize(n);
+  e = cudaMemcpy(ng->h_new_ids.data(), ng->new_ids.p, 4 * n, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) { delete ng; return cuda_fail(e, "new_ids download", __FILE__, __LINE__); }
+  ng->h_deg.resize(n);
+  uint32_t mx = 0;
+  for (int64_t v = 0; v < n; v++) {
+    ng->h_deg[ng->h_new_ids[v]] = g->h_deg[v];
+    mx = std::max(mx, g->h_deg[v]);
+  }
+  ng->max_deg = mx;
+  if ((s = finish_graph(ng)) != RG_OK) { delete ng; return s; }
+  if (h_new_ids) memcpy(h_new_ids, ng->h_new_ids.data(), 4 * n);
+  *out = ng;
+  return RG_OK;
+}

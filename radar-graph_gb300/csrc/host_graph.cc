@@ -1,0 +1,311 @@
+// Host-side graph input: seeded generator, Ligra file formats, symmetric
+// clean-up into CSR.  These feed the device graph image (rg_graph_create).
+//
+// Generator: GAP/src/generator.h:52-114 (R-MAT A=0.57 B=0.19 C=0.19 with
+// 2^18-edge blocks each drawn from mt19937 seeded with seed+block, then an
+// id permutation from an mt19937(seed) shuffle; Erdos-Renyi draws uniform
+// endpoint pairs with the same blocking and no permutation).
+// Text format: IO.h:231-268.  Binary format: IO.h:477-626.
+// Symmetric clean-up: IO.h:429-474 (per vertex sort, unique, drop self-loop).
+
+#include <omp.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "rg_host.h"
+
+namespace rg {
+
+namespace {
+
+constexpr int64_t kGenBlock = 1 << 18;  // generator.h:152
+
+// Parallel exclusive prefix sum of uint32 counts into n+1 uint32 offsets.
+// Returns false if the total does not fit in 32 bits.
+bool prefix_u32(const std::vector<uint32_t>& cnt, uint32_t* out) {
+  int64_t n = (int64_t)cnt.size();
+  int T = omp_get_max_threads();
+  std::vector<uint64_t> part(T + 1, 0);
+#pragma omp parallel num_threads(T)
+  {
+    int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    int64_t b = n * t / nt, e = n * (t + 1) / nt;
+    uint64_t s = 0;
+    for (int64_t i = b; i < e; i++) s += cnt[i];
+    part[t + 1] = s;
+#pragma omp barrier
+#pragma omp single
+    for (int i = 0; i < nt; i++) part[i + 1] += part[i];
+    uint64_t a = part[t];
+    for (int64_t i = b; i < e; i++) { out[i] = (uint32_t)a; a += cnt[i]; }
+  }
+  if (part[T] > 0xFFFFFFFFull) return false;
+  out[n] = (uint32_t)part[T];
+  return true;
+}
+
+}  // namespace
+
+rg_status generate_edges(int scale, int edge_factor, uint64_t seed, int uniform, uint32_t* src,
+                         uint32_t* dst) {
+  if (scale < 1 || scale > 31 || edge_factor < 1 || !src || !dst) {
+    return fail(RG_EINVAL, "rg_generate_edges: bad scale/edge_factor/pointer");
+  }
+  const int64_t nn = int64_t(1) << scale;
+  const int64_t ne = nn * edge_factor;
+  const int64_t nblocks = (ne + kGenBlock - 1) / kGenBlock;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t blk = 0; blk < nblocks; blk++) {
+    std::mt19937 rng((uint32_t)(seed + (uint64_t)blk));
+    const int64_t e0 = blk * kGenBlock, e1 = std::min(e0 + kGenBlock, ne);
+    if (uniform) {
+      std::uniform_int_distribution<int32_t> ud(0, (int32_t)(nn - 1));
+      for (int64_t e = e0; e < e1; e++) {
+        int32_t a = ud(rng);
+        int32_t b = ud(rng);
+        src[e] = (uint32_t)a;
+        dst[e] = (uint32_t)b;
+      }
+    } else {
+      const float A = 0.57f, B = 0.19f, C = 0.19f;
+      std::uniform_real_distribution<float> ud(0, 1.0f);
+      for (int64_t e = e0; e < e1; e++) {
+        uint32_t s = 0, d = 0;
+        for (int depth = 0; depth < scale; depth++) {
+          float r = ud(rng);
+          s <<= 1;
+          d <<= 1;
+          if (r < A + B) {
+            if (r > A) d++;
+          } else {
+            s++;
+            if (r > A + B + C) d++;
+          }
+        }
+        src[e] = s;
+        dst[e] = d;
+      }
+    }
+  }
+  if (!uniform) {  // PermuteIDs (generator.h:52-62)
+    std::vector<uint32_t> perm(nn);
+    for (int64_t i = 0; i < nn; i++) perm[i] = (uint32_t)i;
+    std::mt19937 rng((uint32_t)seed);
+    std::shuffle(perm.begin(), perm.end(), rng);
+#pragma omp parallel for
+    for (int64_t e = 0; e < ne; e++) {
+      src[e] = perm[src[e]];
+      dst[e] = perm[dst[e]];
+    }
+  }
+  return RG_OK;
+}
+
+// Per-vertex sort + unique + self-loop removal over a scattered adjacency
+// (`off` n+1, `tmp` holds the raw lists), then repack into exact arrays.
+static rg_status clean_and_pack(int64_t n, const std::vector<uint32_t>& off, std::vector<uint32_t>& tmp,
+                                uint32_t** off_out, uint32_t** adj_out, int64_t* m_out) {
+  std::vector<uint32_t> nd(n);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < n; i++) {
+    uint32_t* b = tmp.data() + off[i];
+    uint32_t* e = tmp.data() + off[i + 1];
+    std::sort(b, e);
+    uint32_t* ne = std::unique(b, e);
+    ne = std::remove(b, ne, (uint32_t)i);
+    nd[i] = (uint32_t)(ne - b);
+  }
+  uint32_t* o = (uint32_t*)malloc(sizeof(uint32_t) * (n + 1));
+  if (!o) return fail(RG_ENOMEM, "host malloc of offsets failed");
+  if (!prefix_u32(nd, o)) { free(o); return fail(RG_EUNSUPPORTED, "graph has >= 2^32 edges"); }
+  const int64_t m = o[n];
+  uint32_t* a = (uint32_t*)malloc(sizeof(uint32_t) * (m + 4));  // +4: room for 16-byte tails
+  if (!a) { free(o); return fail(RG_ENOMEM, "host malloc of edges failed"); }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < n; i++) memcpy(a + o[i], tmp.data() + off[i], 4ull * nd[i]);
+  memset(a + m, 0, 16);
+  *off_out = o;
+  *adj_out = a;
+  *m_out = m;
+  return RG_OK;
+}
+
+rg_status csr_from_edges(int64_t n, int64_t ne, const uint32_t* src, const uint32_t* dst,
+                         uint32_t** off_out, uint32_t** adj_out, int64_t* m_out) {
+  if (n <= 0 || ne < 0 || (ne > 0 && (!src || !dst)) || !off_out || !adj_out || !m_out) {
+    return fail(RG_EINVAL, "rg_csr_from_edges: bad arguments");
+  }
+  if (2 * ne > 0xFFFFFFFFll) return fail(RG_EUNSUPPORTED, "rg_csr_from_edges: >= 2^32 entries");
+  std::vector<std::atomic<uint32_t>> cnt(n);
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; i++) cnt[i].store(0, std::memory_order_relaxed);
+  bool bad = false;
+#pragma omp parallel for reduction(|| : bad)
+  for (int64_t e = 0; e < ne; e++) {
+    if (src[e] >= (uint64_t)n || dst[e] >= (uint64_t)n) { bad = true; continue; }
+    cnt[src[e]].fetch_add(1, std::memory_order_relaxed);
+    cnt[dst[e]].fetch_add(1, std::memory_order_relaxed);
+  }
+  if (bad) return fail(RG_EINVAL, "rg_csr_from_edges: endpoint >= n");
+  std::vector<uint32_t> c(n);
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; i++) c[i] = cnt[i].load(std::memory_order_relaxed);
+  std::vector<uint32_t> off(n + 1);
+  prefix_u32(c, off.data());
+  std::vector<std::atomic<uint32_t>>& pos = cnt;
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; i++) pos[i].store(off[i], std::memory_order_relaxed);
+  std::vector<uint32_t> tmp(2 * ne);
+#pragma omp parallel for
+  for (int64_t e = 0; e < ne; e++) {
+    tmp[pos[src[e]].fetch_add(1, std::memory_order_relaxed)] = dst[e];
+    tmp[pos[dst[e]].fetch_add(1, std::memory_order_relaxed)] = src[e];
+  }
+  return clean_and_pack(n, off, tmp, off_out, adj_out, m_out);
+}
+
+rg_status write_adjacency(const char* path, int64_t n, int64_t m, const uint32_t* off,
+                          const uint32_t* adj) {
+  if (!path || n <= 0 || m < 0 || !off || (m > 0 && !adj)) {
+    return fail(RG_EINVAL, "rg_write_adjacency: bad arguments");
+  }
+  FILE* f = fopen(path, "w");
+  if (!f) return fail(RG_EIO, "rg_write_adjacency: cannot open %s", path);
+  std::string buf;
+  buf.reserve(1 << 20);
+  auto flush = [&]() { fwrite(buf.data(), 1, buf.size(), f); buf.clear(); };
+  char tmp[32];
+  buf += "AdjacencyGraph\n";
+  snprintf(tmp, sizeof tmp, "%lld\n", (long long)n); buf += tmp;
+  snprintf(tmp, sizeof tmp, "%lld\n", (long long)m); buf += tmp;
+  for (int64_t i = 0; i < n; i++) {
+    snprintf(tmp, sizeof tmp, "%u\n", off[i]); buf += tmp;
+    if (buf.size() > (1u << 20)) flush();
+  }
+  for (int64_t i = 0; i < m; i++) {
+    snprintf(tmp, sizeof tmp, "%u\n", adj[i]); buf += tmp;
+    if (buf.size() > (1u << 20)) flush();
+  }
+  flush();
+  bool ok = fclose(f) == 0;
+  return ok ? RG_OK : fail(RG_EIO, "rg_write_adjacency: write failed");
+}
+
+namespace {
+
+bool read_file(const char* path, std::vector<char>& out) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  out.resize(sz > 0 ? sz : 0);
+  size_t got = sz > 0 ? fread(out.data(), 1, sz, f) : 0;
+  fclose(f);
+  return (long)got == sz;
+}
+
+inline bool is_space(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t' || c == '\0'; }
+
+}  // namespace
+
+rg_status read_graph(const char* path, int symmetric, int binary, int64_t* n_out, int64_t* m_out,
+                     uint32_t** off_out, uint32_t** adj_out) {
+  if (!path || !n_out || !m_out || !off_out || !adj_out) {
+    return fail(RG_EINVAL, "rg_read_graph: null argument");
+  }
+  if (!symmetric) {
+    return fail(RG_EUNSUPPORTED, "rg_read_graph: directed graphs are not supported yet");
+  }
+  if (binary) {  // IO.h:477-626: .config holds n, .adj uint32 edges, .idx uint32 offsets
+    std::string base(path);
+    FILE* cf = fopen((base + ".config").c_str(), "r");
+    if (!cf) return fail(RG_EIO, "rg_read_graph: cannot open %s.config", path);
+    long long n = -1;
+    int got = fscanf(cf, "%lld", &n);
+    fclose(cf);
+    if (got != 1 || n <= 0) return fail(RG_EFORMAT, "rg_read_graph: bad .config");
+    std::vector<char> adjb, idxb;
+    if (!read_file((base + ".adj").c_str(), adjb)) return fail(RG_EIO, "cannot read %s.adj", path);
+    if (!read_file((base + ".idx").c_str(), idxb)) return fail(RG_EIO, "cannot read %s.idx", path);
+    if ((long long)(idxb.size() / 4) != n || idxb.size() % 4 || adjb.size() % 4) {
+      return fail(RG_EFORMAT, "rg_read_graph: File size wrong");
+    }
+    int64_t m = (int64_t)(adjb.size() / 4);
+    uint32_t* o = (uint32_t*)malloc(4 * (n + 1));
+    uint32_t* a = (uint32_t*)malloc(4 * (m + 4));
+    if (!o || !a) { free(o); free(a); return fail(RG_ENOMEM, "host malloc failed"); }
+    memcpy(o, idxb.data(), 4 * n);
+    o[n] = (uint32_t)m;
+    memcpy(a, adjb.data(), 4 * m);
+    memset(a + m, 0, 16);
+    for (int64_t i = 0; i < n; i++) {
+      if (o[i] > o[i + 1]) { free(o); free(a); return fail(RG_EFORMAT, "offsets not monotone"); }
+    }
+    for (int64_t i = 0; i < m; i++) {
+      if (a[i] >= (uint64_t)n) { free(o); free(a); return fail(RG_EFORMAT, "edge id >= n"); }
+    }
+    *n_out = n; *m_out = m; *off_out = o; *adj_out = a;
+    return RG_OK;
+  }
+  std::vector<char> s;
+  if (!read_file(path, s)) return fail(RG_EIO, "rg_read_graph: Unable to open file: %s", path);
+  s.push_back('\0');
+  size_t p = 0, len = s.size() - 1;
+  auto next_word = [&](size_t& b, size_t& e) -> bool {
+    while (p < len && is_space(s[p])) p++;
+    if (p >= len) return false;
+    b = p;
+    while (p < len && !is_space(s[p])) p++;
+    e = p;
+    return true;
+  };
+  size_t b, e;
+  if (!next_word(b, e) || std::string(&s[b], e - b) != "AdjacencyGraph") {
+    return fail(RG_EFORMAT, "rg_read_graph: Bad input file (header)");
+  }
+  auto next_num = [&](uint64_t& v) -> bool {
+    size_t bb, ee;
+    if (!next_word(bb, ee)) return false;
+    uint64_t x = 0;
+    for (size_t i = bb; i < ee; i++) {
+      if (s[i] < '0' || s[i] > '9') return false;
+      x = x * 10 + (uint64_t)(s[i] - '0');
+    }
+    v = x;
+    return true;
+  };
+  uint64_t n = 0, m = 0;
+  if (!next_num(n) || !next_num(m) || n == 0) return fail(RG_EFORMAT, "rg_read_graph: Bad input file (n/m)");
+  if (m > 0xFFFFFFFFull) return fail(RG_EUNSUPPORTED, "rg_read_graph: >= 2^32 edges");
+  std::vector<uint32_t> off(n + 1);
+  std::vector<uint32_t> tmp(m);
+  for (uint64_t i = 0; i < n; i++) {
+    uint64_t v;
+    if (!next_num(v) || v > m) return fail(RG_EFORMAT, "rg_read_graph: Bad input file (offsets)");
+    off[i] = (uint32_t)v;
+  }
+  off[n] = (uint32_t)m;
+  for (uint64_t i = 0; i < m; i++) {
+    uint64_t v;
+    if (!next_num(v) || v >= n) return fail(RG_EFORMAT, "rg_read_graph: Bad input file (edges)");
+    tmp[i] = (uint32_t)v;
+  }
+  uint64_t extra;
+  if (next_num(extra)) return fail(RG_EFORMAT, "rg_read_graph: Bad input file (trailing data)");
+  for (uint64_t i = 0; i < n; i++) {
+    if (off[i] > off[i + 1]) return fail(RG_EFORMAT, "rg_read_graph: offsets not monotone");
+  }
+  *n_out = (int64_t)n;
+  return clean_and_pack((int64_t)n, off, tmp, off_out, adj_out, m_out);
+}
+
+}  // namespace rg

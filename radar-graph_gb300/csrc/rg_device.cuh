@@ -1,0 +1,154 @@
+// Internal device-side declarations: the device graph image, the frontier,
+// per-graph workspace, and small primitives (scan, block reductions).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "rg_host.h"
+
+namespace rg {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;  // UINT_E_MAX
+constexpr int kSweepChunk = 512;         // edges per warp chunk of a full-graph sweep
+
+rg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define RG_CUDA(...)                                                                  \
+  do {                                                                                \
+    cudaError_t e_ = (__VA_ARGS__);                                                   \
+    if (e_ != cudaSuccess) return ::rg::cuda_fail(e_, #__VA_ARGS__, __FILE__, __LINE__); \
+  } while (0)
+#define RG_TRY(...)                 \
+  do {                              \
+    rg_status s_ = (__VA_ARGS__);   \
+    if (s_ != RG_OK) return s_;     \
+  } while (0)
+
+// Kernel view of a symmetric CSR graph.
+struct DevGraph {
+  uint32_t n;
+  uint32_t m;
+  const uint32_t* __restrict__ off;  // n+1
+  const uint32_t* __restrict__ adj;  // m (+4 zero padding, 16-byte aligned)
+};
+
+// A device allocation that frees itself.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // Grows (never shrinks) to at least `b` bytes; contents are not kept.
+  rg_status reserve(size_t b);
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Device frontier: compacted queue of ids (ascending when produced by the
+// engine), the exclusive scan of their degrees (for edge-balanced push), and
+// a bitmap.  `count`/`degsum` mirror the device values after a sync.
+struct Frontier {
+  DevBuf queue;   // n+64 ids
+  DevBuf qoff;    // n+65 scan entries
+  DevBuf bits;    // (n+31)/32 words (+pad)
+  int64_t count = 0;
+  int64_t degsum = 0;
+  bool queue_valid = false;
+  bool bits_valid = false;
+};
+
+// Scratch reused by every call on a graph (no per-level cudaMalloc).
+struct Workspace {
+  DevBuf scan_partials;  // scan / compaction block partials
+  DevBuf scan_tmp;
+  DevBuf counters;       // small device scalars
+  uint64_t* h_info = nullptr;  // pinned host mirror of level info (count, degsum, ...)
+  ~Workspace();
+};
+
+}  // namespace rg
+
+struct rg_graph {
+  int device = 0;
+  int64_t n = 0, m = 0;
+  rg::DevBuf off, adj;          // CSR on the device
+  rg::DevBuf chunk_v;           // sweep partition: first vertex of every kSweepChunk edges
+  int64_t nchunks = 0;
+  bool sorted = false;
+  rg::DevBuf new_ids;           // orig -> internal (when sorted)
+  std::vector<uint32_t> h_new_ids;  // same on the host (empty when not sorted)
+  std::vector<uint32_t> h_deg;      // degree by internal id
+  uint32_t max_deg = 0;
+  rg::Workspace ws;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  rg::DevGraph view() const {
+    return rg::DevGraph{(uint32_t)n, (uint32_t)m, off.as<uint32_t>(), adj.as<uint32_t>()};
+  }
+  ~rg_graph();
+};
+
+struct rg_frontier {
+  const rg_graph* g = nullptr;
+  rg::Frontier f;
+};
+
+namespace rg {
+
+// Exclusive scan of `n` uint32 values into out[0..n] (out[n] = total).
+// Total must fit 32 bits.  Uses ws.scan_partials.  Async on `st`.
+rg_status scan_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st);
+
+// Builds frontier f (queue+qoff, ascending) from its bitmap.  Writes
+// (count, degsum) into ws.h_info[0..1] and syncs the stream if `sync`.
+// Optional epilogues: depth[v] = level for every member; or_into |= bits.
+rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool sync,
+                       int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr,
+                       uint32_t* queue_out = nullptr, uint32_t* qoff_out = nullptr);
+
+// Sets a frontier from host ids (queue + qoff from host degrees + bitmap).
+rg_status frontier_from_host(const rg_graph* g, Frontier& f, const uint32_t* ids, int64_t k,
+                             cudaStream_t st);
+rg_status frontier_alloc(const rg_graph* g, Frontier& f);
+rg_status frontier_set_all(const rg_graph* g, Frontier& f, cudaStream_t st);
+// Bitmap from the current queue (clears first).
+rg_status frontier_bits_from_queue(const rg_graph* g, Frontier& f, cudaStream_t st);
+
+// ---- small device helpers ------------------------------------------------
+
+__device__ __forceinline__ bool bit_test(const uint32_t* bits, uint32_t v) {
+  return (bits[v >> 5] >> (v & 31)) & 1u;
+}
+// Sets bit v; skips the atomic when a plain read already shows it set.
+__device__ __forceinline__ void bit_set(uint32_t* bits, uint32_t v) {
+  uint32_t b = 1u << (v & 31);
+  if (!(__ldcg(bits + (v >> 5)) & b)) atomicOr(bits + (v >> 5), b);
+}
+
+// Largest i in [lo, hi] with a[i] <= x (a non-decreasing, a[lo] <= x).
+template <class T>
+__device__ __forceinline__ uint32_t upper_index(const T* a, uint32_t lo, uint32_t hi, uint32_t x) {
+  while (lo < hi) {
+    uint32_t mid = lo + ((hi - lo + 1) >> 1);
+    if (a[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace rg

@@ -1,0 +1,352 @@
+"""Python mirror of the librg.so C ABI (include/radar_graph.h).
+
+This is the host-side face of the GB300 frontier engine for Python callers:
+it mirrors the reference's per-app Compute(graph, P) interface
+(PageRank.C:120, BFS.C:122, BC-manyiter-v2.C:205, Radii.C:140) and the
+Ligra command-line options (-s, -r, -maxiters, -preprocess, -b) through
+`run_app`.  Arrays are numpy; every call checks the returned rg_status and
+raises RgError with the library's message.  There is no CPU fallback: if
+librg.so is missing or no GPU is present, calls raise.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "librg.so")
+
+VARIANTS = {"push": 0, "push-pull": 1, "degree-sorting": 2, "hubdup": 3, "radar": 4}
+# variants whose reference binaries degree-sort the graph before Compute by
+# default (-preprocess 1, ligra.h:566 in RADAR and degree-sorting)
+SORTED_VARIANTS = ("degree-sorting", "radar")
+
+OPS = {"pagerank": 0, "bfs": 1, "bc_fwd": 2, "bc_bwd": 3, "radii": 4}
+VOPS = {"pr_damp": 0, "bc_visit": 1, "bc_back": 2, "radii_sync": 3}
+NO_OUTPUT = 1
+DENSE_FORWARD = 8
+
+STATUS = {0: "RG_OK", 1: "RG_EINVAL", 2: "RG_ENOMEM", 3: "RG_ECUDA", 4: "RG_EIO",
+          5: "RG_EFORMAT", 6: "RG_EUNSUPPORTED", 7: "RG_ETIMEOUT", 8: "RG_ENODEV"}
+
+
+class RgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Timing(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("edge_ms", C.c_double), ("edges_traversed", C.c_int64),
+                ("algorithmic_bytes", C.c_int64), ("edge_launches", C.c_int64),
+                ("kernel_launches", C.c_int64)]
+
+
+class OpArgs(C.Structure):
+    _fields_ = [("p_curr", C.c_void_p), ("p_next", C.c_void_p), ("parents", C.c_void_p),
+                ("num_paths", C.c_void_p), ("deps", C.c_void_p), ("visited_bits", C.c_void_p),
+                ("visited", C.c_void_p), ("next_visited", C.c_void_p), ("radii", C.c_void_p),
+                ("round", C.c_int32)]
+
+
+_lib = None
+
+_P = C.POINTER
+_u32p = _P(C.c_uint32)
+_i32p = _P(C.c_int32)
+_i64p = _P(C.c_int64)
+_f64p = _P(C.c_double)
+_u8p = _P(C.c_uint8)
+
+# name -> argtypes (restype is always c_int = rg_status unless listed in _RESTYPE)
+_SIGS = {
+    "rg_last_error": [], "rg_status_str": [C.c_int], "rg_version": [],
+    "rg_generate_edges": [C.c_int, C.c_int, C.c_uint64, C.c_int, _u32p, _u32p],
+    "rg_csr_from_edges": [C.c_int64, C.c_int64, _u32p, _u32p, _P(_u32p), _P(_u32p), _i64p],
+    "rg_write_adjacency": [C.c_char_p, C.c_int64, C.c_int64, _u32p, _u32p],
+    "rg_read_graph": [C.c_char_p, C.c_int, C.c_int, _i64p, _i64p, _P(_u32p), _P(_u32p)],
+    "rg_host_free": [C.c_void_p],
+    "rg_graph_create": [C.c_int64, C.c_int64, _u32p, _u32p, C.c_void_p],
+    "rg_graph_create_device": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p],
+    "rg_graph_degree_sort": [C.c_void_p, C.c_void_p, _u32p],
+    "rg_graph_info": [C.c_void_p, _i64p, _i64p, _i32p],
+    "rg_graph_download": [C.c_void_p, _u32p, _u32p, _u32p],
+    "rg_graph_free": [C.c_void_p],
+    "rg_pagerank": [C.c_void_p, C.c_int, C.c_int64, _f64p, _i64p, _f64p],
+    "rg_bfs": [C.c_void_p, C.c_int, C.c_uint32, _u32p, _i32p, _i64p, _i64p],
+    "rg_bc": [C.c_void_p, C.c_int, C.c_int, _f64p, _i64p],
+    "rg_bc_sources": [C.c_void_p, C.c_int, _u32p, C.c_int, _f64p, _i64p],
+    "rg_bc_pick_sources": [C.c_void_p, C.c_int, _u32p],
+    "rg_radii": [C.c_void_p, C.c_int, _i32p, _i64p],
+    "rg_radii_seeds": [C.c_void_p, C.c_int, _u32p, C.c_int, _i32p, _i64p],
+    "rg_frontier_create": [C.c_void_p, C.c_void_p],
+    "rg_frontier_free": [C.c_void_p],
+    "rg_frontier_set": [C.c_void_p, _u32p, C.c_int64],
+    "rg_frontier_set_all": [C.c_void_p],
+    "rg_frontier_count": [C.c_void_p, _i64p],
+    "rg_frontier_get": [C.c_void_p, _u8p],
+    "rg_edgemap": [C.c_void_p, C.c_void_p, C.c_int, _P(OpArgs), C.c_void_p, C.c_uint32, C.c_int64,
+                   C.c_void_p],
+    "rg_vertexmap": [C.c_void_p, C.c_void_p, C.c_int, _P(OpArgs), C.c_void_p],
+    "rg_device_alloc": [C.c_size_t, _P(C.c_void_p)],
+    "rg_device_free": [C.c_void_p],
+    "rg_copy_to_device": [C.c_void_p, C.c_void_p, C.c_size_t],
+    "rg_copy_to_host": [C.c_void_p, C.c_void_p, C.c_size_t],
+    "rg_synchronize": [],
+    "rg_last_timing": [_P(Timing)],
+}
+_RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
+            "rg_host_free": None}
+
+
+def exported_symbols():
+    """Names the C ABI exports (every function declared in include/*.h)."""
+    return sorted(_SIGS)
+
+
+def lib():
+    """Loads librg.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RgError(8, f"{LIB_PATH} is missing; build it with radar-graph_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RESTYPE.get(name, C.c_int)
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        msg = lib().rg_last_error()
+        raise RgError(status, msg.decode() if msg else "")
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(_P(t))
+
+
+def version():
+    return lib().rg_version().decode()
+
+
+def last_timing():
+    t = Timing()
+    _check(lib().rg_last_timing(C.byref(t)))
+    return {k: getattr(t, k) for k, _ in Timing._fields_}
+
+
+# ---------------------------------------------------------------------------
+# input formats (host side)
+# ---------------------------------------------------------------------------
+
+def generate_edges(scale, edge_factor, seed=1, uniform=False):
+    """Seeded R-MAT / Erdos-Renyi edge list (GAP generator algorithm)."""
+    ne = edge_factor << scale
+    src = np.empty(ne, np.uint32)
+    dst = np.empty(ne, np.uint32)
+    _check(lib().rg_generate_edges(scale, edge_factor, seed, 1 if uniform else 0, _ptr(src, C.c_uint32),
+                                   _ptr(dst, C.c_uint32)))
+    return src, dst
+
+
+def _take_host_csr(n, m, po, pa):
+    off = np.ctypeslib.as_array(po, shape=(n + 1,)).copy()
+    adj = np.ctypeslib.as_array(pa, shape=(max(m, 1),))[:m].copy()
+    lib().rg_host_free(C.cast(po, C.c_void_p))
+    lib().rg_host_free(C.cast(pa, C.c_void_p))
+    return off, adj
+
+
+def csr_from_edges(n, src, dst):
+    """Symmetric CSR (both directions, sorted, deduplicated, no self-loops)."""
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    po, pa, m = _u32p(), _u32p(), C.c_int64()
+    _check(lib().rg_csr_from_edges(n, len(src), _ptr(src, C.c_uint32), _ptr(dst, C.c_uint32), C.byref(po),
+                                   C.byref(pa), C.byref(m)))
+    return _take_host_csr(n, m.value, po, pa)
+
+
+def rmat_csr(scale, edge_factor, seed=1, uniform=False):
+    src, dst = generate_edges(scale, edge_factor, seed, uniform)
+    return csr_from_edges(1 << scale, src, dst)
+
+
+def write_adjacency(path, off, adj):
+    off = np.ascontiguousarray(off, np.uint32)
+    adj = np.ascontiguousarray(adj, np.uint32)
+    _check(lib().rg_write_adjacency(str(path).encode(), len(off) - 1, len(adj), _ptr(off, C.c_uint32),
+                                    _ptr(adj, C.c_uint32)))
+
+
+def read_graph(path, symmetric=True, binary=False):
+    """Ligra text (or binary) graph -> cleaned symmetric CSR (off, adj)."""
+    n, m, po, pa = C.c_int64(), C.c_int64(), _u32p(), _u32p()
+    _check(lib().rg_read_graph(str(path).encode(), 1 if symmetric else 0, 1 if binary else 0, C.byref(n),
+                               C.byref(m), C.byref(po), C.byref(pa)))
+    return _take_host_csr(n.value, m.value, po, pa)
+
+
+# ---------------------------------------------------------------------------
+# device graph and apps
+# ---------------------------------------------------------------------------
+
+def _variant(v):
+    if isinstance(v, str):
+        if v not in VARIANTS:
+            raise ValueError(f"unknown variant {v!r}; one of {list(VARIANTS)}")
+        return VARIANTS[v]
+    return int(v)
+
+
+class Graph:
+    """A device-resident CSR image (rg_graph)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+        n, m, s = C.c_int64(), C.c_int64(), C.c_int32()
+        _check(lib().rg_graph_info(self._h, C.byref(n), C.byref(m), C.byref(s)))
+        self.n, self.m, self.sorted = n.value, m.value, bool(s.value)
+
+    @classmethod
+    def from_csr(cls, off, adj):
+        off = np.ascontiguousarray(off, np.uint32)
+        adj = np.ascontiguousarray(adj, np.uint32)
+        h = C.c_void_p()
+        _check(lib().rg_graph_create(len(off) - 1, len(adj), _ptr(off, C.c_uint32), _ptr(adj, C.c_uint32),
+                                     C.byref(h)))
+        return cls(h)
+
+    def degree_sort(self):
+        """New graph relabelled by degree (preprocessGraph); .new_ids set."""
+        h = C.c_void_p()
+        ids = np.empty(self.n, np.uint32)
+        _check(lib().rg_graph_degree_sort(self._h, C.byref(h), _ptr(ids, C.c_uint32)))
+        g = Graph(h)
+        g.new_ids = ids
+        return g
+
+    def download(self):
+        off = np.empty(self.n + 1, np.uint32)
+        adj = np.empty(max(self.m, 1), np.uint32)
+        ids = np.empty(self.n, np.uint32)
+        _check(lib().rg_graph_download(self._h, _ptr(off, C.c_uint32), _ptr(adj, C.c_uint32),
+                                       _ptr(ids, C.c_uint32)))
+        return off, adj[:self.m], ids
+
+    def free(self):
+        if self._h is not None and self._h.value:
+            lib().rg_graph_free(self._h)
+        self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.free()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- apps ---------------------------------------------------------------
+    def pagerank(self, variant="push", max_iters=100):
+        ranks = np.empty(self.n, np.float64)
+        it, l1 = C.c_int64(), C.c_double()
+        _check(lib().rg_pagerank(self._h, _variant(variant), max_iters, _ptr(ranks, C.c_double), C.byref(it),
+                                 C.byref(l1)))
+        return ranks, it.value, l1.value
+
+    def bfs(self, variant="push", root=0):
+        parents = np.empty(self.n, np.uint32)
+        depth = np.empty(self.n, np.int32)
+        rounds, reached = C.c_int64(), C.c_int64()
+        _check(lib().rg_bfs(self._h, _variant(variant), root, _ptr(parents, C.c_uint32), _ptr(depth, C.c_int32),
+                            C.byref(rounds), C.byref(reached)))
+        return parents, depth, rounds.value, reached.value
+
+    def bc(self, variant="push", max_iters=16):
+        deps = np.empty(self.n, np.float64)
+        lv = C.c_int64()
+        _check(lib().rg_bc(self._h, _variant(variant), max_iters, _ptr(deps, C.c_double), C.byref(lv)))
+        return deps, lv.value
+
+    def bc_sources(self, sources, variant="push"):
+        s = np.ascontiguousarray(sources, np.uint32)
+        deps = np.empty(self.n, np.float64)
+        lv = C.c_int64()
+        _check(lib().rg_bc_sources(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s),
+                                   _ptr(deps, C.c_double), C.byref(lv)))
+        return deps, lv.value
+
+    def bc_pick_sources(self, k):
+        out = np.empty(k, np.uint32)
+        _check(lib().rg_bc_pick_sources(self._h, k, _ptr(out, C.c_uint32)))
+        return out
+
+    def radii(self, variant="push"):
+        r = np.empty(self.n, np.int32)
+        rounds = C.c_int64()
+        _check(lib().rg_radii(self._h, _variant(variant), _ptr(r, C.c_int32), C.byref(rounds)))
+        return r, rounds.value
+
+    def radii_seeds(self, seeds, variant="push"):
+        s = np.ascontiguousarray(seeds, np.uint32)
+        r = np.empty(self.n, np.int32)
+        rounds = C.c_int64()
+        _check(lib().rg_radii_seeds(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s), _ptr(r, C.c_int32),
+                                    C.byref(rounds)))
+        return r, rounds.value
+
+
+def radii_seeds_orig(n):
+    """Radii sample vertices hashInt(i) % n for i < min(n, 64) (Radii.C:162-169)."""
+    M = (1 << 64) - 1
+    out = []
+    for i in range(min(n, 64)):
+        a = i
+        a = ((a + 0x7ed55d166bef7a1d) + (a << 12)) & M
+        a = ((a ^ 0xc761c23c510fa2dd) ^ (a >> 9)) & M
+        a = ((a + 0x165667b183a9c0e1) + (a << 59)) & M
+        a = ((a + 0xd3a2646cab3487e3) ^ (a << 49)) & M
+        a = ((a + 0xfd7046c5ef9ab54c) + (a << 3)) & M
+        a = ((a ^ 0xb55a4f090dd4a67b) ^ (a >> 32)) & M
+        out.append(a % n)
+    return np.array(out, np.uint32)
+
+
+def run_app(app, off, adj, variant="push", maxiters=None, root=0, preprocess=None):
+    """parallel_main + Compute of one reference app (ligra.h:556-651).
+
+    app: "PageRank" | "BFS" | "BC" | "Radii".  preprocess: None = the variant's
+    default (degree sort for degree-sorting and RADAR), 1/0 = sort, -1 = none.
+    Returns the app's per-vertex output in ORIGINAL id order.
+    """
+    if preprocess is None:
+        preprocess = 1 if variant in SORTED_VARIANTS else -1
+    with Graph.from_csr(off, adj) as g0:
+        g = g0.degree_sort() if preprocess in (0, 1) else g0
+        try:
+            if app == "PageRank":
+                return g.pagerank(variant, 100 if maxiters is None else maxiters)
+            if app == "BFS":
+                return g.bfs(variant, root)
+            if app == "BC":
+                return g.bc(variant, 16 if maxiters is None else maxiters)
+            if app == "Radii":
+                return g.radii(variant)
+            raise ValueError(f"unknown app {app}")
+        finally:
+            if g is not g0:
+                g.free()
