@@ -226,6 +226,9 @@ typedef struct rg_timing {
   int64_t kernel_launches;  /* all kernel launches of the call */
 } rg_timing;
 rg_status rg_last_timing(rg_timing* t);
+/* on != 0: every edge-kernel launch of the following app calls is bracketed
+ * by CUDA events on its stream and rg_timing.edge_ms reports their sum. */
+rg_status rg_set_kernel_timing(int on);
 
 #ifdef __cplusplus
 }

@@ -25,10 +25,31 @@ namespace rg {
 // ---------------------------------------------------------------------------
 static thread_local rg_timing g_timing;
 
+// Optional per-launch timing of edge kernels (rg_set_kernel_timing).
+static bool g_kernel_timing = false;
+static thread_local std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_kt_events;
+static thread_local size_t g_kt_used = 0;
+
+static void kt_begin(cudaStream_t st) {
+  if (!g_kernel_timing) return;
+  if (g_kt_used == g_kt_events.size()) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return;
+    g_kt_events.push_back({a, b});
+  }
+  cudaEventRecord(g_kt_events[g_kt_used].first, st);
+}
+static void kt_end(cudaStream_t st) {
+  if (!g_kernel_timing || g_kt_used >= g_kt_events.size()) return;
+  cudaEventRecord(g_kt_events[g_kt_used].second, st);
+  g_kt_used++;
+}
+
 struct CallTimer {
   rg_graph* g;
   explicit CallTimer(rg_graph* gr) : g(gr) {
     memset(&g_timing, 0, sizeof g_timing);
+    g_kt_used = 0;
     cudaEventRecord(g->ev0, g->stream);
   }
   rg_status stop() {
@@ -37,6 +58,13 @@ struct CallTimer {
     float ms = 0;
     RG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
     g_timing.total_ms = ms;
+    double edge = 0;
+    for (size_t i = 0; i < g_kt_used; i++) {
+      float e = 0;
+      RG_CUDA(cudaEventElapsedTime(&e, g_kt_events[i].first, g_kt_events[i].second));
+      edge += e;
+    }
+    g_timing.edge_ms = edge;
     return RG_OK;
   }
 };
@@ -182,8 +210,10 @@ static rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const H
     grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * per_sm);
   }
   if (grid < 1) grid = 1;
+  kt_begin(st);
   kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, (uint32_t)in.count, (uint32_t)in.degsum, op, hub,
                               next_bits);
+  kt_end(st);
   RG_CUDA(cudaGetLastError());
   g_timing.kernel_launches++;
   g_timing.edge_launches++;
@@ -205,7 +235,9 @@ static rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out
     if (dense && !o.dense_forward) {
       const int64_t groups_per_block = 256 / 8;
       int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
+      kt_begin(st);
       pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), in.bits, op, nb);
+      kt_end(st);
       RG_CUDA(cudaGetLastError());
       g_timing.kernel_launches++;
       g_timing.edge_launches++;
@@ -499,6 +531,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   for (int64_t it = 0; it < max_iters; it++) {
     const double* prev = it ? L1 + it - 1 : nullptr;
     if (g->m > 0) {
+      kt_begin(st);
       if (variant == RG_PUSH_PULL) {
         pr_pull_sweep<<<sweep_grid, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C,
                                                   acc, prev);
@@ -506,6 +539,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
         sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C, acc,
                                                hub, prev);
       }
+      kt_end(st);
       RG_CUDA(cudaGetLastError());
       g_timing.kernel_launches++;
       g_timing.edge_launches++;
@@ -878,6 +912,11 @@ rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* r
 rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k, int32_t* h_radii,
                          int64_t* rounds_out) {
   return radii_run(g, variant, h_seeds, k, h_radii, rounds_out, 0);
+}
+
+rg_status rg_set_kernel_timing(int on) {
+  g_kernel_timing = on != 0;
+  return RG_OK;
 }
 
 rg_status rg_last_timing(rg_timing* t) {

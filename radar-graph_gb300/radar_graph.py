@@ -95,6 +95,7 @@ _SIGS = {
     "rg_copy_to_host": [C.c_void_p, C.c_void_p, C.c_size_t],
     "rg_synchronize": [],
     "rg_last_timing": [_P(Timing)],
+    "rg_set_kernel_timing": [C.c_int],
 }
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
             "rg_host_free": None}
@@ -138,6 +139,11 @@ def last_timing():
     t = Timing()
     _check(lib().rg_last_timing(C.byref(t)))
     return {k: getattr(t, k) for k, _ in Timing._fields_}
+
+
+def set_kernel_timing(on):
+    """Bracket every edge-kernel launch with CUDA events (see last_timing()['edge_ms'])."""
+    _check(lib().rg_set_kernel_timing(1 if on else 0))
 
 
 # ---------------------------------------------------------------------------
