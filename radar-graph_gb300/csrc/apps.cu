@@ -15,6 +15,7 @@
 #include <random>
 #include <vector>
 
+#include "app_common.cuh"
 #include "engine.cuh"
 #include "rg_device.cuh"
 
@@ -23,14 +24,12 @@ namespace rg {
 // ---------------------------------------------------------------------------
 // per-call timing and launch accounting
 // ---------------------------------------------------------------------------
-static thread_local rg_timing g_timing;
+thread_local rg_timing g_timing;
+bool g_kernel_timing = false;
+thread_local std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_kt_events;
+thread_local size_t g_kt_used = 0;
 
-// Optional per-launch timing of edge kernels (rg_set_kernel_timing).
-static bool g_kernel_timing = false;
-static thread_local std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_kt_events;
-static thread_local size_t g_kt_used = 0;
-
-static void kt_begin(cudaStream_t st) {
+void kt_begin(cudaStream_t st) {
   if (!g_kernel_timing) return;
   if (g_kt_used == g_kt_events.size()) {
     cudaEvent_t a, b;
@@ -39,37 +38,35 @@ static void kt_begin(cudaStream_t st) {
   }
   cudaEventRecord(g_kt_events[g_kt_used].first, st);
 }
-static void kt_end(cudaStream_t st) {
+void kt_end(cudaStream_t st) {
   if (!g_kernel_timing || g_kt_used >= g_kt_events.size()) return;
   cudaEventRecord(g_kt_events[g_kt_used].second, st);
   g_kt_used++;
 }
 
-struct CallTimer {
-  rg_graph* g;
-  explicit CallTimer(rg_graph* gr) : g(gr) {
-    memset(&g_timing, 0, sizeof g_timing);
-    g_kt_used = 0;
-    cudaEventRecord(g->ev0, g->stream);
-  }
-  rg_status stop() {
-    RG_CUDA(cudaEventRecord(g->ev1, g->stream));
-    RG_CUDA(cudaEventSynchronize(g->ev1));
-    float ms = 0;
-    RG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
-    g_timing.total_ms = ms;
-    double edge = 0;
-    for (size_t i = 0; i < g_kt_used; i++) {
-      float e = 0;
-      RG_CUDA(cudaEventElapsedTime(&e, g_kt_events[i].first, g_kt_events[i].second));
-      edge += e;
-    }
-    g_timing.edge_ms = edge;
-    return RG_OK;
-  }
-};
+CallTimer::CallTimer(rg_graph* gr) : g(gr) {
+  memset(&g_timing, 0, sizeof g_timing);
+  g_kt_used = 0;
+  cudaEventRecord(g->ev0, g->stream);
+}
 
-static int device_sms() {
+rg_status CallTimer::stop() {
+  RG_CUDA(cudaEventRecord(g->ev1, g->stream));
+  RG_CUDA(cudaEventSynchronize(g->ev1));
+  float ms = 0;
+  RG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+  g_timing.total_ms = ms;
+  double edge = 0;
+  for (size_t i = 0; i < g_kt_used; i++) {
+    float e = 0;
+    RG_CUDA(cudaEventElapsedTime(&e, g_kt_events[i].first, g_kt_events[i].second));
+    edge += e;
+  }
+  g_timing.edge_ms = edge;
+  return RG_OK;
+}
+
+int device_sms() {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -79,7 +76,7 @@ static int device_sms() {
   }
   return sms;
 }
-static int max_dyn_smem() {
+int max_dyn_smem() {
   static int v = 0;
   if (!v) {
     int dev = 0;
@@ -104,14 +101,15 @@ static std::vector<HubCache*> g_hub_cache;
 
 // Hub slots that fit the shared-memory budget for an element of `elem` bytes
 // next to the push kernel's static staging arrays.
-static uint32_t hub_budget(size_t elem, int64_t n) {
-  size_t static_bytes = 3 * sizeof(uint32_t) * (kHubPushThreads * kPushItems + 1) + 64;
+uint32_t hub_budget(size_t elem, int64_t n) {
+  constexpr int kTile = kHubPushThreads * kPushItems;
+  size_t static_bytes = sizeof(uint32_t) * (kTile + 3 * (kTile + 1)) + 256;
   size_t dyn = (size_t)max_dyn_smem() - static_bytes - 1024;
   uint64_t h = dyn / elem;
   return (uint32_t)std::min<uint64_t>(h, (uint64_t)n);
 }
 
-static rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
+rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
   HubCache* hc = nullptr;
   for (HubCache* c : g_hub_cache) if (c->g == g && c->requested == H) hc = c;
   if (!hc) {
@@ -156,7 +154,7 @@ void drop_hub_cache(const rg_graph* g) {
   }
 }
 
-static int hub_mode_of(int variant) {
+int hub_mode_of(int variant) {
   return variant == RG_RADAR ? kHubPrefix : variant == RG_HUBDUP ? kHubMap : kHubNone;
 }
 
@@ -200,8 +198,10 @@ static rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const H
   } else {
     static bool attr_set = false;
     if (!attr_set) {
+      cudaFuncAttributes fa;
+      RG_CUDA(cudaFuncGetAttributes(&fa, kern));
       RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   max_dyn_smem() - 3 * 4 * (kTile + 1) - 64));
+                                   max_dyn_smem() - (int)fa.sharedSizeBytes));
       attr_set = true;
     }
     int per_sm = 0;
@@ -210,8 +210,14 @@ static rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const H
     grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * per_sm);
   }
   if (grid < 1) grid = 1;
+  Workspace& ws = g->ws;
+  RG_TRY(ws.tiles.reserve(sizeof(uint32_t) * (tiles + 2)));
+  tile_starts<<<(unsigned)((tiles + 1 + 255) / 256), 256, 0, st>>>(in.qoff, (uint32_t)in.count,
+                                                                    (uint32_t)in.degsum, kTile, (uint32_t)tiles,
+                                                                    ws.tiles.as<uint32_t>());
+  g_timing.kernel_launches++;
   kt_begin(st);
-  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, (uint32_t)in.count, (uint32_t)in.degsum, op, hub,
+  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
                               next_bits);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
@@ -273,302 +279,11 @@ static rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out
 // ---------------------------------------------------------------------------
 // small vertex kernels
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void fill_kernel(T* a, int64_t n, T v) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
-}
-template <class T>
-static void fill(T* a, int64_t n, T v, cudaStream_t st) {
-  int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
-  fill_kernel<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(a, n, v);
-  g_timing.kernel_launches++;
-}
-
-// out[v] = in[new_ids[v]]: results in original-id order (writeOutputToFile).
-template <class T>
-__global__ void gather_kernel(const T* __restrict__ in, const uint32_t* __restrict__ new_ids, int64_t n,
-                              T* __restrict__ out) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = in[new_ids[i]];
-}
-
-template <class T>
-static rg_status download_orig(rg_graph* g, const T* d_arr, T* h_out, DevBuf& tmp, cudaStream_t st) {
-  if (!h_out) return RG_OK;
-  const T* src = d_arr;
-  if (g->sorted) {
-    RG_TRY(tmp.reserve(sizeof(T) * g->n));
-    int64_t blocks = std::min<int64_t>((g->n + 255) / 256, (int64_t)device_sms() * 32);
-    gather_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(d_arr, g->new_ids.as<uint32_t>(), g->n, tmp.as<T>());
-    RG_CUDA(cudaGetLastError());
-    g_timing.kernel_launches++;
-    src = tmp.as<T>();
-  }
-  RG_CUDA(cudaMemcpyAsync(h_out, src, sizeof(T) * g->n, cudaMemcpyDeviceToHost, st));
-  return RG_OK;
-}
-
-static uint32_t to_internal(const rg_graph* g, uint32_t orig) {
+uint32_t to_internal(const rg_graph* g, uint32_t orig) {
   return g->sorted ? g->h_new_ids[orig] : orig;
 }
 
-// ---------------------------------------------------------------------------
-// PageRank (PageRank.C:120-189)
-// ---------------------------------------------------------------------------
-constexpr double kDamping = 0.85;
-constexpr int kSweepThreads = 1024;
-constexpr double kEpsilon = 0.0000001;
-
-__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p_curr, double* acc, double* contrib,
-                        double one_over_n) {
-  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    p_curr[v] = one_over_n;
-    acc[v] = 0.0;
-    uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? one_over_n / (double)d : 0.0;
-  }
-}
-
-__device__ __forceinline__ bool pr_converged(const double* l1_prev) {
-  return l1_prev != nullptr && *l1_prev < kEpsilon;
-}
-
-// Dense push over every edge (edgeMapDenseForward with a full frontier):
-// acc[d] += contrib[s].  Each warp owns kSweepChunk consecutive edges read as
-// 16-byte vectors; chunk_v gives the chunk's first source so a lane finds its
-// source with a short search.
-template <int kHub>
-__global__ void __launch_bounds__(1024) pr_push_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
-                                                     uint32_t nchunks, const double* __restrict__ contrib,
-                                                     double* acc, HubInfo hub, const double* l1_prev) {
-  if (pr_converged(l1_prev)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* hs = reinterpret_cast<double*>(smem_raw);
-  if (kHub != kHubNone) {
-    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = 0.0;
-    __syncthreads();
-  }
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t c = warp; c < nchunks; c += nwarps) {
-    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
-#pragma unroll
-    for (int r = 0; r < kSweepChunk / 128; r++) {
-      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
-      if (e < g.m) {
-        const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
-        uint32_t s = upper_index(g.off, vlo, vhi, e);
-        uint32_t nxt = g.off[s + 1];
-        double cs = contrib[s];
-        const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (ee >= nxt) {
-            do { s++; nxt = g.off[s + 1]; } while (ee >= nxt);
-            cs = contrib[s];
-          }
-          const uint32_t d = dd[i];
-          uint32_t slot;
-          if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) atomicAdd(hs + slot, cs);
-          else atomicAdd(acc + d, cs);
-        }
-      }
-    }
-  }
-  if (kHub != kHubNone) {
-    __syncthreads();
-    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) {
-      const double x = hs[h];
-      if (x != 0.0) atomicAdd(acc + hub_vertex<kHub>(hub, h), x);
-    }
-  }
-}
-
-// Dense pull over every vertex (edgeMapDense with a full frontier, push-pull
-// variant): acc[v] = sum over in-neighbours u of contrib[u].  Edge-balanced
-// like the push sweep; partial sums of a row are combined across the warp by
-// a segmented scan (rows are non-decreasing across lanes) and added once per
-// row piece.
-__global__ void __launch_bounds__(256) pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
-                                                     uint32_t nchunks, const double* __restrict__ contrib,
-                                                     double* acc, const double* l1_prev) {
-  if (pr_converged(l1_prev)) return;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t c = warp; c < nchunks; c += nwarps) {
-    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
-#pragma unroll
-    for (int r = 0; r < kSweepChunk / 128; r++) {
-      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
-      uint32_t row = 0xFFFFFFFFu;
-      double part = 0.0;
-      if (e < g.m) {
-        const uint4 u4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
-        uint32_t v = upper_index(g.off, vlo, vhi, e);
-        uint32_t nxt = g.off[v + 1];
-        const uint32_t uu[4] = {u4.x, u4.y, u4.z, u4.w};
-        row = v;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (ee >= nxt) {
-            atomicAdd(acc + row, part);  // a row piece that ends inside this lane
-            part = 0.0;
-            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
-            row = v;
-          }
-          part += contrib[uu[i]];
-        }
-      }
-      // segmented inclusive scan of the lanes' last row pieces
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, part, o);
-        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
-        if (lane >= o && tr == row) part += t;
-      }
-      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
-      if (row != 0xFFFFFFFFu && (lane == 31 || next_row != row)) atomicAdd(acc + row, part);
-    }
-  }
-}
-
-// vertexMap(PR_Vertex_F) + the L1 step + reset, fused:
-//   p' = 0.85*acc + 0.15/n;  l1 += |p_curr - p'|;  acc = p';  p_curr = 0;
-//   contrib = p'/deg  (for the next iteration's edge pass)
-__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, double* acc,
-                                                   double* p_curr, double* contrib, double added, double* l1_out,
-                                                   const double* l1_prev) {
-  if (pr_converged(l1_prev)) return;
-  double local = 0.0;
-  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const double pn = kDamping * acc[v] + added;
-    local += fabs(p_curr[v] - pn);
-    acc[v] = pn;
-    p_curr[v] = 0.0;
-    const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? pn / (double)d : 0.0;
-  }
-  local = warp_sum(local);
-  __shared__ double ws[8];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = threadIdx.x < 8 ? ws[threadIdx.x] : 0.0;
-    t = warp_sum(t);
-    if (threadIdx.x == 0) atomicAdd(l1_out, t);
-  }
-}
-
-struct PrState {
-  DevBuf a, b, contrib, l1, tmp;
-};
-
-rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
-                       double* l1_out, uint32_t hub_h, bool use_graph) {
-  if (!g) return fail(RG_EINVAL, "null graph");
-  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
-  if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
-  cudaStream_t st = g->stream;
-  const int64_t n = g->n;
-  static thread_local PrState S;
-  RG_TRY(S.a.reserve(8 * n));
-  RG_TRY(S.b.reserve(8 * n));
-  RG_TRY(S.contrib.reserve(8 * n));
-  RG_TRY(S.l1.reserve(8 * (max_iters + 1)));
-  CallTimer timer(g);
-  double* A = S.a.as<double>();
-  double* B = S.b.as<double>();
-  double* C = S.contrib.as<double>();
-  double* L1 = S.l1.as<double>();
-  RG_CUDA(cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st));
-  const int sms = device_sms();
-  const int vblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16);
-  pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, 1 / (double)n);
-  RG_CUDA(cudaGetLastError());
-  g_timing.kernel_launches++;
-  const double added = (1 - kDamping) * (1 / (double)n);
-  // hub set-up
-  int hm = hub_mode_of(variant);
-  HubInfo hub;
-  size_t dyn = 0;
-  if (hm != kHubNone) {
-    uint32_t budget = hub_budget(sizeof(double), n);
-    uint32_t H = hub_h ? std::min(hub_h, budget) : budget;
-    if (hm == kHubPrefix) hub.H = H;
-    else RG_TRY(hub_map(g, H, hub));
-    dyn = sizeof(double) * hub.H;
-  }
-  auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
-                  : hm == kHubMap  ? pr_push_sweep<kHubMap>
-                                   : pr_push_sweep<kHubNone>;
-  int sweep_grid;
-  if (variant == RG_PUSH_PULL) {
-    int per_sm = 0;
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pr_pull_sweep, 256, 0));
-    sweep_grid = sms * std::max(per_sm, 1);
-  } else {
-    if (dyn) RG_CUDA(cudaFuncSetAttribute(sweep_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    int per_sm = 0;
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_fn, kSweepThreads, dyn));
-    sweep_grid = sms * std::max(per_sm, 1);
-  }
-  const int sweep_threads = variant == RG_PUSH_PULL ? 256 : kSweepThreads;
-  sweep_grid = (int)std::min<int64_t>(sweep_grid,
-                                      std::max<int64_t>((g->nchunks * 32 + sweep_threads - 1) / sweep_threads, 1));
-  // iterations: acc alternates B, A, B, ... ; kernels of iteration i return at
-  // once when iteration i-1 already reached L1 < 1e-7 (device-side break)
-  double* acc = B;
-  double* cur = A;
-  for (int64_t it = 0; it < max_iters; it++) {
-    const double* prev = it ? L1 + it - 1 : nullptr;
-    if (g->m > 0) {
-      kt_begin(st);
-      if (variant == RG_PUSH_PULL) {
-        pr_pull_sweep<<<sweep_grid, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C,
-                                                  acc, prev);
-      } else {
-        sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, C, acc,
-                                               hub, prev);
-      }
-      kt_end(st);
-      RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
-      g_timing.edge_launches++;
-    }
-    pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added, L1 + it, prev);
-    RG_CUDA(cudaGetLastError());
-    g_timing.kernel_launches++;
-    std::swap(acc, cur);
-  }
-  (void)use_graph;
-  std::vector<double> l1h(max_iters + 1, 0.0);
-  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, 8 * (max_iters + 1), cudaMemcpyDeviceToHost, st));
-  RG_CUDA(cudaStreamSynchronize(st));
-  int64_t done = max_iters;
-  bool broke = false;
-  for (int64_t it = 0; it < max_iters; it++) {
-    if (l1h[it] < kEpsilon) { done = it; broke = true; break; }
-  }
-  // the ranks are the acc buffer of the last executed iteration
-  int64_t last = broke ? done : max_iters - 1;
-  const double* ranks = max_iters == 0 ? A : ((last % 2 == 0) ? B : A);
-  RG_TRY(download_orig<double>(g, ranks, h_ranks, S.tmp, st));
-  RG_TRY(timer.stop());
-  g_timing.edges_traversed = g->m * (broke ? done + 1 : max_iters);
-  g_timing.algorithmic_bytes = (4 * g->m + 4 * (n + 1) + 16 * n) * (broke ? done + 1 : max_iters);
-  if (iters_out) *iters_out = broke ? done + 1 : max_iters + 1;
-  if (l1_out) *l1_out = max_iters ? l1h[last] : 0.0;
-  return RG_OK;
-}
+constexpr double kDamping = 0.85;  // PR_Vertex_F damping (PageRank.C:126), engine-level vertexMap
 
 // ---------------------------------------------------------------------------
 // BFS (BFS.C:122-188)
@@ -577,7 +292,7 @@ __global__ void set_u32(uint32_t* a, uint32_t i, uint32_t v) { a[i] = v; }
 __global__ void set_i32(int32_t* a, uint32_t i, int32_t v) { a[i] = v; }
 
 struct BfsState {
-  DevBuf parents, depth, tmp;
+  DevBuf parents, depth, visited, tmp;
   Frontier f[2];
 };
 
@@ -591,6 +306,7 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   static thread_local BfsState S;
   RG_TRY(S.parents.reserve(4 * n));
   RG_TRY(S.depth.reserve(4 * n));
+  RG_TRY(S.visited.reserve(4 * ((n + 31) / 32 + 8)));
   RG_TRY(frontier_alloc(g, S.f[0]));
   RG_TRY(frontier_alloc(g, S.f[1]));
   const uint32_t root = to_internal(g, root_orig);
@@ -609,17 +325,22 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   o.dense_forward = variant != RG_PUSH_PULL;
   o.hub_h = hub_h;
   int64_t rounds = 0, reached = 1;
-  OpBfs op{parents};
+  uint32_t* visited = S.visited.as<uint32_t>();
+  RG_CUDA(cudaMemsetAsync(visited, 0, 4 * ((n + 31) / 32), st));
+  set_u32<<<1, 1, 0, st>>>(visited, root >> 5, 1u << (root & 31));
+  OpBfs op{parents, visited, nullptr};
   while (cur.count > 0) {
     rounds++;
-    RG_TRY(edge_map(g, cur, op, &nxt, o, st, depth, (int32_t)rounds));
+    op.next = nxt.bits;
+    RG_TRY(edge_map(g, cur, op, &nxt, o, st, depth, (int32_t)rounds, visited));
     reached += nxt.count;
     std::swap(cur, nxt);
   }
+  RG_TRY(timer.stop());
   RG_TRY(download_orig<uint32_t>(g, parents, h_parents, S.tmp, st));
   RG_CUDA(cudaStreamSynchronize(st));
   RG_TRY(download_orig<int32_t>(g, depth, h_depth, S.tmp, st));
-  RG_TRY(timer.stop());
+  RG_CUDA(cudaStreamSynchronize(st));
   // edges examined: the out-edges of every reached vertex (SURVEY byte model)
   g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 4 * (n + 1) + 4 * n + 2 * ((n + 7) / 8) * rounds;
   if (rounds_out) *rounds_out = rounds;
@@ -757,8 +478,9 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     RG_CUDA(cudaGetLastError());
     g_timing.kernel_launches++;
   }
-  RG_TRY(download_orig<double>(g, deps, h_deps, S.tmp, st));
   RG_TRY(timer.stop());
+  RG_TRY(download_orig<double>(g, deps, h_deps, S.tmp, st));
+  RG_CUDA(cudaStreamSynchronize(st));
   g_timing.algorithmic_bytes =
       4 * g_timing.edges_traversed + (int64_t)nsrc * (8 * (n + 1) + 8 * n + n + 16 * n + 8 * n);
   if (levels_out) *levels_out = total_levels;
@@ -861,11 +583,12 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
     radii_sync<<<(unsigned)((cur.count + 255) / 256), 256, 0, st>>>(cur.queue, cur.count, vis, nvis);
     g_timing.kernel_launches++;
     OpRadii op{vis, nvis, radii, round};
-    RG_TRY(edge_map(g, cur, op, &nxt, o, st));
+    RG_TRY(edge_map(g, cur, op, &nxt, o, st, radii, round));  // radii[v] = round for the next frontier
     std::swap(cur, nxt);
   }
-  RG_TRY(download_orig<int32_t>(g, radii, h_radii, S.tmp, st));
   RG_TRY(timer.stop());
+  RG_TRY(download_orig<int32_t>(g, radii, h_radii, S.tmp, st));
+  RG_CUDA(cudaStreamSynchronize(st));
   g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 16 * n + 4 * n;
   if (rounds_out) *rounds_out = round;
   return RG_OK;
@@ -876,11 +599,6 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
 using namespace rg;
 
 extern "C" {
-
-rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
-                      double* l1_out) {
-  return pagerank_run(g, variant, max_iters, h_ranks, iters_out, l1_out, 0, false);
-}
 
 rg_status rg_bfs(rg_graph* g, rg_variant variant, uint32_t root, uint32_t* h_parents, int32_t* h_depth,
                  int64_t* rounds_out, int64_t* reached_out) {
@@ -1024,7 +742,7 @@ rg_status rg_edgemap(rg_graph* g, rg_frontier* in, rg_op op, const rg_op_args* a
       s = edge_map(g, iv,
                    OpRadii{(const unsigned long long*)a->visited, (unsigned long long*)a->next_visited, a->radii,
                            a->round},
-                   want_out ? &ov : nullptr, o, st);
+                   want_out ? &ov : nullptr, o, st, want_out ? a->radii : nullptr, a->round);
       break;
     default:
       return fail(RG_EINVAL, "unknown op %d", (int)op);

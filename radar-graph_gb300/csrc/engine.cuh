@@ -67,7 +67,8 @@ __device__ __forceinline__ uint32_t hub_vertex(const HubInfo& h, uint32_t slot) 
 struct OpPr {
   const double* __restrict__ contrib;
   double* p_next;
-  using HubT = double;
+  // hub copies accumulate in fx63 fixed point (integer shared-memory atomics)
+  using HubT = unsigned long long;
   static constexpr int kPull = kPullSum;
   static constexpr bool kOutput = false;
   __device__ __forceinline__ bool cond(uint32_t) const { return true; }
@@ -75,12 +76,12 @@ struct OpPr {
     atomicAdd(p_next + d, contrib[s]);
     return false;
   }
-  __device__ static HubT hub_identity() { return 0.0; }
+  __device__ static HubT hub_identity() { return 0ull; }
   __device__ __forceinline__ void hub_push(HubT* hs, uint32_t slot, uint32_t s, uint32_t) const {
-    atomicAdd(hs + slot, contrib[s]);
+    atomicAdd(hs + slot, (unsigned long long)to_fx63(contrib[s]));
   }
   __device__ __forceinline__ bool hub_merge(uint32_t v, HubT x) const {
-    if (x != 0.0) atomicAdd(p_next + v, x);
+    if (x != 0ull) atomicAdd(p_next + v, from_fx63(x));
     return false;
   }
   using PullT = double;
@@ -94,12 +95,20 @@ struct OpPr {
 };
 
 // BFS_F (BFS.C:28-99; push-pull cond/update src/push-pull/Ligra/apps/BFS.C:33-48).
+// With `visited` (union of all frontiers so far) and `next` (the bitmap being
+// built) the unvisited test reads two L2-resident bitmaps instead of the
+// parent array; without them it reads parents[d] like the reference's cond.
 struct OpBfs {
   uint32_t* parents;
+  const uint32_t* visited = nullptr;
+  const uint32_t* next = nullptr;
   using HubT = uint32_t;
   static constexpr int kPull = kPullFirst;
   static constexpr bool kOutput = true;
-  __device__ __forceinline__ bool cond(uint32_t d) const { return parents[d] == kNone; }
+  __device__ __forceinline__ bool cond(uint32_t d) const {
+    if (visited) return !bit_test(visited, d) && !(next && (__ldcg(next + (d >> 5)) >> (d & 31) & 1u));
+    return parents[d] == kNone;
+  }
   __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
     return atomicCAS(parents + d, kNone, s) == kNone;
   }
@@ -185,7 +194,9 @@ struct OpBcBwd {
 };
 
 // Radii_F (Radii.C:37-106): OR the source's mask into next_visited[d] when it
-// adds bits; radii[d] = round; d joins the next frontier.
+// adds bits; d joins the next frontier.  radii[d] = round is written for
+// every member of the next frontier by the compaction that follows (the same
+// set the reference's CAS on radii activates).
 struct OpRadii {
   const unsigned long long* __restrict__ visited;
   unsigned long long* next_visited;
@@ -200,7 +211,6 @@ struct OpRadii {
     unsigned long long w = vd | visited[s];
     if (w == vd) return false;
     atomicOr(next_visited + d, w);
-    if (radii[d] != round) radii[d] = round;
     return true;
   }
   __device__ static HubT hub_identity() { return 0ull; }
@@ -229,7 +239,6 @@ struct OpRadii {
     unsigned long long w = vd | x;
     if (w == vd) return false;
     next_visited[v] |= w;
-    if (radii[v] != round) radii[v] = round;
     return true;
   }
 };
@@ -239,55 +248,114 @@ template <> struct IsRadii<OpRadii> { static constexpr bool value = true; };
 
 // ---------------------------------------------------------------------------
 // push over a compacted frontier, edge-balanced
+//
+// Each CTA owns tiles of kThreads*kPushItems consecutive frontier edges.  The
+// frontier entries overlapping a tile are staged in shared memory and every
+// tile position learns its owning entry by a scatter (entry j marks the
+// position where its edges start) followed by a block-wide max-scan, so a
+// lane finds its source in O(1) instead of a binary search per edge.
 // ---------------------------------------------------------------------------
 constexpr int kPushThreads = 256;     // plain push
-constexpr int kHubPushThreads = 1024; // hub push: one large CTA per SM keeps occupancy with big hub arrays
+constexpr int kHubPushThreads = 512;  // hub push
 constexpr int kPushItems = 4;
+
+template <int kThreads>
+__device__ __forceinline__ uint32_t block_max_scan_prefix(uint32_t v) {
+  // returns max over threads < threadIdx.x (0 for thread 0)
+  __shared__ uint32_t warp_max[kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc = max(inc, t);
+  }
+  if (lane == 31) warp_max[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < kThreads / 32 ? warp_max[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t u = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t = max(t, u);
+    }
+    if (lane < kThreads / 32) warp_max[lane] = t;
+  }
+  __syncthreads();
+  uint32_t ex = __shfl_up_sync(0xffffffffu, inc, 1);
+  if (lane == 0) ex = 0;
+  if (w > 0) ex = max(ex, warp_max[w - 1]);
+  __syncthreads();
+  return ex;
+}
+
+// ts[t] = the frontier entry holding edge t*tile (t < ntiles); ts[ntiles] =
+// the entry holding the last edge.  One thread per tile, so the searches of
+// all tiles overlap instead of stalling each CTA.
+static __global__ void tile_starts(const uint32_t* __restrict__ qoff, uint32_t k, uint32_t total, uint32_t tile,
+                            uint32_t ntiles, uint32_t* __restrict__ ts) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > ntiles) return;
+  const uint32_t e = t < ntiles ? t * tile : total - 1;
+  ts[t] = upper_index(qoff, 0u, k - 1, e);
+}
 
 template <class Op, int kHub, int kThreads>
 __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t* __restrict__ queue,
-                                                         const uint32_t* __restrict__ qoff, uint32_t k,
-                                                         uint32_t total, Op op, HubInfo hub,
-                                                         uint32_t* __restrict__ next_bits) {
-  constexpr int kPushTile = kThreads * kPushItems;
-  constexpr int kPushCap = kPushTile + 1;  // staged frontier entries per tile
+                                                     const uint32_t* __restrict__ qoff,
+                                                     const uint32_t* __restrict__ tstart, uint32_t total, Op op,
+                                                     HubInfo hub, uint32_t* __restrict__ next_bits) {
+  constexpr int kTile = kThreads * kPushItems;
+  constexpr int kCap = kTile + 1;  // staged frontier entries per tile
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using HubT = typename Op::HubT;
   HubT* hs = reinterpret_cast<HubT*>(smem_raw);
-  __shared__ uint32_t s_i0, s_i1;
-  __shared__ uint32_t s_q[kPushCap], s_qo[kPushCap], s_base[kPushCap];
+  __shared__ __align__(16) uint32_t s_owner[kTile];
+  __shared__ uint32_t s_q[kCap], s_qo[kCap], s_base[kCap];
   if (kHub != kHubNone) {
-    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = Op::hub_identity();
+    for (uint32_t h = threadIdx.x; h < hub.H; h += kThreads) hs[h] = Op::hub_identity();
     __syncthreads();
   }
-  for (uint64_t tile = blockIdx.x; tile * kPushTile < total; tile += gridDim.x) {
-    const uint32_t e0 = (uint32_t)(tile * kPushTile);
-    const uint32_t e1 = min(e0 + (uint32_t)kPushTile, total);
-    if (threadIdx.x == 0) {
-      uint32_t i0 = upper_index(qoff, 0u, k - 1, e0);
-      s_i0 = i0;
-      s_i1 = upper_index(qoff, i0, k - 1, e1 - 1);
-    }
+  for (uint64_t tile = blockIdx.x; tile * kTile < total; tile += gridDim.x) {
+    const uint32_t e0 = (uint32_t)(tile * kTile);
+    const uint32_t e1 = min(e0 + (uint32_t)kTile, total);
+    // entries [i0, i1] cover the tile (i1 may be one past: an entry whose
+    // edges start exactly at e1 is staged but never owns a position)
+    const uint32_t i0 = tstart[tile], i1 = tstart[tile + 1], r = i1 - i0 + 1;
+    reinterpret_cast<uint4*>(s_owner)[threadIdx.x] = make_uint4(0, 0, 0, 0);
     __syncthreads();
-    const uint32_t i0 = s_i0, i1 = s_i1, r = i1 - i0 + 1;
-    const bool staged = r <= (uint32_t)kPushCap;
+    const bool staged = r <= (uint32_t)kCap;
     if (staged) {
-      for (uint32_t j = threadIdx.x; j < r; j += blockDim.x) {
-        uint32_t s = queue[i0 + j];
+      for (uint32_t j = threadIdx.x; j < r; j += kThreads) {
+        const uint32_t s = queue[i0 + j];
+        const uint32_t qo = qoff[i0 + j];
         s_q[j] = s;
-        s_qo[j] = qoff[i0 + j];
+        s_qo[j] = qo;
         s_base[j] = g.off[s];
+        if (j > 0 && qo < e1) atomicMax(&s_owner[qo - e0], j);
       }
+      __syncthreads();
+      // inclusive max-scan of the owner marks: position p -> last entry starting at or before p
+      uint4 w4 = reinterpret_cast<uint4*>(s_owner)[threadIdx.x];
+      w4.y = max(w4.y, w4.x);
+      w4.z = max(w4.z, w4.y);
+      w4.w = max(w4.w, w4.z);
+      const uint32_t pre = block_max_scan_prefix<kThreads>(w4.w);
+      w4.x = max(w4.x, pre);
+      w4.y = max(w4.y, pre);
+      w4.z = max(w4.z, pre);
+      w4.w = max(w4.w, pre);
+      reinterpret_cast<uint4*>(s_owner)[threadIdx.x] = w4;
+      __syncthreads();
     }
-    __syncthreads();
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += kThreads) {
       uint32_t s, pos;
       if (staged) {
-        uint32_t li = upper_index(s_qo, 0u, r - 1, e);
+        const uint32_t li = s_owner[e - e0];
         s = s_q[li];
         pos = s_base[li] + (e - s_qo[li]);
       } else {
-        uint32_t gi = upper_index(qoff, i0, i1, e);
+        const uint32_t gi = upper_index(qoff, i0, i1, e);
         s = queue[gi];
         pos = g.off[s] + (e - qoff[gi]);
       }
@@ -298,7 +366,6 @@ __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t*
         if constexpr (IsRadii<Op>::value) {
           if (op.hub_changes(s, d)) {
             op.hub_push(hs, slot, s, d);
-            if (op.radii[d] != op.round) op.radii[d] = op.round;
             bit_set(next_bits, d);
           }
         } else {
@@ -312,8 +379,8 @@ __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t*
   }
   if (kHub != kHubNone) {
     __syncthreads();
-    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) {
-      uint32_t v = hub_vertex<kHub>(hub, h);
+    for (uint32_t h = threadIdx.x; h < hub.H; h += kThreads) {
+      const uint32_t v = hub_vertex<kHub>(hub, h);
       if (op.hub_merge(v, hs[h]) && Op::kOutput) bit_set(next_bits, v);
     }
   }

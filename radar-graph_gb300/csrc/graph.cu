@@ -462,7 +462,12 @@ extern "C" rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t
   return graph_create_common(n, m, d_off, d_adj, cudaMemcpyDeviceToDevice, out);
 }
 
+namespace rg {
+void drop_hub_cache(const rg_graph* g);
+}
+
 extern "C" rg_status rg_graph_free(rg_graph* g) {
+  if (g) rg::drop_hub_cache(g);
   delete g;
   return RG_OK;
 }
@@ -569,17 +574,38 @@ __global__ void rank_to_ids(const uint32_t* __restrict__ sorted_ids, const uint3
   }
 }
 
-// One warp per original vertex: copy its list to the new position, relabelled.
-__global__ void relabel_lists(const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj, uint32_t n,
-                              const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ new_off,
-                              uint32_t* __restrict__ new_adj) {
-  int64_t wv = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t v = wv; v < n; v += nw) {
-    uint32_t b = off[v], e = off[v + 1];
-    uint32_t o = new_off[new_ids[v]];
-    for (uint32_t j = b + lane; j < e; j += 32) new_adj[o + (j - b)] = new_ids[adj[j]];
+// Edge-balanced relabel: every warp owns kSweepChunk consecutive edges of the
+// original CSR (16-byte loads), finds each edge's source from the chunk
+// partition, and writes new_ids[neighbour] at the source's new position.
+__global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                     uint32_t nchunks, const uint32_t* __restrict__ new_ids,
+                                                     const uint32_t* __restrict__ new_off,
+                                                     uint32_t* __restrict__ new_adj) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / 128; r++) {
+      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+      if (e >= g.m) continue;
+      const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+      uint32_t s = upper_index(g.off, vlo, vhi, e);
+      uint32_t nxt = g.off[s + 1];
+      uint32_t base = new_off[new_ids[s]] - g.off[s];  // modulo 2^32; base + e is the new slot
+      const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const uint32_t ee = e + i;
+        if (ee >= g.m) break;
+        if (ee >= nxt) {
+          do { s++; nxt = g.off[s + 1]; } while (ee >= nxt);
+          base = new_off[new_ids[s]] - g.off[s];
+        }
+        new_adj[base + ee] = new_ids[dd[i]];
+      }
+    }
   }
 }
 
@@ -628,9 +654,14 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
     delete ng;
     return s;
   }
-  relabel_lists<<<(unsigned)std::min<int64_t>((n * 32 + 255) / 256, 152 * 64), 256, 0, st>>>(
-      g->off.as<uint32_t>(), g->adj.as<uint32_t>(), (uint32_t)n, ng->new_ids.as<uint32_t>(),
-      ng->off.as<uint32_t>(), ng->adj.as<uint32_t>());
+  if (m > 0) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device);
+    const int64_t blocks = std::min<int64_t>((g->nchunks * 32 + 255) / 256, (int64_t)std::max(sms, 1) * 8);
+    relabel_sweep<<<(unsigned)blocks, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
+                                                    ng->new_ids.as<uint32_t>(), ng->off.as<uint32_t>(),
+                                                    ng->adj.as<uint32_t>());
+  }
   cudaError_t e = cudaMemsetAsync(ng->adj.as<uint32_t>() + m, 0, 32, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -1,0 +1,316 @@
+// PageRank (PageRank.C:120-189) on the device.
+//
+// The iteration is kept entirely on the integer pipes: GB300 issues very few
+// FP64 instructions per clock, so a double add per edge -- or a double divide
+// per vertex -- costs more than the memory traffic.  Ranks, contributions and
+// sums are held in fx63 fixed point (u64 = value * 2^63).  This is exact for
+// PageRank's value range: every rank and every vertex's incoming sum is at
+// most the total mass 1 < 2.
+//   contrib[s] = floor(p[s] * 2^63 / deg(s))        (PR_F's p_curr[s]/deg(s))
+//   acc[d]    += contrib[s]  over the edges          (exact integer sums)
+//   p'[v]      = floor(acc[v] * 0.85) + 0.15/n       (PR_Vertex_F, 0.85 and
+//                0.15/n are the reference's double constants scaled by 2^64
+//                and 2^63)
+//   L1         = sum |p[v] - p'[v]|                  (exact, u64)
+// Each term is truncated below 2^-63 (1.1e-19), far below the 1e-9 relative
+// tolerance for graphs up to ~2^28 vertices; the sums are order independent,
+// so results are deterministic.  Ranks are converted to double once, at the
+// end.  The L1 < 1e-7 break (PageRank.C:172) is taken on the device: every
+// kernel of iteration i returns at once if iteration i-1 converged, so a whole
+// run is enqueued without host round trips.
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <vector>
+
+#include "app_common.cuh"
+
+namespace rg {
+
+namespace {
+
+constexpr int kSweepThreads = 1024;  // push sweep CTA (one per SM with hub copies)
+constexpr int kPullThreads = 256;
+// double(0.85) * 2^64, exact (the double nearest 0.85 times a power of two)
+constexpr uint64_t kDampFx64 = 15679732462653118464ull;
+// 1e-7 * 2^63 rounded up: L1_fx < kEpsFx  <=>  L1 < 1e-7
+constexpr uint64_t kEpsFx = 922337203686ull;
+
+__device__ __forceinline__ bool converged(const uint64_t* l1_prev) {
+  return l1_prev != nullptr && *l1_prev < kEpsFx;
+}
+
+__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, uint64_t* p, uint64_t* acc,
+                        uint64_t* contrib, uint64_t p0) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    p[v] = p0;
+    acc[v] = 0;
+    const uint32_t d = off[v + 1] - off[v];
+    contrib[v] = d ? p0 / d : 0ull;
+  }
+}
+
+// Dense push over every edge (edgeMapDenseForward with a full frontier):
+// acc[d] += contrib[s].  Each warp owns kSweepChunk consecutive edges read as
+// 16-byte vectors; chunk_v gives the chunk's first source so a lane finds its
+// source with a short search.  Hub copies (RADAR: ids < H; HUBDUP: bitmap +
+// index map) are per-CTA shared-memory u64 counters merged once per CTA.
+template <int kHub>
+__global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                               uint32_t nchunks, const uint64_t* __restrict__ contrib,
+                                                               unsigned long long* acc, HubInfo hub,
+                                                               const uint64_t* l1_prev) {
+  if (converged(l1_prev)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* hs = reinterpret_cast<unsigned long long*>(smem_raw);
+  if (kHub != kHubNone) {
+    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = 0ull;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / 128; r++) {
+      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+      if (e >= g.m) continue;
+      const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+      uint32_t s = upper_index(g.off, vlo, vhi, e);
+      uint32_t nxt = g.off[s + 1];
+      unsigned long long cs = contrib[s];
+      const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const uint32_t ee = e + i;
+        if (ee >= g.m) break;
+        if (ee >= nxt) {
+          do { s++; nxt = g.off[s + 1]; } while (ee >= nxt);
+          cs = contrib[s];
+        }
+        const uint32_t d = dd[i];
+        uint32_t slot;
+        if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) atomicAdd(hs + slot, cs);
+        else atomicAdd(acc + d, cs);
+      }
+    }
+  }
+  if (kHub != kHubNone) {
+    __syncthreads();
+    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) {
+      const unsigned long long x = hs[h];
+      if (x) atomicAdd(acc + hub_vertex<kHub>(hub, h), x);
+    }
+  }
+}
+
+// Dense pull over every vertex (edgeMapDense with a full frontier, the
+// push-pull variant): acc[v] = sum of contrib[u] over in-neighbours u.
+// Edge-balanced like the push sweep; a lane sums its row pieces in registers,
+// lanes holding the same row are combined by a segmented scan (rows are
+// non-decreasing across lanes), and each row piece is added to acc once.
+__global__ void __launch_bounds__(kPullThreads) pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                              uint32_t nchunks, const uint64_t* __restrict__ contrib,
+                                                              unsigned long long* acc, const uint64_t* l1_prev) {
+  if (converged(l1_prev)) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / 128; r++) {
+      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+      uint32_t row = 0xFFFFFFFFu;
+      unsigned long long part = 0;
+      if (e < g.m) {
+        const uint4 u4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+        uint32_t v = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[v + 1];
+        const uint32_t uu[4] = {u4.x, u4.y, u4.z, u4.w};
+        unsigned long long x[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) x[i] = (e + i < g.m) ? contrib[uu[i]] : 0ull;
+        row = v;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {
+            if (part) atomicAdd(acc + row, part);  // a row piece that ends inside this lane
+            part = 0;
+            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+            row = v;
+          }
+          part += x[i];
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o);
+        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
+        if (lane >= o && tr == row) part += t;
+      }
+      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
+      if (row != 0xFFFFFFFFu && (lane == 31 || next_row != row) && part) atomicAdd(acc + row, part);
+    }
+  }
+}
+
+// vertexMap(PR_Vertex_F) + the L1 step + the reset, fused:
+//   p' = acc*0.85 + 0.15/n;  l1 += |p - p'|;  acc = p';  p = 0 (becomes the
+//   next accumulator);  contrib = p'/deg (next iteration's edge pass).
+__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, uint64_t* acc,
+                                                   uint64_t* p, uint64_t* contrib, uint64_t added,
+                                                   unsigned long long* l1_out, const uint64_t* l1_prev) {
+  if (converged(l1_prev)) return;
+  unsigned long long local = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t pn = __umul64hi(acc[v], kDampFx64) + added;
+    const uint64_t po = p[v];
+    local += pn > po ? pn - po : po - pn;
+    acc[v] = pn;
+    p[v] = 0;
+    const uint32_t d = off[v + 1] - off[v];
+    contrib[v] = d ? pn / d : 0ull;
+  }
+  local = warp_sum(local);
+  __shared__ unsigned long long ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned long long t = threadIdx.x < 8 ? ws[threadIdx.x] : 0ull;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) atomicAdd(l1_out, t);
+  }
+}
+
+// Ranks to double, in original-id order when the graph is degree-sorted.
+__global__ void pr_to_double(const uint64_t* __restrict__ p, const uint32_t* __restrict__ new_ids, int64_t n,
+                             double* __restrict__ out) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    out[v] = __ull2double_rn(p[new_ids ? new_ids[v] : v]) * 1.0842021724855044340e-19;
+  }
+}
+
+struct PrState {
+  DevBuf a, b, contrib, l1, out;
+};
+
+}  // namespace
+
+rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
+                       double* l1_out, uint32_t hub_h) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
+  if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
+  cudaStream_t st = g->stream;
+  const int64_t n = g->n;
+  static thread_local PrState S;
+  RG_TRY(S.a.reserve(8 * n));
+  RG_TRY(S.b.reserve(8 * n));
+  RG_TRY(S.contrib.reserve(8 * n));
+  RG_TRY(S.l1.reserve(8 * (max_iters + 1)));
+  RG_TRY(S.out.reserve(8 * n));
+  // the reference's constants (PageRank.C:126-138), scaled exactly
+  const double one_over_n = 1 / (double)n;
+  const double added_d = (1 - 0.85) * (1 / (double)n);
+  const uint64_t p0 = (uint64_t)(one_over_n * 9.223372036854775808e18);
+  const uint64_t added = (uint64_t)(added_d * 9.223372036854775808e18);
+  // hub set-up (host side, before the timed span)
+  const int hm = hub_mode_of(variant);
+  HubInfo hub;
+  size_t dyn = 0;
+  if (hm != kHubNone && variant != RG_PUSH_PULL) {
+    const uint32_t budget = hub_budget(sizeof(uint64_t), n);
+    const uint32_t H = hub_h ? std::min(hub_h, budget) : budget;
+    if (hm == kHubPrefix) hub.H = H;
+    else RG_TRY(hub_map(g, H, hub));
+    dyn = sizeof(uint64_t) * hub.H;
+  }
+  auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
+                  : hm == kHubMap  ? pr_push_sweep<kHubMap>
+                                   : pr_push_sweep<kHubNone>;
+  const int sms = device_sms();
+  int sweep_grid, per_sm = 0;
+  if (variant == RG_PUSH_PULL) {
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pr_pull_sweep, kPullThreads, 0));
+    sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
+                                        std::max<int64_t>((g->nchunks * 32 + kPullThreads - 1) / kPullThreads, 1));
+  } else {
+    if (dyn) RG_CUDA(cudaFuncSetAttribute(sweep_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_fn, kSweepThreads, dyn));
+    sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
+                                        std::max<int64_t>((g->nchunks * 32 + kSweepThreads - 1) / kSweepThreads, 1));
+  }
+  const int vblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16);
+
+  CallTimer timer(g);
+  uint64_t* A = S.a.as<uint64_t>();
+  uint64_t* B = S.b.as<uint64_t>();
+  uint64_t* C = S.contrib.as<uint64_t>();
+  uint64_t* L1 = S.l1.as<uint64_t>();
+  RG_CUDA(cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st));
+  pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, p0);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  // acc alternates B, A, B, ...; iteration i's kernels return at once when
+  // iteration i-1 already reached L1 < 1e-7
+  uint64_t* acc = B;
+  uint64_t* cur = A;
+  for (int64_t it = 0; it < max_iters; it++) {
+    const uint64_t* prev = it ? L1 + it - 1 : nullptr;
+    if (g->m > 0) {
+      kt_begin(st);
+      if (variant == RG_PUSH_PULL) {
+        pr_pull_sweep<<<sweep_grid, kPullThreads, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
+                                                           C, (unsigned long long*)acc, prev);
+      } else {
+        sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
+                                                         C, (unsigned long long*)acc, hub, prev);
+      }
+      kt_end(st);
+      RG_CUDA(cudaGetLastError());
+      g_timing.kernel_launches++;
+      g_timing.edge_launches++;
+    }
+    pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added,
+                                         (unsigned long long*)(L1 + it), prev);
+    RG_CUDA(cudaGetLastError());
+    g_timing.kernel_launches++;
+    std::swap(acc, cur);
+  }
+  RG_TRY(timer.stop());  // device work done; result copies are outside the timed span
+  std::vector<uint64_t> l1h(max_iters + 1, 0);
+  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, 8 * (max_iters + 1), cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  int64_t done = max_iters;
+  bool broke = false;
+  for (int64_t it = 0; it < max_iters; it++) {
+    if (l1h[it] < kEpsFx) { done = it; broke = true; break; }
+  }
+  const int64_t last = broke ? done : max_iters - 1;
+  const uint64_t* ranks = max_iters == 0 ? A : ((last % 2 == 0) ? B : A);
+  if (h_ranks) {
+    pr_to_double<<<vblocks, 256, 0, st>>>(ranks, g->sorted ? g->new_ids.as<uint32_t>() : nullptr, n,
+                                          S.out.as<double>());
+    RG_CUDA(cudaGetLastError());
+    RG_CUDA(cudaMemcpyAsync(h_ranks, S.out.p, 8 * n, cudaMemcpyDeviceToHost, st));
+    RG_CUDA(cudaStreamSynchronize(st));
+  }
+  const int64_t iters_run = broke ? done + 1 : max_iters;
+  g_timing.edges_traversed = g->m * iters_run;
+  g_timing.algorithmic_bytes = (4 * g->m + 4 * (n + 1) + 16 * n) * iters_run;
+  if (iters_out) *iters_out = broke ? done + 1 : max_iters + 1;
+  if (l1_out) *l1_out = max_iters ? (double)l1h[last] * 1.0842021724855044340e-19 : 0.0;
+  return RG_OK;
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks,
+                                 int64_t* iters_out, double* l1_out) {
+  return rg::pagerank_run(g, variant, max_iters, h_ranks, iters_out, l1_out, 0);
+}
