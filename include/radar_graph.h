@@ -215,6 +215,27 @@ rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes);
 rg_status rg_synchronize(void);
 
 /* ------------------------------------------------------------------------
+ * Engine options (process-wide; the autotuner sets them per graph).  None of
+ * them changes any result, only how the work is scheduled.
+ * ------------------------------------------------------------------------ */
+typedef enum rg_option {
+  /* 0 (default): each variant's own direction, as in the reference: push
+   * variants push in dense iterations (dense_forward), push-pull pulls.
+   * 1: auto -- dense iterations pull when the operator has an early-exit or
+   * gather form that is cheaper on the GPU (BFS, PageRank), push otherwise. */
+  RG_OPT_DIRECTION = 0,
+  /* hub copies per CTA for HUBDUP/RADAR; 0 = as many as the budget allows */
+  RG_OPT_HUB_SLOTS = 1,
+  /* shared-memory budget for hub copies per CTA of the frontier push, in KiB
+   * (default 48; PageRank's full sweeps use one CTA per SM and all of it) */
+  RG_OPT_HUB_SMEM_KB = 2,
+  /* dense iteration when |F| + outdeg(F) > m / value (default 20, ligra.h:283) */
+  RG_OPT_DENSE_DIV = 3
+} rg_option;
+rg_status rg_set_option(rg_option opt, int64_t value);
+rg_status rg_get_option(rg_option opt, int64_t* value);
+
+/* ------------------------------------------------------------------------
  * Timing of the last app call (CUDA events on the launching stream).
  * ------------------------------------------------------------------------ */
 typedef struct rg_timing {

@@ -17,6 +17,15 @@ namespace rg {
 extern thread_local rg_timing g_timing;
 extern bool g_kernel_timing;
 
+// rg_set_option values
+struct Options {
+  int64_t direction = 0;     // RG_OPT_DIRECTION
+  int64_t hub_slots = 0;     // RG_OPT_HUB_SLOTS
+  int64_t hub_smem_kb = 48;  // RG_OPT_HUB_SMEM_KB
+  int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
+};
+extern Options g_opts;
+
 // Events around one edge-kernel launch (only when rg_set_kernel_timing(1)).
 void kt_begin(cudaStream_t st);
 void kt_end(cudaStream_t st);

@@ -105,9 +105,13 @@ uint32_t hub_budget(size_t elem, int64_t n) {
   constexpr int kTile = kHubPushThreads * kPushItems;
   size_t static_bytes = sizeof(uint32_t) * (kTile + 3 * (kTile + 1)) + 256;
   size_t dyn = (size_t)max_dyn_smem() - static_bytes - 1024;
+  dyn = std::min<size_t>(dyn, (size_t)std::max<int64_t>(g_opts.hub_smem_kb, 1) * 1024);
   uint64_t h = dyn / elem;
+  if (g_opts.hub_slots > 0) h = std::min<uint64_t>(h, (uint64_t)g_opts.hub_slots);
   return (uint32_t)std::min<uint64_t>(h, (uint64_t)n);
 }
+
+Options g_opts;
 
 rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
   HubCache* hc = nullptr;
@@ -233,12 +237,15 @@ static rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out
                           int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr) {
   const int64_t nwords = (g->n + 31) / 32;
   if (out) RG_CUDA(cudaMemsetAsync(out->bits, 0, 4 * nwords, st));
-  int64_t threshold = o.threshold == -1 ? g->m / 20 : o.threshold;
+  int64_t threshold = o.threshold == -1 ? g->m / std::max<int64_t>(g_opts.dense_div, 1) : o.threshold;
   if (in.count > 0 && in.degsum > 0) {
     g_timing.edges_traversed += in.degsum;
     const bool dense = in.count + in.degsum > threshold;
     uint32_t* nb = out ? out->bits : nullptr;
-    if (dense && !o.dense_forward) {
+    // auto direction: BFS's pull exits at the first frontier neighbour, so a
+    // dense BFS level pulls whatever the variant
+    const bool pull = dense && (!o.dense_forward || (g_opts.direction == 1 && Op::kPull == kPullFirst));
+    if (pull) {
       const int64_t groups_per_block = 256 / 8;
       int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
       kt_begin(st);
@@ -630,6 +637,39 @@ rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* r
 rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k, int32_t* h_radii,
                          int64_t* rounds_out) {
   return radii_run(g, variant, h_seeds, k, h_radii, rounds_out, 0);
+}
+
+rg_status rg_set_option(rg_option opt, int64_t value) {
+  switch (opt) {
+    case RG_OPT_DIRECTION:
+      if (value != 0 && value != 1) return fail(RG_EINVAL, "direction must be 0 or 1");
+      g_opts.direction = value;
+      return RG_OK;
+    case RG_OPT_HUB_SLOTS:
+      if (value < 0) return fail(RG_EINVAL, "hub slots must be >= 0");
+      g_opts.hub_slots = value;
+      return RG_OK;
+    case RG_OPT_HUB_SMEM_KB:
+      if (value < 1 || value > 227) return fail(RG_EINVAL, "hub shared memory must be 1..227 KiB");
+      g_opts.hub_smem_kb = value;
+      return RG_OK;
+    case RG_OPT_DENSE_DIV:
+      if (value < 1) return fail(RG_EINVAL, "dense divisor must be >= 1");
+      g_opts.dense_div = value;
+      return RG_OK;
+  }
+  return fail(RG_EINVAL, "unknown option %d", (int)opt);
+}
+
+rg_status rg_get_option(rg_option opt, int64_t* value) {
+  if (!value) return fail(RG_EINVAL, "null value");
+  switch (opt) {
+    case RG_OPT_DIRECTION: *value = g_opts.direction; return RG_OK;
+    case RG_OPT_HUB_SLOTS: *value = g_opts.hub_slots; return RG_OK;
+    case RG_OPT_HUB_SMEM_KB: *value = g_opts.hub_smem_kb; return RG_OK;
+    case RG_OPT_DENSE_DIV: *value = g_opts.dense_div; return RG_OK;
+  }
+  return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
 
 rg_status rg_set_kernel_timing(int on) {

@@ -256,7 +256,7 @@ template <> struct IsRadii<OpRadii> { static constexpr bool value = true; };
 // lane finds its source in O(1) instead of a binary search per edge.
 // ---------------------------------------------------------------------------
 constexpr int kPushThreads = 256;     // plain push
-constexpr int kHubPushThreads = 512;  // hub push
+constexpr int kHubPushThreads = 256;  // hub push: small CTAs with a bounded hub array keep occupancy
 constexpr int kPushItems = 4;
 
 template <int kThreads>

@@ -111,10 +111,21 @@ __global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const
 // Edge-balanced like the push sweep; a lane sums its row pieces in registers,
 // lanes holding the same row are combined by a segmented scan (rows are
 // non-decreasing across lanes), and each row piece is added to acc once.
-__global__ void __launch_bounds__(kPullThreads) pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
-                                                              uint32_t nchunks, const uint64_t* __restrict__ contrib,
-                                                              unsigned long long* acc, const uint64_t* l1_prev) {
+// kCache (degree-sorted graphs): the contributions of the H hubs (ids < H)
+// are copied into shared memory once per CTA -- RADAR's duplication of hub
+// data, used here for the reads of a pull instead of the writes of a push.
+template <bool kCache>
+__global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
+    pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v, uint32_t nchunks,
+                  const uint64_t* __restrict__ contrib, unsigned long long* acc, uint32_t H,
+                  const uint64_t* l1_prev) {
   if (converged(l1_prev)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* hc = reinterpret_cast<uint64_t*>(smem_raw);
+  if (kCache) {
+    for (uint32_t h = threadIdx.x; h < H; h += blockDim.x) hc[h] = contrib[h];
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -132,7 +143,10 @@ __global__ void __launch_bounds__(kPullThreads) pr_pull_sweep(DevGraph g, const 
         const uint32_t uu[4] = {u4.x, u4.y, u4.z, u4.w};
         unsigned long long x[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) x[i] = (e + i < g.m) ? contrib[uu[i]] : 0ull;
+        for (int i = 0; i < 4; i++) {
+          const uint32_t u = uu[i];
+          x[i] = (e + i < g.m) ? ((kCache && u < H) ? hc[u] : contrib[u]) : 0ull;
+        }
         row = v;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -219,26 +233,38 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   const double added_d = (1 - 0.85) * (1 / (double)n);
   const uint64_t p0 = (uint64_t)(one_over_n * 9.223372036854775808e18);
   const uint64_t added = (uint64_t)(added_d * 9.223372036854775808e18);
-  // hub set-up (host side, before the timed span)
+  // hub set-up (host side, before the timed span).  The full sweeps run one
+  // CTA per SM, so their hub copies may use the whole shared memory.
   const int hm = hub_mode_of(variant);
+  uint32_t pr_budget = (uint32_t)std::min<int64_t>((max_dyn_smem() - 1024) / (int)sizeof(uint64_t), n);
+  if (g_opts.hub_slots > 0) pr_budget = (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_slots);
+  if (hub_h) pr_budget = std::min(pr_budget, hub_h);
+  // pull: the push-pull variant (threshold 0, PageRank.C:122 in src/push-pull)
+  // or the auto direction; RADAR's pull keeps the hubs' contributions in
+  // shared memory, the others gather from global memory
+  const bool pull = variant == RG_PUSH_PULL || g_opts.direction == 1;
+  const bool cache = pull && variant == RG_RADAR && g->sorted;
   HubInfo hub;
   size_t dyn = 0;
-  if (hm != kHubNone && variant != RG_PUSH_PULL) {
-    const uint32_t budget = hub_budget(sizeof(uint64_t), n);
-    const uint32_t H = hub_h ? std::min(hub_h, budget) : budget;
-    if (hm == kHubPrefix) hub.H = H;
-    else RG_TRY(hub_map(g, H, hub));
+  if (!pull && hm != kHubNone) {
+    if (hm == kHubPrefix) hub.H = pr_budget;
+    else RG_TRY(hub_map(g, pr_budget, hub));
     dyn = sizeof(uint64_t) * hub.H;
   }
+  const uint32_t cacheH = cache ? pr_budget : 0;
   auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
                   : hm == kHubMap  ? pr_push_sweep<kHubMap>
                                    : pr_push_sweep<kHubNone>;
+  auto pull_fn = cache ? pr_pull_sweep<true> : pr_pull_sweep<false>;
+  const int pull_threads = cache ? 1024 : kPullThreads;
+  const size_t pull_dyn = sizeof(uint64_t) * cacheH;
   const int sms = device_sms();
   int sweep_grid, per_sm = 0;
-  if (variant == RG_PUSH_PULL) {
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pr_pull_sweep, kPullThreads, 0));
+  if (pull) {
+    if (pull_dyn) RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_dyn));
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pull_fn, pull_threads, pull_dyn));
     sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
-                                        std::max<int64_t>((g->nchunks * 32 + kPullThreads - 1) / kPullThreads, 1));
+                                        std::max<int64_t>((g->nchunks * 32 + pull_threads - 1) / pull_threads, 1));
   } else {
     if (dyn) RG_CUDA(cudaFuncSetAttribute(sweep_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_fn, kSweepThreads, dyn));
@@ -264,9 +290,9 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     const uint64_t* prev = it ? L1 + it - 1 : nullptr;
     if (g->m > 0) {
       kt_begin(st);
-      if (variant == RG_PUSH_PULL) {
-        pr_pull_sweep<<<sweep_grid, kPullThreads, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
-                                                           C, (unsigned long long*)acc, prev);
+      if (pull) {
+        pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
+                                                            C, (unsigned long long*)acc, cacheH, prev);
       } else {
         sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
                                                          C, (unsigned long long*)acc, hub, prev);

@@ -96,7 +96,11 @@ _SIGS = {
     "rg_synchronize": [],
     "rg_last_timing": [_P(Timing)],
     "rg_set_kernel_timing": [C.c_int],
+    "rg_set_option": [C.c_int, C.c_int64],
+    "rg_get_option": [C.c_int, _i64p],
 }
+
+OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3}
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
             "rg_host_free": None}
 
@@ -139,6 +143,17 @@ def last_timing():
     t = Timing()
     _check(lib().rg_last_timing(C.byref(t)))
     return {k: getattr(t, k) for k, _ in Timing._fields_}
+
+
+def set_option(name, value):
+    """Engine scheduling option (RG_OPT_*); results never depend on them."""
+    _check(lib().rg_set_option(OPTIONS[name], int(value)))
+
+
+def get_option(name):
+    v = C.c_int64()
+    _check(lib().rg_get_option(OPTIONS[name], C.byref(v)))
+    return v.value
 
 
 def set_kernel_timing(on):
