@@ -215,6 +215,26 @@ rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes);
 rg_status rg_synchronize(void);
 
 /* ------------------------------------------------------------------------
+ * Allocation-free BFS.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory -- code running inside
+ * another framework's memory pool, whose allocator owns the device memory,
+ * and latency-critical serving loops, where cudaMalloc/cudaFree synchronize
+ * the device.  The caller passes a symmetric CSR (d_off: n+1 entries, d_adj:
+ * m) and the output d_depth (n int32: BFS depth from `root`, -1 unreached)
+ * as device pointers; the function allocates nothing.  Its working memory
+ * (two frontier queues, a visited bitmap, a counter) is one fixed 16.25 MiB
+ * __device__ array that every GPU loading the library holds until exit, so
+ * n is limited to RG_NOALLOC_MAX_VERTICES (larger n -> RG_EINVAL).  The
+ * first call on each device looks up that array's device address; make it
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU (other streams, other threads) race and must be
+ * serialized by the caller.  Results equal rg_bfs's depths on the same CSR.
+ * ------------------------------------------------------------------------ */
+#define RG_NOALLOC_MAX_VERTICES 2097152
+rg_status rg_bfs_depth_noalloc(const uint32_t* d_off, const uint32_t* d_adj, int64_t n, int64_t m,
+                               uint32_t root, int32_t* d_depth, void* stream, int64_t* rounds_out);
+
+/* ------------------------------------------------------------------------
  * Engine options (process-wide; the autotuner sets them per graph).  None of
  * them changes any result, only how the work is scheduled.
  * ------------------------------------------------------------------------ */

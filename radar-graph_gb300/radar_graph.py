@@ -96,6 +96,8 @@ _SIGS = {
     "rg_synchronize": [],
     "rg_last_timing": [_P(Timing)],
     "rg_set_kernel_timing": [C.c_int],
+    "rg_bfs_depth_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_uint32, C.c_void_p, C.c_void_p,
+                             _i64p],
     "rg_set_option": [C.c_int, C.c_int64],
     "rg_get_option": [C.c_int, _i64p],
 }
