@@ -57,6 +57,11 @@ typedef enum rg_variant {
 typedef struct rg_graph rg_graph;       /* device-resident CSR image (+ permutation) */
 typedef struct rg_frontier rg_frontier; /* device frontier: id queue + bitmap */
 
+/* Work of the calling thread goes to `stream` (a cudaStream_t; NULL = the
+ * thread's own non-blocking stream, the default).  Each thread has its own
+ * scratch, so threads working on one resident graph run concurrently. */
+rg_status rg_set_stream(void* stream);
+
 const char* rg_last_error(void);
 const char* rg_status_str(rg_status s);
 /* Library version string, e.g. "radar-graph-gb300 0.1 sm_103a". */
@@ -148,6 +153,34 @@ rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* r
 /* Radii with explicit seeds (ORIGINAL ids, bit i for seeds[i], k <= 64). */
 rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k,
                          int32_t* h_radii, int64_t* rounds_out);
+
+/* ------------------------------------------------------------------------
+ * Batched execution (no single counterpart in the reference: it runs many
+ * BFS sources, or many graphs, per launch; each result equals the reference
+ * app's result for that source / graph).
+ * ------------------------------------------------------------------------ */
+
+/* BFS from k <= 64 sources (ORIGINAL ids) in one traversal with 64-bit
+ * bitmask frontiers (one bit per source, the propagation Radii.C uses).
+ * h_depths: k*n int32, row q = depths from sources[q] in original-id order
+ * (-1 unreached), equal to rg_bfs(root = sources[q]).  May be NULL. */
+rg_status rg_bfs_multi(rg_graph* g, const uint32_t* h_sources, int k, int32_t* h_depths,
+                       int64_t* rounds_out);
+
+/* A set of graphs resident on the device, run by one persistent kernel. */
+typedef struct rg_batch rg_batch;
+/* Symmetric CSRs (h_offs[i]: ns[i]+1 entries, h_adjs[i]: ms[i]). */
+rg_status rg_batch_create(int ngraphs, const int64_t* ns, const int64_t* ms,
+                          const uint32_t* const* h_offs, const uint32_t* const* h_adjs,
+                          rg_batch** out);
+/* One launch: for every graph i, a k-source BFS from h_sources[i*k ..] (graph-local
+ * ids) and a PageRank of at most pr_iters iterations.  Outputs (any may be
+ * NULL): h_depths = per graph k rows of n_i depths, concatenated in graph
+ * order; h_ranks = per graph n_i ranks, concatenated; h_pr_iters = per graph
+ * the reference's iteration count; device_ms = the launch's device time. */
+rg_status rg_batch_run(rg_batch* b, const uint32_t* h_sources, int k, int64_t pr_iters,
+                       int32_t* h_depths, double* h_ranks, int32_t* h_pr_iters, double* device_ms);
+rg_status rg_batch_free(rg_batch* b);
 
 /* ------------------------------------------------------------------------
  * Engine (ligra.h:277-354 edgeMap, 461-493 vertexMap).  The functor of the

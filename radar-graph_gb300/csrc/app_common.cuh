@@ -71,4 +71,129 @@ rg_status download_orig(rg_graph* g, const T* d_arr, T* h_out, DevBuf& tmp, cuda
   return RG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// frontier views and the edgeMap driver (edgeMapData, ligra.h:277-316)
+// ---------------------------------------------------------------------------
+struct FView {
+  uint32_t* queue = nullptr;
+  uint32_t* qoff = nullptr;
+  uint32_t* bits = nullptr;
+  int64_t count = 0, degsum = 0;
+};
+
+inline FView view_of(Frontier& f) {
+  return FView{f.queue.as<uint32_t>(), f.qoff.as<uint32_t>(), f.bits.as<uint32_t>(), f.count, f.degsum};
+}
+
+struct EmOpts {
+  int variant = RG_PUSH;
+  bool dense_forward = true;
+  int64_t threshold = -1;
+  uint32_t hub_h = 0;  // 0 = budget
+};
+
+// Frontiers below this many edges skip hub privatisation: the shared-memory
+// set-up and merge would cost more than the atomics they save.  Results do not
+// depend on it.
+constexpr int64_t kHubMinEdges = 1 << 16;
+
+template <class Op, int kHub>
+rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo& hub, uint32_t* next_bits,
+                             cudaStream_t st) {
+  constexpr int kT = kHub == kHubNone ? kPushThreads : kHubPushThreads;
+  constexpr int kTile = kT * kPushItems;
+  auto kern = push_lbs<Op, kHub, kT>;
+  const int64_t tiles = (in.degsum + kTile - 1) / kTile;
+  size_t dyn = kHub == kHubNone ? 0 : sizeof(typename Op::HubT) * hub.H;
+  int grid;
+  if (kHub == kHubNone) {
+    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * 8);
+  } else {
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncAttributes fa;
+      RG_CUDA(cudaFuncGetAttributes(&fa, kern));
+      RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   max_dyn_smem() - (int)fa.sharedSizeBytes));
+      attr_set = true;
+    }
+    int per_sm = 0;
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kT, dyn));
+    if (per_sm < 1) per_sm = 1;
+    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * per_sm);
+  }
+  if (grid < 1) grid = 1;
+  Workspace& ws = ctx().ws;
+  RG_TRY(ws.tiles.reserve(sizeof(uint32_t) * (tiles + 2)));
+  tile_starts<<<(unsigned)((tiles + 1 + 255) / 256), 256, 0, st>>>(in.qoff, (uint32_t)in.count,
+                                                                    (uint32_t)in.degsum, kTile, (uint32_t)tiles,
+                                                                    ws.tiles.as<uint32_t>());
+  g_timing.kernel_launches++;
+  kt_begin(st);
+  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
+                              next_bits);
+  kt_end(st);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  g_timing.edge_launches++;
+  return RG_OK;
+}
+
+// One edgeMap.  `out` (may be null for no_output ops) receives the next
+// frontier: its bitmap is cleared, filled, then compacted (which syncs).
+template <class Op>
+rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const EmOpts& o, cudaStream_t st,
+                          int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr) {
+  const int64_t nwords = (g->n + 31) / 32;
+  if (out) RG_CUDA(cudaMemsetAsync(out->bits, 0, 4 * nwords, st));
+  int64_t threshold = o.threshold == -1 ? g->m / std::max<int64_t>(g_opts.dense_div, 1) : o.threshold;
+  if (in.count > 0 && in.degsum > 0) {
+    g_timing.edges_traversed += in.degsum;
+    const bool dense = in.count + in.degsum > threshold;
+    uint32_t* nb = out ? out->bits : nullptr;
+    // auto direction: BFS's pull exits at the first frontier neighbour, so a
+    // dense BFS level pulls whatever the variant
+    const bool pull = dense && (!o.dense_forward || (g_opts.direction == 1 && Op::kPull == kPullFirst));
+    if (pull) {
+      const int64_t groups_per_block = 256 / 8;
+      int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
+      kt_begin(st);
+      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), in.bits, op, nb);
+      kt_end(st);
+      RG_CUDA(cudaGetLastError());
+      g_timing.kernel_launches++;
+      g_timing.edge_launches++;
+    } else {
+      int hm = in.degsum >= kHubMinEdges ? hub_mode_of(o.variant) : kHubNone;
+      HubInfo hub;
+      if (hm == kHubPrefix) {
+        hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
+                        : hub_budget(sizeof(typename Op::HubT), g->n);
+        RG_TRY(launch_push<Op, kHubPrefix>(g, in, op, hub, nb, st));
+      } else if (hm == kHubMap) {
+        uint32_t H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
+                             : hub_budget(sizeof(typename Op::HubT), g->n);
+        RG_TRY(hub_map(g, H, hub));
+        RG_TRY(launch_push<Op, kHubMap>(g, in, op, hub, nb, st));
+      } else {
+        RG_TRY(launch_push<Op, kHubNone>(g, in, op, hub, nb, st));
+      }
+    }
+  }
+  if (out) {
+    Frontier tmp;  // non-owning shell for compact_bits
+    tmp.bits.p = out->bits;
+    RG_TRY(compact_bits(g, tmp, st, true, depth, level, or_into, out->queue, out->qoff));
+    tmp.bits.p = nullptr;
+    out->count = tmp.count;
+    out->degsum = tmp.degsum;
+    g_timing.kernel_launches += 3;
+  }
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small vertex kernels
+// ---------------------------------------------------------------------------
+
 }  // namespace rg

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <mutex>
 #include <random>
 #include <vector>
 
@@ -47,14 +48,15 @@ void kt_end(cudaStream_t st) {
 CallTimer::CallTimer(rg_graph* gr) : g(gr) {
   memset(&g_timing, 0, sizeof g_timing);
   g_kt_used = 0;
-  cudaEventRecord(g->ev0, g->stream);
+  cudaEventRecord(ctx().ev0, ctx().stream);
 }
 
 rg_status CallTimer::stop() {
-  RG_CUDA(cudaEventRecord(g->ev1, g->stream));
-  RG_CUDA(cudaEventSynchronize(g->ev1));
+  Ctx& c = ctx();
+  RG_CUDA(cudaEventRecord(c.ev1, c.stream));
+  RG_CUDA(cudaEventSynchronize(c.ev1));
   float ms = 0;
-  RG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+  RG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
   g_timing.total_ms = ms;
   double edge = 0;
   for (size_t i = 0; i < g_kt_used; i++) {
@@ -113,7 +115,10 @@ uint32_t hub_budget(size_t elem, int64_t n) {
 
 Options g_opts;
 
+static std::mutex g_hub_mu;  // the hub cache is shared by all threads
+
 rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
+  std::lock_guard<std::mutex> lk(g_hub_mu);
   HubCache* hc = nullptr;
   for (HubCache* c : g_hub_cache) if (c->g == g && c->requested == H) hc = c;
   if (!hc) {
@@ -152,6 +157,7 @@ rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
 }
 
 void drop_hub_cache(const rg_graph* g) {
+  std::lock_guard<std::mutex> lk(g_hub_mu);
   for (auto it = g_hub_cache.begin(); it != g_hub_cache.end();) {
     if ((*it)->g == g) { delete *it; it = g_hub_cache.erase(it); }
     else ++it;
@@ -162,130 +168,6 @@ int hub_mode_of(int variant) {
   return variant == RG_RADAR ? kHubPrefix : variant == RG_HUBDUP ? kHubMap : kHubNone;
 }
 
-// ---------------------------------------------------------------------------
-// frontier views and the edgeMap driver (edgeMapData, ligra.h:277-316)
-// ---------------------------------------------------------------------------
-struct FView {
-  uint32_t* queue = nullptr;
-  uint32_t* qoff = nullptr;
-  uint32_t* bits = nullptr;
-  int64_t count = 0, degsum = 0;
-};
-
-static FView view_of(Frontier& f) {
-  return FView{f.queue.as<uint32_t>(), f.qoff.as<uint32_t>(), f.bits.as<uint32_t>(), f.count, f.degsum};
-}
-
-struct EmOpts {
-  int variant = RG_PUSH;
-  bool dense_forward = true;
-  int64_t threshold = -1;
-  uint32_t hub_h = 0;  // 0 = budget
-};
-
-// Frontiers below this many edges skip hub privatisation: the shared-memory
-// set-up and merge would cost more than the atomics they save.  Results do not
-// depend on it.
-constexpr int64_t kHubMinEdges = 1 << 16;
-
-template <class Op, int kHub>
-static rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo& hub, uint32_t* next_bits,
-                             cudaStream_t st) {
-  constexpr int kT = kHub == kHubNone ? kPushThreads : kHubPushThreads;
-  constexpr int kTile = kT * kPushItems;
-  auto kern = push_lbs<Op, kHub, kT>;
-  const int64_t tiles = (in.degsum + kTile - 1) / kTile;
-  size_t dyn = kHub == kHubNone ? 0 : sizeof(typename Op::HubT) * hub.H;
-  int grid;
-  if (kHub == kHubNone) {
-    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * 8);
-  } else {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncAttributes fa;
-      RG_CUDA(cudaFuncGetAttributes(&fa, kern));
-      RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   max_dyn_smem() - (int)fa.sharedSizeBytes));
-      attr_set = true;
-    }
-    int per_sm = 0;
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kT, dyn));
-    if (per_sm < 1) per_sm = 1;
-    grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * per_sm);
-  }
-  if (grid < 1) grid = 1;
-  Workspace& ws = g->ws;
-  RG_TRY(ws.tiles.reserve(sizeof(uint32_t) * (tiles + 2)));
-  tile_starts<<<(unsigned)((tiles + 1 + 255) / 256), 256, 0, st>>>(in.qoff, (uint32_t)in.count,
-                                                                    (uint32_t)in.degsum, kTile, (uint32_t)tiles,
-                                                                    ws.tiles.as<uint32_t>());
-  g_timing.kernel_launches++;
-  kt_begin(st);
-  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
-                              next_bits);
-  kt_end(st);
-  RG_CUDA(cudaGetLastError());
-  g_timing.kernel_launches++;
-  g_timing.edge_launches++;
-  return RG_OK;
-}
-
-// One edgeMap.  `out` (may be null for no_output ops) receives the next
-// frontier: its bitmap is cleared, filled, then compacted (which syncs).
-template <class Op>
-static rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const EmOpts& o, cudaStream_t st,
-                          int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr) {
-  const int64_t nwords = (g->n + 31) / 32;
-  if (out) RG_CUDA(cudaMemsetAsync(out->bits, 0, 4 * nwords, st));
-  int64_t threshold = o.threshold == -1 ? g->m / std::max<int64_t>(g_opts.dense_div, 1) : o.threshold;
-  if (in.count > 0 && in.degsum > 0) {
-    g_timing.edges_traversed += in.degsum;
-    const bool dense = in.count + in.degsum > threshold;
-    uint32_t* nb = out ? out->bits : nullptr;
-    // auto direction: BFS's pull exits at the first frontier neighbour, so a
-    // dense BFS level pulls whatever the variant
-    const bool pull = dense && (!o.dense_forward || (g_opts.direction == 1 && Op::kPull == kPullFirst));
-    if (pull) {
-      const int64_t groups_per_block = 256 / 8;
-      int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
-      kt_begin(st);
-      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), in.bits, op, nb);
-      kt_end(st);
-      RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
-      g_timing.edge_launches++;
-    } else {
-      int hm = in.degsum >= kHubMinEdges ? hub_mode_of(o.variant) : kHubNone;
-      HubInfo hub;
-      if (hm == kHubPrefix) {
-        hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
-                        : hub_budget(sizeof(typename Op::HubT), g->n);
-        RG_TRY(launch_push<Op, kHubPrefix>(g, in, op, hub, nb, st));
-      } else if (hm == kHubMap) {
-        uint32_t H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
-                             : hub_budget(sizeof(typename Op::HubT), g->n);
-        RG_TRY(hub_map(g, H, hub));
-        RG_TRY(launch_push<Op, kHubMap>(g, in, op, hub, nb, st));
-      } else {
-        RG_TRY(launch_push<Op, kHubNone>(g, in, op, hub, nb, st));
-      }
-    }
-  }
-  if (out) {
-    Frontier tmp;  // non-owning shell for compact_bits
-    tmp.bits.p = out->bits;
-    RG_TRY(compact_bits(g, tmp, st, true, depth, level, or_into, out->queue, out->qoff));
-    tmp.bits.p = nullptr;
-    out->count = tmp.count;
-    out->degsum = tmp.degsum;
-    g_timing.kernel_launches += 3;
-  }
-  return RG_OK;
-}
-
-// ---------------------------------------------------------------------------
-// small vertex kernels
-// ---------------------------------------------------------------------------
 uint32_t to_internal(const rg_graph* g, uint32_t orig) {
   return g->sorted ? g->h_new_ids[orig] : orig;
 }
@@ -308,7 +190,9 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (root_orig >= (uint64_t)g->n) return fail(RG_EINVAL, "root %u >= n", root_orig);
-  cudaStream_t st = g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
   const int64_t n = g->n;
   static thread_local BfsState S;
   RG_TRY(S.parents.reserve(4 * n));
@@ -391,7 +275,9 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
   for (int i = 0; i < nsrc; i++) {
     if (src_orig[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "source %u >= n", src_orig[i]);
   }
-  cudaStream_t st = g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
   const int64_t n = g->n;
   const int64_t nwords = (n + 31) / 32;
   static thread_local BcState S;
@@ -542,7 +428,9 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (k < 0 || k > 64 || (k > 0 && !seeds_orig)) return fail(RG_EINVAL, "need 0..64 seeds");
-  cudaStream_t st = g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
   const int64_t n = g->n;
   static thread_local RadiiState S;
   RG_TRY(S.visited.reserve(8 * n));
@@ -692,9 +580,8 @@ rg_status rg_frontier_create(const rg_graph* g, rg_frontier** out) {
   f->g = g;
   rg_status s = frontier_alloc(g, f->f);
   if (s != RG_OK) { delete f; return s; }
-  RG_CUDA(cudaMemsetAsync(f->f.bits.p, 0, f->f.bits.bytes, g->stream));
-  RG_CUDA(cudaMemsetAsync(f->f.qoff.p, 0, 4, g->stream));
-  RG_CUDA(cudaStreamSynchronize(g->stream));
+  RG_CUDA(cudaMemset(f->f.bits.p, 0, f->f.bits.bytes));
+  RG_CUDA(cudaMemset(f->f.qoff.p, 0, 4));
   *out = f;
   return RG_OK;
 }
@@ -706,12 +593,16 @@ rg_status rg_frontier_free(rg_frontier* f) {
 
 rg_status rg_frontier_set(rg_frontier* f, const uint32_t* h_ids, int64_t k) {
   if (!f || k < 0 || (k > 0 && !h_ids)) return fail(RG_EINVAL, "bad arguments");
-  return frontier_from_host(f->g, f->f, h_ids, k, f->g->stream);
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  return frontier_from_host(f->g, f->f, h_ids, k, cx->stream);
 }
 
 rg_status rg_frontier_set_all(rg_frontier* f) {
   if (!f) return fail(RG_EINVAL, "null frontier");
-  return frontier_set_all(f->g, f->f, f->g->stream);
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  return frontier_set_all(f->g, f->f, cx->stream);
 }
 
 rg_status rg_frontier_count(const rg_frontier* f, int64_t* count) {
@@ -742,7 +633,9 @@ rg_status rg_edgemap(rg_graph* g, rg_frontier* in, rg_op op, const rg_op_args* a
                      int64_t threshold, void* stream) {
   if (!g || !in || !a || in->g != g || (out && out->g != g)) return fail(RG_EINVAL, "bad arguments");
   if (in->f.count > g->n + 64) return fail(RG_EINVAL, "edgeMap: Sizes Don't match");
-  cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = stream ? (cudaStream_t)stream : cx->stream;
   memset(&g_timing, 0, sizeof g_timing);
   FView iv = view_of(in->f);
   const bool want_out = out && !(flags & RG_NO_OUTPUT);
@@ -821,7 +714,9 @@ rg_status rg_vertexmap(rg_graph* g, rg_frontier* f, rg_vop vop, const rg_op_args
       (vop == RG_VOP_RADII_SYNC && (!a->visited || !a->next_visited))) {
     return fail(RG_EINVAL, "vertex op is missing an array");
   }
-  cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = stream ? (cudaStream_t)stream : cx->stream;
   if (!f->f.queue_valid) RG_TRY(compact_bits(g, f->f, st, true));
   if (f->f.count > 0) {
     vertexmap_kernel<<<(unsigned)((f->f.count + 255) / 256), 256, 0, st>>>(

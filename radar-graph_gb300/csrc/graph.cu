@@ -57,6 +57,54 @@ Workspace::~Workspace() {
   if (h_info) cudaFreeHost(h_info);
 }
 
+static thread_local Ctx* t_ctx = nullptr;
+
+rg_status get_ctx(Ctx** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(RG_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (t_ctx && t_ctx->device == dev) {
+    *out = t_ctx;
+    return RG_OK;
+  }
+  // a thread that switches devices keeps one context per process lifetime of
+  // the last device used; the old one is released
+  delete t_ctx;
+  t_ctx = nullptr;
+  Ctx* c = new (std::nothrow) Ctx();
+  if (!c) return fail(RG_ENOMEM, "host allocation failed");
+  c->device = dev;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaHostAlloc((void**)&c->ws.h_info, 64, cudaHostAllocDefault) != cudaSuccess ||
+      c->ws.counters.reserve(4096) != RG_OK) {
+    cudaGetLastError();
+    delete c;
+    return fail(RG_ECUDA, "stream/event/pinned allocation failed");
+  }
+  cudaMemset(c->ws.counters.p, 0, 4096);
+  c->stream = c->own_stream;
+  t_ctx = c;
+  *out = c;
+  return RG_OK;
+}
+
+Ctx& ctx() { return *t_ctx; }
+
+}  // namespace rg
+
+extern "C" rg_status rg_set_stream(void* stream) {
+  rg::Ctx* c = nullptr;
+  RG_TRY(rg::get_ctx(&c));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return RG_OK;
+}
+
+namespace rg {
+
 // ---------------------------------------------------------------------------
 // exclusive scan of uint32 (three kernels: tile sums, scan of sums, apply)
 // ---------------------------------------------------------------------------
@@ -256,7 +304,7 @@ __global__ void comp_emit(const uint32_t* __restrict__ bits, int64_t nwords, con
 
 rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool sync, int32_t* depth,
                        int32_t level, uint32_t* or_into, uint32_t* queue_out, uint32_t* qoff_out) {
-  Workspace& ws = const_cast<rg_graph*>(g)->ws;
+  Workspace& ws = ctx().ws;
   const int64_t nwords = (g->n + 31) / 32;
   const int64_t nt = (nwords + kCompTile - 1) / kCompTile;
   RG_TRY(ws.scan_partials.reserve(sizeof(uint32_t) * 2 * (nt + 1)));
@@ -362,7 +410,7 @@ __global__ void build_chunk_starts(const uint32_t* __restrict__ off, uint32_t n,
 }
 
 static rg_status finish_graph(rg_graph* g) {
-  cudaStream_t st = g->stream;
+  cudaStream_t st = ctx().stream;
   if (g->m > 0) {
     g->nchunks = (g->m + kSweepChunk - 1) / kSweepChunk;
     RG_TRY(g->chunk_v.reserve(sizeof(uint32_t) * (g->nchunks + 1)));
@@ -370,40 +418,23 @@ static rg_status finish_graph(rg_graph* g) {
         g->off.as<uint32_t>(), (uint32_t)g->n, (uint32_t)g->m, g->nchunks, g->chunk_v.as<uint32_t>());
     RG_CUDA(cudaGetLastError());
   }
-  RG_TRY(g->ws.counters.reserve(4096));
-  RG_CUDA(cudaMemsetAsync(g->ws.counters.p, 0, 4096, st));
   RG_CUDA(cudaStreamSynchronize(st));
   return RG_OK;
 }
 
 static rg_status new_graph(rg_graph** out) {
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
   rg_graph* g = new (std::nothrow) rg_graph();
   if (!g) return fail(RG_ENOMEM, "host allocation failed");
-  cudaError_t e = cudaGetDevice(&g->device);
-  if (e != cudaSuccess) {
-    delete g;
-    cudaGetLastError();
-    return fail(RG_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
-  }
-  if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess ||
-      cudaHostAlloc((void**)&g->ws.h_info, 64, cudaHostAllocDefault) != cudaSuccess) {
-    cudaGetLastError();
-    delete g;
-    return fail(RG_ECUDA, "stream/event/pinned allocation failed");
-  }
+  g->device = c->device;
   *out = g;
   return RG_OK;
 }
 
 }  // namespace rg
 
-rg_graph::~rg_graph() {
-  if (stream) cudaStreamSynchronize(stream);
-  if (ev0) cudaEventDestroy(ev0);
-  if (ev1) cudaEventDestroy(ev1);
-  if (stream) cudaStreamDestroy(stream);
-}
+rg_graph::~rg_graph() {}
 
 using namespace rg;
 
@@ -439,10 +470,11 @@ static rg_status graph_create_common(int64_t n, int64_t m, const uint32_t* off, 
     delete g;
     return s;
   }
-  cudaError_t e = cudaMemcpyAsync(g->off.p, h_off.data(), 4 * (n + 1), cudaMemcpyHostToDevice, g->stream);
-  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(g->adj.p, adj, 4 * m, kind, g->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(g->adj.as<uint32_t>() + m, 0, 32, g->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  cudaStream_t st = ctx().stream;
+  cudaError_t e = cudaMemcpyAsync(g->off.p, h_off.data(), 4 * (n + 1), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(g->adj.p, adj, 4 * m, kind, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->adj.as<uint32_t>() + m, 0, 32, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     delete g;
     return cuda_fail(e, "graph upload", __FILE__, __LINE__);
@@ -614,8 +646,10 @@ __global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t*
 extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids) {
   if (!g || !out) return fail(RG_EINVAL, "rg_graph_degree_sort: null argument");
   const int64_t n = g->n, m = g->m;
-  cudaStream_t st = g->stream;
-  Workspace& ws = const_cast<rg_graph*>(g)->ws;
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
+  cudaStream_t st = c->stream;
+  Workspace& ws = c->ws;
   DevBuf k0, v0, k1, v1, hist, new_deg;
   const int64_t nblocks = (n + kSortTile - 1) / kSortTile;
   RG_TRY(k0.reserve(4 * n)); RG_TRY(v0.reserve(4 * n));

@@ -220,7 +220,9 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
-  cudaStream_t st = g->stream;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
   const int64_t n = g->n;
   static thread_local PrState S;
   RG_TRY(S.a.reserve(8 * n));

@@ -78,6 +78,23 @@ struct Workspace {
 
 }  // namespace rg
 
+namespace rg {
+// Per-thread execution context: the stream the calling thread's work goes
+// to, two timing events and the scratch of the engine.  Graphs are shared
+// read-only between threads, so several queries on one resident graph can be
+// in flight on different threads (one stream each).
+struct Ctx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  Workspace ws;
+};
+// The calling thread's context for the current device (created on first use).
+rg_status get_ctx(Ctx** out);
+Ctx& ctx();  // only after a successful get_ctx on this thread
+}  // namespace rg
+
 struct rg_graph {
   int device = 0;
   int64_t n = 0, m = 0;
@@ -89,9 +106,6 @@ struct rg_graph {
   std::vector<uint32_t> h_new_ids;  // same on the host (empty when not sorted)
   std::vector<uint32_t> h_deg;      // degree by internal id
   uint32_t max_deg = 0;
-  rg::Workspace ws;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   rg::DevGraph view() const {
     return rg::DevGraph{(uint32_t)n, (uint32_t)m, off.as<uint32_t>(), adj.as<uint32_t>()};
   }

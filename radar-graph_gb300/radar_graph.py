@@ -61,7 +61,7 @@ _u8p = _P(C.c_uint8)
 
 # name -> argtypes (restype is always c_int = rg_status unless listed in _RESTYPE)
 _SIGS = {
-    "rg_last_error": [], "rg_status_str": [C.c_int], "rg_version": [],
+    "rg_last_error": [], "rg_status_str": [C.c_int], "rg_version": [], "rg_set_stream": [C.c_void_p],
     "rg_generate_edges": [C.c_int, C.c_int, C.c_uint64, C.c_int, _u32p, _u32p],
     "rg_csr_from_edges": [C.c_int64, C.c_int64, _u32p, _u32p, _P(_u32p), _P(_u32p), _i64p],
     "rg_write_adjacency": [C.c_char_p, C.c_int64, C.c_int64, _u32p, _u32p],
@@ -100,6 +100,10 @@ _SIGS = {
                              _i64p],
     "rg_set_option": [C.c_int, C.c_int64],
     "rg_get_option": [C.c_int, _i64p],
+    "rg_bfs_multi": [C.c_void_p, _u32p, C.c_int, _i32p, _i64p],
+    "rg_batch_create": [C.c_int, _i64p, _i64p, _P(_u32p), _P(_u32p), C.c_void_p],
+    "rg_batch_run": [C.c_void_p, _u32p, C.c_int, C.c_int64, _i32p, _f64p, _i32p, _f64p],
+    "rg_batch_free": [C.c_void_p],
 }
 
 OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3}
@@ -331,6 +335,63 @@ class Graph:
         _check(lib().rg_radii_seeds(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s), _ptr(r, C.c_int32),
                                     C.byref(rounds)))
         return r, rounds.value
+
+
+def _graph_bfs_multi(self, sources):
+    """BFS from up to 64 sources in one traversal; returns (depths[k, n], rounds)."""
+    s = np.ascontiguousarray(sources, np.uint32)
+    d = np.empty((len(s), self.n), np.int32)
+    rounds = C.c_int64()
+    _check(lib().rg_bfs_multi(self._h, _ptr(s, C.c_uint32), len(s), _ptr(d, C.c_int32), C.byref(rounds)))
+    return d, rounds.value
+
+
+Graph.bfs_multi = _graph_bfs_multi
+
+
+class Batch:
+    """Many graphs resident on the device, run by one persistent launch."""
+
+    def __init__(self, csrs):
+        self.csrs = [(np.ascontiguousarray(o, np.uint32), np.ascontiguousarray(a, np.uint32)) for o, a in csrs]
+        g = len(self.csrs)
+        self.ns = np.array([len(o) - 1 for o, _ in self.csrs], np.int64)
+        self.ms = np.array([len(a) for _, a in self.csrs], np.int64)
+        offs = (_u32p * g)(*[_ptr(o, C.c_uint32) for o, _ in self.csrs])
+        adjs = (_u32p * g)(*[_ptr(a, C.c_uint32) for _, a in self.csrs])
+        self._h = C.c_void_p()
+        _check(lib().rg_batch_create(g, _ptr(self.ns, C.c_int64), _ptr(self.ms, C.c_int64), offs, adjs,
+                                     C.byref(self._h)))
+
+    def run(self, sources, pr_iters=10):
+        """sources: [ngraphs, k] graph-local ids.  Returns (depths per graph
+        [k, n_i], ranks per graph, PageRank iterations, device ms)."""
+        src = np.ascontiguousarray(sources, np.uint32)
+        g, k = src.shape
+        depths = np.empty(int(k * self.ns.sum()), np.int32)
+        ranks = np.empty(int(self.ns.sum()), np.float64)
+        iters = np.empty(g, np.int32)
+        ms = C.c_double()
+        _check(lib().rg_batch_run(self._h, _ptr(src, C.c_uint32), k, pr_iters, _ptr(depths, C.c_int32),
+                                  _ptr(ranks, C.c_double), _ptr(iters, C.c_int32), C.byref(ms)))
+        out_d, out_r, o, r = [], [], 0, 0
+        for n in self.ns:
+            out_d.append(depths[o:o + k * n].reshape(k, n))
+            out_r.append(ranks[r:r + n])
+            o += k * n
+            r += n
+        return out_d, out_r, iters, ms.value
+
+    def free(self):
+        if self._h is not None and self._h.value:
+            lib().rg_batch_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def radii_seeds_orig(n):
