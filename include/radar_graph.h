@@ -183,6 +183,42 @@ rg_status rg_batch_run(rg_batch* b, const uint32_t* h_sources, int k, int64_t pr
 rg_status rg_batch_free(rg_batch* b);
 
 /* ------------------------------------------------------------------------
+ * Serving: a request loop over resident graphs (no counterpart in the
+ * reference).  Worker threads, each with its own stream, run queries as they
+ * arrive; BFS queries waiting for the same graph are coalesced (up to
+ * max_batch <= 64) into one multi-source traversal; a batch is admitted when
+ * its estimated device memory fits hbm_fraction of the HBM free at start.
+ * Results equal the single-query entry points:
+ *   RG_QUERY_BFS   source = root (ORIGINAL id) -> int32[n] depths (rg_bfs)
+ *   RG_QUERY_BC    source = BC source           -> double[n] (rg_bc_sources
+ *                  with that one source)
+ *   RG_QUERY_RADII source = seed s: samples hashInt(64*s + i) % n, i < 64
+ *                  -> int32[n] radii (rg_radii_seeds with those samples)
+ * ------------------------------------------------------------------------ */
+typedef struct rg_server rg_server;
+typedef enum rg_query_kind { RG_QUERY_BFS = 0, RG_QUERY_BC = 1, RG_QUERY_RADII = 2 } rg_query_kind;
+typedef struct rg_server_stats {
+  int64_t completed;  /* queries finished since the last reset */
+  int64_t launches;   /* batches run (one traversal each) */
+  int64_t batched;    /* queries that shared a batch with others */
+  double p50_ms;      /* submit-to-result latency percentiles */
+  double p99_ms;
+  double qps;         /* completed / (last completion - first submission) */
+} rg_server_stats;
+rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, int max_batch,
+                           double hbm_fraction, rg_server** out);
+rg_status rg_server_submit(rg_server* s, int graph, rg_query_kind kind, uint32_t source,
+                           uint64_t* ticket);
+/* Blocks until the query is done and copies its result (bytes >= result). */
+rg_status rg_server_wait(rg_server* s, uint64_t ticket, void* h_result, size_t bytes,
+                         double* latency_ms);
+rg_status rg_server_get_stats(rg_server* s, rg_server_stats* out);
+rg_status rg_server_reset_stats(rg_server* s);
+/* Finishes the queued queries, stops the workers, frees the server (the
+ * graphs stay the caller's). */
+rg_status rg_server_free(rg_server* s);
+
+/* ------------------------------------------------------------------------
  * Engine (ligra.h:277-354 edgeMap, 461-493 vertexMap).  The functor of the
  * reference (update/updateAtomic/cond/mergeDuplicates, utils.h:62-79) cannot
  * cross a C ABI, so the operator is a closed enum of device functors that

@@ -104,7 +104,20 @@ _SIGS = {
     "rg_batch_create": [C.c_int, _i64p, _i64p, _P(_u32p), _P(_u32p), C.c_void_p],
     "rg_batch_run": [C.c_void_p, _u32p, C.c_int, C.c_int64, _i32p, _f64p, _i32p, _f64p],
     "rg_batch_free": [C.c_void_p],
+    "rg_server_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p],
+    "rg_server_submit": [C.c_void_p, C.c_int, C.c_int, C.c_uint32, _P(C.c_uint64)],
+    "rg_server_wait": [C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t, _f64p],
+    "rg_server_get_stats": [C.c_void_p, C.c_void_p],
+    "rg_server_reset_stats": [C.c_void_p],
+    "rg_server_free": [C.c_void_p],
 }
+
+QUERY_KINDS = {"bfs": 0, "bc": 1, "radii": 2}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("launches", C.c_int64), ("batched", C.c_int64),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("qps", C.c_double)]
 
 OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3}
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
@@ -392,6 +405,65 @@ class Batch:
             self.free()
         except Exception:
             pass
+
+
+class Server:
+    """Request loop over resident graphs (rg_server_*): submit queries from any
+    thread, wait for their results; BFS queries are coalesced into 64-wide
+    multi-source traversals."""
+
+    def __init__(self, graphs, workers=4, max_batch=64, hbm_fraction=0.8):
+        self.graphs = list(graphs)
+        arr = (C.c_void_p * len(self.graphs))(*[g.handle.value for g in self.graphs])
+        self._h = C.c_void_p()
+        _check(lib().rg_server_create(arr, len(self.graphs), workers, max_batch, hbm_fraction, C.byref(self._h)))
+
+    def submit(self, graph, kind, source):
+        t = C.c_uint64()
+        _check(lib().rg_server_submit(self._h, graph, QUERY_KINDS[kind], int(source), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket, graph, kind):
+        n = self.graphs[graph].n
+        out = np.empty(n, np.float64 if kind == "bc" else np.int32)
+        lat = C.c_double()
+        _check(lib().rg_server_wait(self._h, ticket, out.ctypes.data, out.nbytes, C.byref(lat)))
+        return out, lat.value
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().rg_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        _check(lib().rg_server_reset_stats(self._h))
+
+    def free(self):
+        if self._h is not None and self._h.value:
+            lib().rg_server_free(self._h)
+        self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.free()
+
+
+def radii_query_seeds(seed, n):
+    """Sample vertices of a served Radii query: hashInt(64*seed + i) % n, i < 64."""
+    M = (1 << 64) - 1
+    out = []
+    for i in range(min(n, 64)):
+        a = (64 * seed + i) & M
+        a = ((a + 0x7ed55d166bef7a1d) + (a << 12)) & M
+        a = ((a ^ 0xc761c23c510fa2dd) ^ (a >> 9)) & M
+        a = ((a + 0x165667b183a9c0e1) + (a << 59)) & M
+        a = ((a + 0xd3a2646cab3487e3) ^ (a << 49)) & M
+        a = ((a + 0xfd7046c5ef9ab54c) + (a << 3)) & M
+        a = ((a ^ 0xb55a4f090dd4a67b) ^ (a >> 32)) & M
+        out.append(a % n)
+    return np.array(out, np.uint32)
 
 
 def radii_seeds_orig(n):

@@ -1,0 +1,91 @@
+"""Serving: queries submitted concurrently to the request loop must return
+exactly what the same query returns alone through the single-query entry
+points -- BFS depths and Radii bit-exact, BC within 1e-9 relative -- whether
+they were coalesced into a multi-source batch or not."""
+
+import threading
+
+import numpy as np
+import pytest
+
+import radar_graph as rg
+from conftest import assert_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import build as b
+    b.build()
+
+
+@pytest.fixture(scope="module")
+def graphs():
+    a = rg.Graph.from_csr(*rg.rmat_csr(12, 16, seed=1))
+    b0 = rg.Graph.from_csr(*rg.rmat_csr(13, 8, seed=2))
+    b = b0.degree_sort()
+    b0.free()
+    yield [a, b]
+    a.free()
+    b.free()
+
+
+def _alone(G, kind, src):
+    if kind == "bfs":
+        return G.bfs("push", int(src))[1]
+    if kind == "bc":
+        return G.bc_sources(np.array([src], np.uint32), "push")[0]
+    return G.radii_seeds(rg.radii_query_seeds(int(src), G.n), "push")[0]
+
+
+def test_mixed_queries_alone_equal_in_the_mix(graphs):
+    rng = np.random.default_rng(5)
+    queries = []
+    for _ in range(90):
+        gi = int(rng.integers(0, 2))
+        kind = rng.choice(["bfs", "bfs", "bfs", "bc", "radii"])
+        n = graphs[gi].n
+        queries.append((gi, str(kind), int(rng.integers(0, n)) if kind != "radii" else int(rng.integers(0, 1000))))
+    results = [None] * len(queries)
+    with rg.Server(graphs, workers=3, max_batch=64) as S:
+        def client(idx):
+            for i in idx:
+                gi, kind, src = queries[i]
+                t = S.submit(gi, kind, src)
+                results[i] = S.wait(t, gi, kind)[0]
+        # submit from several threads at once so queries arrive while others run
+        th = [threading.Thread(target=client, args=(list(range(j, len(queries), 4)),)) for j in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        st = S.stats()
+    assert st["completed"] == len(queries)
+    assert st["launches"] <= len(queries)
+    for (gi, kind, src), got in zip(queries, results):
+        want = _alone(graphs[gi], kind, src)
+        if kind == "bc":
+            assert_close(got, want, what=f"bc g{gi} s{src}")
+        else:
+            assert np.array_equal(got, want), (gi, kind, src)
+
+
+def test_bfs_queries_are_coalesced(graphs):
+    with rg.Server(graphs[:1], workers=1, max_batch=64) as S:
+        # a burst: one worker, so later arrivals wait and are coalesced
+        tickets = [S.submit(0, "bfs", s) for s in range(0, 4000, 40)]
+        outs = [S.wait(t, 0, "bfs")[0] for t in tickets]
+        st = S.stats()
+    assert st["launches"] < len(tickets)
+    assert st["batched"] > 0
+    for s, got in zip(range(0, 4000, 40), outs):
+        assert np.array_equal(got, graphs[0].bfs("push", s)[1])
+
+
+def test_bad_queries_are_errors(graphs):
+    with rg.Server(graphs, workers=1) as S:
+        with pytest.raises(rg.RgError):
+            S.submit(5, "bfs", 0)
+        with pytest.raises(rg.RgError):
+            S.submit(0, "bfs", 10**9)
