@@ -1,28 +1,37 @@
-"""Benchmark: RADAR PageRank / BFS / BC / Radii on a symmetric R-MAT scale-24
-graph (edge factor 16, a=0.57 b=0.19 c=0.19, seed 1) on one GB300.
+"""Benchmark of the GB300 frontier engine against the reference's CPU path.
 
-A step is one pass of the four RADAR apps over the resident graph: PageRank
-20 iterations, BFS from one root, BC from one source, Radii with 64 samples.
-`value` = edges traversed / device time (GTEPS), inputs resident in HBM; the
-graph (about 2 GB of edges) is far larger than L2, so no flush is needed
+Headline workload: RADAR (degree-sorted graph, hub duplication where the
+autotuner finds it pays) PageRank / BFS / BC / Radii on a symmetric R-MAT
+scale-24 graph (edge factor 16, a=0.57 b=0.19 c=0.19, seed 1) on one GB300.
+A step is one pass of the four apps over the resident graph: PageRank 20
+iterations, BFS from one root, BC from one source, Radii with 64 samples.
+`value` = edges traversed / device time (GTEPS) with the graph resident in HBM;
+the graph (about 2 GB of edges) is far larger than L2, so no flush is needed
 between steps.  `e2e` = the same through the public C ABI from host buffers:
-every step uploads the CSR, degree-sorts it on the device and copies every
+each step uploads the CSR, degree-sorts it on the device and copies every
 app's result back.
+
+The same JSON line also carries the batched launch (512 uneven R-MAT graphs,
+64-source BFS + 10-iteration PageRank each, one persistent launch) and the
+served stream (3 resident graphs, Poisson arrivals of a BFS/BC/Radii mix),
+each against the plain one-query-per-launch GPU path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--scale S] [--impl reference]
 
-Under torchrun each rank runs an independent replica on its own GPU
-(replicas only: the engine has no cross-GPU exchange); rank 0 prints the
-whole-job line.
+Under torchrun each rank runs an independent replica on its own GPU (replicas
+only: the engine has no cross-GPU exchange); rank 0 prints the whole-job line.
 """
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
+import queue
 import statistics
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 import numpy as np
@@ -31,6 +40,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "radar-graph_gb300"))
 
 METRIC = "GTEPS + % HBM roofline per app (RMAT s24); batched queries/s, p50/p99 vs plain"
+APPS = ("pagerank", "bfs", "bc", "radii")
 
 
 def peaks():
@@ -78,11 +88,10 @@ class Clocks:
                 continue
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_init(args):
+def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -99,30 +108,18 @@ def barrier(pg):
         pg.barrier()
 
 
-def allmax(pg, x):
+def allreduce(pg, x, op):
     if pg is None:
         return x
     import torch
     t = torch.tensor([x], dtype=torch.float64)
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.all_reduce(t, op=getattr(pg.ReduceOp, op))
     return float(t.item())
 
 
-def allsum(pg, x):
-    if pg is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64)
-    pg.all_reduce(t, op=pg.ReduceOp.SUM)
-    return float(t.item())
-
-
-def make_graph(rg, scale, ef, seed):
-    t0 = time.time()
-    src, dst = rg.generate_edges(scale, ef, seed)
-    off, adj = rg.csr_from_edges(1 << scale, src, dst)
-    del src, dst
-    return off, adj, time.time() - t0
+def make_graph(rg, scale, ef, seed, uniform=False):
+    src, dst = rg.generate_edges(scale, ef, seed, uniform)
+    return rg.csr_from_edges(1 << scale, src, dst)
 
 
 def pick_root(off, seed=27491095):
@@ -136,12 +133,11 @@ def pick_root(off, seed=27491095):
 
 
 def run_step(rg, gs, root, bc_src, stats):
-    """One pass of the four RADAR apps; returns (device ms, edges, launches)."""
+    """One pass of the four RADAR apps over the resident graph."""
     ms, edges, launches = 0.0, 0, 0
     per = {}
     gs.pagerank("radar", 20)
-    t = rg.last_timing()
-    per["pagerank"] = t
+    per["pagerank"] = rg.last_timing()
     gs.bfs("radar", root)
     per["bfs"] = rg.last_timing()
     gs.bc_sources(bc_src, "radar")
@@ -161,87 +157,199 @@ def run_step(rg, gs, root, bc_src, stats):
     return ms, edges, launches
 
 
-def cpu_baseline(off, adj, seconds_budget=20.0):
-    """The oracle port (OpenMP, all host cores) on a bounded sample of the same
-    workload: RADAR PageRank (2 iterations), BFS, BC (1 source), Radii."""
+# ---------------------------------------------------------------------------
+# batched launch: 512 uneven graphs, one persistent launch vs one query per launch
+# ---------------------------------------------------------------------------
+
+def bench_batched(rg, ngraphs=512, k=64, pr_iters=10, plain_graphs=24, seed=7):
+    rng = np.random.default_rng(seed)
+    specs = [(int(rng.integers(10, 17)), int(rng.integers(8, 33)), 1000 + i) for i in range(ngraphs)]
+    t0 = time.time()
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:  # ctypes releases the GIL; each call is OpenMP inside
+        csrs = list(ex.map(lambda s: make_graph(rg, *s), specs))
+    gen_s = time.time() - t0
+    srcs = []
+    for i, (off, _) in enumerate(csrs):
+        deg = np.diff(off.astype(np.int64))
+        nz = np.nonzero(deg)[0]
+        srcs.append(np.random.default_rng(i).choice(nz, size=k).astype(np.uint32))
+    sources = np.stack(srcs)
+    B = rg.Batch(csrs)
+    B.run(sources, pr_iters)  # warm
+    runs = []
+    for _ in range(3):
+        depths, ranks, iters, ms = B.run(sources, pr_iters)
+        runs.append(ms)
+    ms = min(runs)
+    nq = ngraphs * (k + 1)
+    batched_qps = nq / (ms / 1e3)
+    # plain: every query alone through the single-query entry points
+    plain_ms, plain_q, identical = 0.0, 0, True
+    for i in range(plain_graphs):
+        off, adj = csrs[i]
+        with rg.Graph.from_csr(off, adj) as G:
+            G.bfs("push", int(sources[i, 0]))  # warm this graph's buffers
+            t0 = time.perf_counter()
+            for q in range(k):
+                _, d, _, _ = G.bfs("push", int(sources[i, q]))
+                identical &= bool(np.array_equal(d, depths[i][q]))
+            r, _, _ = G.pagerank("push-pull", pr_iters)
+            identical &= bool(np.array_equal(r, ranks[i]))
+            plain_ms += (time.perf_counter() - t0) * 1e3
+            plain_q += k + 1
+    plain_qps = plain_q / (plain_ms / 1e3)
+    B.free()
+    total_e = int(sum(len(a) for _, a in csrs))
+    return {"graphs": ngraphs, "scales": "U[10,16]", "edge_factor": "U[8,32]", "sources_per_graph": k,
+            "pr_iters": pr_iters, "total_directed_edges": total_e, "queries": nq, "launch_ms": round(ms, 3),
+            "queries_per_s": round(batched_qps, 1), "plain_queries_per_s": round(plain_qps, 1),
+            "plain_sample_queries": plain_q, "speedup_vs_plain": round(batched_qps / plain_qps, 2),
+            "identical_results": identical, "graph_build_s": round(gen_s, 1)}
+
+
+# ---------------------------------------------------------------------------
+# served stream: 3 resident graphs, Poisson arrivals, BFS 60% / BC 25% / Radii 15%
+# ---------------------------------------------------------------------------
+
+def bench_serving(rg, graphs, rates=(200, 800, 3200), per_rate=300, seed=5, workers=4):
+    rng = np.random.default_rng(seed)
+
+    def draw(nq):
+        qs = []
+        for _ in range(nq):
+            gi = int(rng.integers(0, len(graphs)))
+            u = rng.random()
+            kind = "bfs" if u < 0.6 else ("bc" if u < 0.85 else "radii")
+            src = int(rng.integers(0, graphs[gi].n)) if kind != "radii" else int(rng.integers(0, 1 << 20))
+            qs.append((gi, kind, src))
+        return qs
+
+    # one page-locked result buffer per (graph, kind), used by both arms
+    bufs = {(gi, kind): rg.pinned_empty(G.n, np.float64 if kind == "bc" else np.int32)
+            for gi, G in enumerate(graphs) for kind in ("bfs", "bc", "radii")}
+
+    # plain: one query at a time through the single-query entry points
+    plain_qs = draw(60)
+    plain_out = []
+    plain_s = 0.0
+    for gi, kind, src in plain_qs:
+        G, buf = graphs[gi], bufs[(gi, kind)]
+        t0 = time.perf_counter()
+        if kind == "bfs":
+            G.bfs("push", src, depth_out=buf, parents=False)
+        elif kind == "bc":
+            G.bc_sources(np.array([src], np.uint32), "push", out=buf)
+        else:
+            G.radii_seeds(rg.radii_query_seeds(src, G.n), "push", out=buf)
+        plain_s += time.perf_counter() - t0
+        plain_out.append(np.array(buf))  # kept for the identity check, outside the timed span
+    plain_qps = len(plain_qs) / plain_s
+    out = {"graphs": [int(g.n) for g in graphs], "mix": "BFS 60% / BC 25% / Radii 15%",
+           "plain_queries_per_s": round(plain_qps, 1), "rates": []}
+    with rg.Server(graphs, workers=workers, max_batch=64) as S:
+        # identical results: the plain sample served in one burst
+        ts = [S.submit(gi, kind, src) for gi, kind, src in plain_qs]
+        identical = True
+        for (gi, kind, _), t, want in zip(plain_qs, ts, plain_out):
+            got = S.wait(t, gi, kind, out=bufs[(gi, kind)])[0]
+            if kind == "bc":
+                ok = np.array_equal(np.isnan(got), np.isnan(want)) and np.allclose(
+                    got[~np.isnan(got)], want[~np.isnan(want)], rtol=1e-9, atol=0)
+            else:
+                ok = np.array_equal(got, want)
+            identical &= bool(ok)
+        out["identical_results"] = identical
+        best = 0.0
+        for rate in rates:
+            qs = draw(per_rate)
+            S.reset_stats()
+            inbox = queue.Queue()
+
+            def waiter():
+                for _ in range(len(qs)):
+                    t, gi, kind = inbox.get()
+                    S.wait(t, gi, kind, out=bufs[(gi, kind)])
+
+            w = threading.Thread(target=waiter)
+            w.start()
+            gaps = rng.exponential(1.0 / rate, size=len(qs))
+            t_next = time.perf_counter()
+            for (gi, kind, src), gap in zip(qs, gaps):  # Poisson arrivals
+                t_next += gap
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                inbox.put((S.submit(gi, kind, src), gi, kind))
+            w.join()
+            st = S.stats()
+            best = max(best, st["qps"])
+            out["rates"].append({"offered_qps": rate, "qps": round(st["qps"], 1), "p50_ms": round(st["p50_ms"], 3),
+                                 "p99_ms": round(st["p99_ms"], 3), "launches": st["launches"],
+                                 "queries": st["completed"], "coalesced": st["batched"]})
+        out["best_qps"] = round(best, 1)
+        out["speedup_vs_plain"] = round(best / plain_qps, 2)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port (OpenMP, all host cores)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(off, adj, pr_iters=2):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     cores = os.cpu_count() or 1
     ids, so, sa = orc.degree_sort(off, adj)
-    n = len(off) - 1
-    m = len(adj)
+    n, m = len(off) - 1, len(adj)
     root = pick_root(off)
     deg = np.diff(off.astype(np.int64)).astype(np.uint32)
+    sdeg = np.diff(so.astype(np.int64))
     src = orc.bc_sources(deg, 1)
     seeds = orc.radii_seeds(n)
+    t, e = {}, {}
     t0 = time.time()
-    orc.pagerank(so, sa, "radar", 2, cores)
-    t_pr = time.time() - t0
-    edges = 2 * m
+    orc.pagerank(so, sa, "radar", pr_iters, cores)
+    t["pagerank"], e["pagerank"] = time.time() - t0, pr_iters * m
     t0 = time.time()
     par, _ = orc.bfs(so, sa, int(ids[root]), "radar", cores)
-    t_bfs = time.time() - t0
-    reached = par != 0xFFFFFFFF
-    e_bfs = int(np.diff(so.astype(np.int64))[reached].sum())
+    t["bfs"], e["bfs"] = time.time() - t0, int(sdeg[par != 0xFFFFFFFF].sum())
     t0 = time.time()
-    orc.bc(so, sa, ids[src], "radar", cores)
-    t_bc = time.time() - t0
+    d, _ = orc.bc(so, sa, ids[src], "radar", cores)
+    t["bc"], e["bc"] = time.time() - t0, 2 * int(sdeg[~np.isnan(d)].sum())
     t0 = time.time()
     orc.radii(so, sa, ids[seeds], "radar", cores)
-    t_radii = time.time() - t0
-    # Radii/BC edge counts are taken from the GPU run's own counters by the caller
-    return {"t": {"pagerank": t_pr, "bfs": t_bfs, "bc": t_bc, "radii": t_radii},
-            "edges": {"pagerank": edges, "bfs": e_bfs}, "cores": cores}
+    t["radii"] = time.time() - t0
+    return t, e, cores
 
 
 def reference_arm(args):
     """--impl reference: the reference algorithm on the host cores (the oracle
     port, OpenMP, all threads), same workload and metric as the GPU arm."""
-    world, rank, local, pg = dist_init(args)
+    world, rank, local, pg = dist_init()
     if rank != 0:
         return 0
     import radar_graph as rg
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
-    off, adj, _ = make_graph(rg, args.scale, 16, 1)
+    off, adj = make_graph(rg, args.scale, 16, 1)
     n, m = len(off) - 1, len(adj)
-    cores = os.cpu_count() or 1
-    ids, so, sa = orc.degree_sort(off, adj)
-    root = pick_root(off)
-    deg = np.diff(off.astype(np.int64)).astype(np.uint32)
-    src = orc.bc_sources(deg, 1)
-    seeds = orc.radii_seeds(n)
-    sdeg = np.diff(so.astype(np.int64))
-
-    def step():
-        e = 0
-        t0 = time.time()
-        orc.pagerank(so, sa, "radar", args.cpu_pr_iters, cores)
-        e += args.cpu_pr_iters * m
-        par, _ = orc.bfs(so, sa, int(ids[root]), "radar", cores)
-        e += int(sdeg[par != 0xFFFFFFFF].sum())
-        d, _ = orc.bc(so, sa, ids[src], "radar", cores)
-        e += 2 * int(sdeg[~np.isnan(d)].sum())
-        orc.radii(so, sa, ids[seeds], "radar", cores)
-        return e, time.time() - t0
-
-    for _ in range(args.warmup):
-        step()
-    tot_e, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        e, t = step()
-        tot_e += e
-        tot_t += t
+    steps = []
+    for i in range(args.warmup + args.steps):
+        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters)
+        if "radii" not in e:  # Radii's edge count is deterministic: take it from the GPU-free restatement once
+            e["radii"] = e.get("radii", 0)
+        if i >= args.warmup:
+            steps.append((t, e))
+    tot_t = sum(sum(t.values()) for t, _ in steps)
+    tot_e = sum(sum(e.values()) for _, e in steps)
     v = tot_e / tot_t / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GTEPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tot_t / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"RADAR PageRank({args.cpu_pr_iters} it)+BFS+BC(1)+Radii(64), RMAT s{args.scale} ef16 "
-                               f"seed 1, symmetric, degree-sorted", "n": n, "m": m},
+                               "seed 1, symmetric, degree-sorted", "n": n, "m": m},
         "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
                          "sample": f"PageRank {args.cpu_pr_iters} iterations + BFS + BC 1 source + Radii 64 "
-                                   f"sources per step on the full graph"},
+                                   "sources per step on the full graph (Radii edges not counted)"},
         "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -256,17 +364,21 @@ def main():
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and served legs")
     ap.add_argument("--cpu-pr-iters", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return reference_arm(args)
 
-    world, rank, local, pg = dist_init(args)
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    world, rank, local, pg = dist_init()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     import radar_graph as rg
     rg.lib()
-    off, adj, gen_s = make_graph(rg, args.scale, 16, 1)
+    t0 = time.time()
+    off, adj = make_graph(rg, args.scale, 16, 1)
+    gen_s = time.time() - t0
     n, m = len(off) - 1, len(adj)
     root = pick_root(off)
     hbm, peak_kind = peaks()
@@ -275,13 +387,14 @@ def main():
     gs = g.degree_sort()
     g.free()
     bc_src = gs.bc_pick_sources(1)
+    tuning = gs.autotune("radar")
     rg.set_kernel_timing(True)
-    stats = {}
     for _ in range(args.warmup):
         run_step(rg, gs, root, bc_src, {})
     barrier(pg)
     rg.lib().rg_synchronize()
     clocks = Clocks(local)
+    stats = {}
     tot_ms, tot_edges, launches = 0.0, 0, 0
     wall0 = time.time()
     for _ in range(args.steps):
@@ -294,58 +407,67 @@ def main():
     barrier(pg)
     clk = clocks.stop()
     rg.set_kernel_timing(False)
-    ms_step = allmax(pg, tot_ms / args.steps)
-    edges_all = allsum(pg, tot_edges / args.steps)
+    ms_step = allreduce(pg, tot_ms / args.steps, "MAX")
+    edges_all = allreduce(pg, tot_edges / args.steps, "SUM")
     value = edges_all / (ms_step / 1e3) / 1e9
 
-    # roofline of the dominant kernel: the PageRank edge sweep
+    # roofline of the dominant kernel: the PageRank edge sweep (pull or push,
+    # whichever the autotuner chose), timed per launch with CUDA events
     pr = stats["pagerank"]
     sweep_ms = pr["edge_ms"] / max(pr["edge_launches"], 1)
     sweep_bytes = 4 * m + 4 * (n + 1) + 8 * n + 8 * n
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
+    pr_dir = tuning["pagerank"][1]["direction"]
     apps = {}
     for k, s in stats.items():
-        apps[k] = {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3),
-                   "ms": round(s["ms"] / args.steps, 3),
-                   "hbm_frac": round(s["bytes"] / (s["ms"] / 1e3) / 1e9 / hbm, 4)}
+        apps[k] = {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3), "ms": round(s["ms"] / args.steps, 3),
+                   "hbm_frac_of_measured": round(s["bytes"] / (s["ms"] / 1e3) / 1e9 / hbm, 4),
+                   "tuned": tuning[k][1]}
 
     # e2e through the C ABI from host buffers
-    e2e = None
-    if rank == 0 or True:
-        e2e_ms, e2e_edges = 0.0, 0
-        h2d = 4 * (n + 1) + 4 * m
-        d2h = 8 * n + (4 + 4) * n + 8 * n + 4 * n
-        for i in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            with rg.Graph.from_csr(off, adj) as g1, g1.degree_sort() as g2:
-                g2.pagerank("radar", 20)
-                e = rg.last_timing()["edges_traversed"]
-                g2.bfs("radar", root)
-                e += rg.last_timing()["edges_traversed"]
-                g2.bc_sources(bc_src, "radar")
-                e += rg.last_timing()["edges_traversed"]
-                g2.radii("radar")
-                e += rg.last_timing()["edges_traversed"]
-            dt = time.perf_counter() - t0
-            if i >= args.warmup:
-                e2e_ms += dt * 1e3
-                e2e_edges += e
-        e2e = {"value": round(e2e_edges / (e2e_ms / 1e3) / 1e9 * world, 4), "unit": "GTEPS",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "ms_per_step": round(e2e_ms / args.steps, 3)}
+    h2d = 4 * (n + 1) + 4 * m
+    d2h = 8 * n + 4 * n + 4 * n + 8 * n + 4 * n
+    e2e_ms, e2e_edges = 0.0, 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        with rg.Graph.from_csr(off, adj) as g1, g1.degree_sort() as g2:
+            g2.set_tuning(tuning)
+            g2.pagerank("radar", 20)
+            e = rg.last_timing()["edges_traversed"]
+            g2.bfs("radar", root)
+            e += rg.last_timing()["edges_traversed"]
+            g2.bc_sources(bc_src, "radar")
+            e += rg.last_timing()["edges_traversed"]
+            g2.radii("radar")
+            e += rg.last_timing()["edges_traversed"]
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_ms += dt * 1e3
+            e2e_edges += e
+    e2e = {"value": round(e2e_edges / (e2e_ms / 1e3) / 1e9 * world, 4), "unit": "GTEPS",
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms / args.steps, 3)}
+
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        extra["batched"] = bench_batched(rg)
+        gsv = []
+        for sc in (20, 22):
+            o2, a2 = make_graph(rg, sc, 16, 1)
+            with rg.Graph.from_csr(o2, a2) as gg:
+                gsv.append(gg.degree_sort())
+        gsv.append(gs)
+        extra["serving"] = bench_serving(rg, gsv)
+        for G in gsv[:2]:
+            G.free()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        c = cpu_baseline(off, adj)
-        # edge counts of BC/Radii from the GPU run (identical traversal)
-        e_bc = stats["bc"]["edges"] / args.steps
-        e_radii = stats["radii"]["edges"] / args.steps
-        t = c["t"]
-        tot_e = c["edges"]["pagerank"] + c["edges"]["bfs"] + e_bc + e_radii
+        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters)
+        e["radii"] = stats["radii"]["edges"] / args.steps  # identical traversal, deterministic
         tot_t = sum(t.values())
-        cpu = {"value": round(tot_e / tot_t / 1e9, 4), "unit": "GTEPS", "cores": c["cores"], "kind": "port",
-               "sample": "oracle port, OpenMP: RADAR PageRank 2 iterations + BFS + BC 1 source + Radii 64 sources "
-                         f"on the full graph ({tot_t:.1f} s)",
+        cpu = {"value": round(sum(e.values()) / tot_t / 1e9, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
+               "sample": "oracle port, OpenMP, all host cores: RADAR PageRank 2 iterations + BFS + BC 1 source + "
+                         f"Radii 64 sources on the full graph ({tot_t:.1f} s)",
                "seconds": {k: round(v, 3) for k, v in t.items()}}
 
     if rank == 0:
@@ -354,19 +476,21 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"RADAR PageRank(20 it)+BFS+BC(1 src)+Radii(64) on RMAT s{args.scale} ef16 seed 1, "
-                                   "symmetric, degree-sorted", "n": n, "m": m, "parallelism": "replicas",
-                       "l2": "inputs larger than L2 (no flush)", "graph_build_s": round(gen_s, 1)},
+                                   "symmetric, degree-sorted, autotuned schedule", "n": n, "m": m,
+                       "parallelism": "replicas", "l2": "inputs larger than L2 (no flush)",
+                       "graph_build_s": round(gen_s, 1)},
             "apps": apps,
-            "roofline": {"bound": "hbm", "kernel": "pr_push_sweep<hub prefix>", "achieved": round(achieved, 1),
-                         "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
-                         "peak_kind": peak_kind, "bytes_per_launch": sweep_bytes,
-                         "avg_launch_ms": round(sweep_ms, 4)},
+            "roofline": {"bound": "hbm", "kernel": "pr_pull_sweep" if pr_dir == 1 else "pr_push_sweep",
+                         "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_launch": sweep_bytes, "avg_launch_ms": round(sweep_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk,
             "wall_s": round(wall, 3),
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     gs.free()
     return 0

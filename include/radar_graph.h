@@ -209,9 +209,14 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
                            double hbm_fraction, rg_server** out);
 rg_status rg_server_submit(rg_server* s, int graph, rg_query_kind kind, uint32_t source,
                            uint64_t* ticket);
-/* Blocks until the query is done and copies its result (bytes >= result). */
+/* Blocks until the query is done and copies its result (bytes >= result)
+ * from device memory straight into h_result (fastest when h_result comes
+ * from rg_pinned_alloc); the result's device memory is then released. */
 rg_status rg_server_wait(rg_server* s, uint64_t ticket, void* h_result, size_t bytes,
                          double* latency_ms);
+/* Page-locked host memory for result buffers (cudaHostAlloc). */
+rg_status rg_pinned_alloc(size_t bytes, void** h_ptr);
+rg_status rg_pinned_free(void* h_ptr);
 rg_status rg_server_get_stats(rg_server* s, rg_server_stats* out);
 rg_status rg_server_reset_stats(rg_server* s);
 /* Finishes the queued queries, stops the workers, frees the server (the
@@ -304,8 +309,9 @@ rg_status rg_bfs_depth_noalloc(const uint32_t* d_off, const uint32_t* d_adj, int
                                uint32_t root, int32_t* d_depth, void* stream, int64_t* rounds_out);
 
 /* ------------------------------------------------------------------------
- * Engine options (process-wide; the autotuner sets them per graph).  None of
- * them changes any result, only how the work is scheduled.
+ * Engine options (per calling thread; a graph tuned by rg_autotune uses its
+ * own choice per app instead).  None of them changes any result, only how
+ * the work is scheduled.
  * ------------------------------------------------------------------------ */
 typedef enum rg_option {
   /* 0 (default): each variant's own direction, as in the reference: push
@@ -316,13 +322,27 @@ typedef enum rg_option {
   /* hub copies per CTA for HUBDUP/RADAR; 0 = as many as the budget allows */
   RG_OPT_HUB_SLOTS = 1,
   /* shared-memory budget for hub copies per CTA of the frontier push, in KiB
-   * (default 48; PageRank's full sweeps use one CTA per SM and all of it) */
+   * (default 48; PageRank's full sweeps use one CTA per SM and all of it);
+   * 0 = no hub copies (HUBDUP/RADAR then update hubs with global atomics) */
   RG_OPT_HUB_SMEM_KB = 2,
   /* dense iteration when |F| + outdeg(F) > m / value (default 20, ligra.h:283) */
   RG_OPT_DENSE_DIV = 3
 } rg_option;
 rg_status rg_set_option(rg_option opt, int64_t value);
 rg_status rg_get_option(rg_option opt, int64_t* value);
+
+/* Autotuner: times candidate schedules of PageRank (5 iterations), BFS, BC
+ * (one source) and Radii on g for `variant` -- direction, dense threshold,
+ * hub copies and their shared-memory budget -- and keeps the fastest per app
+ * in g; later calls on g use it (instead of the thread's options).
+ * best_ms[4] (may be NULL) receives the winners' times. */
+rg_status rg_autotune(rg_graph* g, rg_variant variant, double* best_ms);
+/* The tuned value of `opt` for app 0 PageRank, 1 BFS, 2 BC, 3 Radii (-1 if
+ * the app is not tuned); rg_graph_clear_tuning forgets every choice. */
+rg_status rg_graph_tuned_option(const rg_graph* g, int app, rg_option opt, int64_t* value);
+/* Sets one tuned option of app on g (e.g. to reuse a tuning on a copy). */
+rg_status rg_graph_set_tuned_option(rg_graph* g, int app, rg_option opt, int64_t value);
+rg_status rg_graph_clear_tuning(rg_graph* g);
 
 /* ------------------------------------------------------------------------
  * Timing of the last app call (CUDA events on the launching stream).

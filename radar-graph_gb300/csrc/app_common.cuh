@@ -18,13 +18,19 @@ extern thread_local rg_timing g_timing;
 extern bool g_kernel_timing;
 
 // rg_set_option values
-struct Options {
-  int64_t direction = 0;     // RG_OPT_DIRECTION
-  int64_t hub_slots = 0;     // RG_OPT_HUB_SLOTS
-  int64_t hub_smem_kb = 48;  // RG_OPT_HUB_SMEM_KB
-  int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
+// The calling thread's options (rg_set_option).  An app call on a graph that
+// the autotuner has tuned runs with the graph's choice for that app instead.
+extern thread_local Options g_opts;
+
+enum App { kAppPagerank = 0, kAppBfs = 1, kAppBc = 2, kAppRadii = 3 };
+
+struct OptScope {
+  Options saved;
+  OptScope(const rg_graph* g, int app) : saved(g_opts) {
+    if (g && g->tuned[app]) g_opts = g->topt[app];
+  }
+  ~OptScope() { g_opts = saved; }
 };
-extern Options g_opts;
 
 // Events around one edge-kernel launch (only when rg_set_kernel_timing(1)).
 void kt_begin(cudaStream_t st);
@@ -39,6 +45,22 @@ struct CallTimer {
 
 int device_sms();
 int max_dyn_smem();
+
+// App drivers (pagerank.cu, apps.cu, multi.cu).  Host outputs are in original
+// id order; the optional device outputs (d_*) receive the same arrays on the
+// device (for serving, which keeps results resident until they are fetched).
+rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
+                       double* l1_out, uint32_t hub_h);
+rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_parents, int32_t* h_depth,
+                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h);
+rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
+                 uint32_t hub_h, double* d_deps_out = nullptr);
+rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k, int32_t* h_radii,
+                    int64_t* rounds_out, uint32_t hub_h);
+rg_status bc_pick(const rg_graph* g, int k, uint32_t* out);
+rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
+                        int32_t* d_depths_out = nullptr, int32_t* h_max_depth = nullptr,
+                        int32_t* d_max_depth = nullptr);
 
 // Hub slots that fit the push kernel's shared-memory budget (elem bytes each).
 uint32_t hub_budget(size_t elem, int64_t n);
@@ -164,7 +186,7 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
       g_timing.kernel_launches++;
       g_timing.edge_launches++;
     } else {
-      int hm = in.degsum >= kHubMinEdges ? hub_mode_of(o.variant) : kHubNone;
+      int hm = (in.degsum >= kHubMinEdges && g_opts.hub_smem_kb > 0) ? hub_mode_of(o.variant) : kHubNone;
       HubInfo hub;
       if (hm == kHubPrefix) {
         hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))

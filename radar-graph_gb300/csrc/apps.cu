@@ -113,7 +113,7 @@ uint32_t hub_budget(size_t elem, int64_t n) {
   return (uint32_t)std::min<uint64_t>(h, (uint64_t)n);
 }
 
-Options g_opts;
+thread_local Options g_opts;
 
 static std::mutex g_hub_mu;  // the hub cache is shared by all threads
 
@@ -190,6 +190,7 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (root_orig >= (uint64_t)g->n) return fail(RG_EINVAL, "root %u >= n", root_orig);
+  OptScope opt_scope(g, kAppBfs);
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;
@@ -268,13 +269,14 @@ struct BcState {
 };
 
 rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
-                 uint32_t hub_h) {
+                 uint32_t hub_h, double* d_deps_out) {
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (nsrc < 0 || (nsrc > 0 && !src_orig)) return fail(RG_EINVAL, "bad source list");
   for (int i = 0; i < nsrc; i++) {
     if (src_orig[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "source %u >= n", src_orig[i]);
   }
+  OptScope opt_scope(g, kAppBc);
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;
@@ -372,6 +374,15 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     g_timing.kernel_launches++;
   }
   RG_TRY(timer.stop());
+  if (d_deps_out) {  // device copy in original-id order
+    if (g->sorted) {
+      const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
+      gather_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(deps, g->new_ids.as<uint32_t>(), n, d_deps_out);
+      RG_CUDA(cudaGetLastError());
+    } else {
+      RG_CUDA(cudaMemcpyAsync(d_deps_out, deps, 8 * n, cudaMemcpyDeviceToDevice, st));
+    }
+  }
   RG_TRY(download_orig<double>(g, deps, h_deps, S.tmp, st));
   RG_CUDA(cudaStreamSynchronize(st));
   g_timing.algorithmic_bytes =
@@ -428,6 +439,7 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (k < 0 || k > 64 || (k > 0 && !seeds_orig)) return fail(RG_EINVAL, "need 0..64 seeds");
+  OptScope opt_scope(g, kAppRadii);
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;
@@ -538,7 +550,7 @@ rg_status rg_set_option(rg_option opt, int64_t value) {
       g_opts.hub_slots = value;
       return RG_OK;
     case RG_OPT_HUB_SMEM_KB:
-      if (value < 1 || value > 227) return fail(RG_EINVAL, "hub shared memory must be 1..227 KiB");
+      if (value < 0 || value > 227) return fail(RG_EINVAL, "hub shared memory must be 0..227 KiB");
       g_opts.hub_smem_kb = value;
       return RG_OK;
     case RG_OPT_DENSE_DIV:

@@ -150,6 +150,18 @@ __global__ void ms_gather(const int32_t* __restrict__ in, const uint32_t* __rest
   }
 }
 
+// out[v] = max over rows q of depth(q, v), in original-id order: a vertex's
+// Radii mask last grows in the round of its farthest sample (Radii.C:188-196).
+__global__ void ms_max_rows(const int32_t* __restrict__ depth, int64_t n, int k,
+                            const uint32_t* __restrict__ new_ids, int32_t* __restrict__ out) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = new_ids ? new_ids[v] : v;
+    int32_t m = -1;
+    for (int q = 0; q < k; q++) m = max(m, depth[(int64_t)q * n + u]);
+    out[v] = m;
+  }
+}
+
 struct MsState {
   DevBuf F, N, seen, depth, src, out;
   Frontier f[2];
@@ -158,9 +170,10 @@ struct MsState {
 }  // namespace
 
 rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
-                        int32_t* d_depths_out) {
+                        int32_t* d_depths_out, int32_t* h_max_depth, int32_t* d_max_depth) {
   if (!g) return fail(RG_EINVAL, "null graph");
   if (k < 1 || k > 64 || !src_orig) return fail(RG_EINVAL, "need 1..64 sources");
+  OptScope opt_scope(g, kAppBfs);
   for (int q = 0; q < k; q++) {
     if (src_orig[q] >= (uint64_t)g->n) return fail(RG_EINVAL, "source %u >= n", src_orig[q]);
   }
@@ -237,6 +250,17 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
     std::swap(cur, nxt);
   }
   RG_TRY(timer.stop());
+  if (h_max_depth || d_max_depth) {
+    int32_t* dst = d_max_depth;
+    if (!dst) {
+      RG_TRY(S.out.reserve(4 * n));
+      dst = S.out.as<int32_t>();
+    }
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
+    ms_max_rows<<<(unsigned)blocks, 256, 0, st>>>(depth, n, k, g->sorted ? g->new_ids.as<uint32_t>() : nullptr, dst);
+    RG_CUDA(cudaGetLastError());
+    if (h_max_depth) RG_CUDA(cudaMemcpyAsync(h_max_depth, dst, 4 * n, cudaMemcpyDeviceToHost, st));
+  }
   const int32_t* res = depth;
   if (g->sorted && (h_depths || d_depths_out)) {
     RG_TRY(S.out.reserve(4 * n * k));
@@ -361,7 +385,9 @@ __device__ void batch_msbfs(const BatchDesc& D, int gi) {
       }
     }
     __syncthreads();
-    if (!s_any) break;
+    const int any = s_any;
+    __syncthreads();  // every thread has read the flag before thread 0 resets it
+    if (!any) break;
   }
 }
 
@@ -413,7 +439,9 @@ __device__ void batch_pagerank(const BatchDesc& D, int gi) {
       contrib[v] = d ? pn / d : 0ull;
     }
     __syncthreads();
-    if (s_l1 < kEpsFx) { broke = true; break; }
+    const bool conv = s_l1 < kEpsFx;
+    __syncthreads();  // every thread has read the sum before thread 0 resets it
+    if (conv) { broke = true; break; }
   }
   for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) D.ranks[vb + v] = __ull2double_rn(p[v]) * 1.0842021724855044340e-19;
   if (threadIdx.x == 0) D.pr_iters[gi] = (int32_t)(broke ? it : D.max_iters + 1);

@@ -21,6 +21,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 #include <vector>
 
@@ -220,6 +221,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
+  OptScope opt_scope(g, kAppPagerank);
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;
@@ -245,10 +247,10 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   // or the auto direction; RADAR's pull keeps the hubs' contributions in
   // shared memory, the others gather from global memory
   const bool pull = variant == RG_PUSH_PULL || g_opts.direction == 1;
-  const bool cache = pull && variant == RG_RADAR && g->sorted;
+  const bool cache = pull && variant == RG_RADAR && g->sorted && g_opts.hub_smem_kb > 0;
   HubInfo hub;
   size_t dyn = 0;
-  if (!pull && hm != kHubNone) {
+  if (!pull && hm != kHubNone && g_opts.hub_smem_kb > 0) {
     if (hm == kHubPrefix) hub.H = pr_budget;
     else RG_TRY(hub_map(g, pr_budget, hub));
     dyn = sizeof(uint64_t) * hub.H;
@@ -280,36 +282,100 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   uint64_t* B = S.b.as<uint64_t>();
   uint64_t* C = S.contrib.as<uint64_t>();
   uint64_t* L1 = S.l1.as<uint64_t>();
-  RG_CUDA(cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st));
-  pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, p0);
-  RG_CUDA(cudaGetLastError());
-  g_timing.kernel_launches++;
-  // acc alternates B, A, B, ...; iteration i's kernels return at once when
-  // iteration i-1 already reached L1 < 1e-7
-  uint64_t* acc = B;
-  uint64_t* cur = A;
-  for (int64_t it = 0; it < max_iters; it++) {
-    const uint64_t* prev = it ? L1 + it - 1 : nullptr;
-    if (g->m > 0) {
-      kt_begin(st);
-      if (pull) {
-        pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
-                                                            C, (unsigned long long*)acc, cacheH, prev);
-      } else {
-        sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
-                                                         C, (unsigned long long*)acc, hub, prev);
+  // The whole run (init + every iteration) is enqueued without host round
+  // trips; it is captured once as a CUDA graph and replayed on later calls
+  // with the same graph, buffers and schedule (not while per-kernel timing
+  // is on, which needs the launches one by one).
+  int64_t launches = 0, edge_launches = 0;
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st);
+    if (e != cudaSuccess) return e;
+    pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, p0);
+    launches++;
+    // acc alternates B, A, B, ...; iteration i's kernels return at once when
+    // iteration i-1 already reached L1 < 1e-7
+    uint64_t* acc = B;
+    uint64_t* cur = A;
+    for (int64_t it = 0; it < max_iters; it++) {
+      const uint64_t* prev = it ? L1 + it - 1 : nullptr;
+      if (g->m > 0) {
+        kt_begin(st);
+        if (pull) {
+          pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+                                                              (uint32_t)g->nchunks, C, (unsigned long long*)acc,
+                                                              cacheH, prev);
+        } else {
+          sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+                                                           (uint32_t)g->nchunks, C, (unsigned long long*)acc, hub,
+                                                           prev);
+        }
+        kt_end(st);
+        launches++;
+        edge_launches++;
       }
-      kt_end(st);
-      RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
-      g_timing.edge_launches++;
+      pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added,
+                                           (unsigned long long*)(L1 + it), prev);
+      launches++;
+      std::swap(acc, cur);
     }
-    pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added,
-                                         (unsigned long long*)(L1 + it), prev);
-    RG_CUDA(cudaGetLastError());
-    g_timing.kernel_launches++;
-    std::swap(acc, cur);
+    return cudaGetLastError();
+  };
+  struct GraphKey {
+    const void *off, *adj, *a, *b, *c, *l1;
+    int64_t n, m, iters;
+    int variant, grid, pull, cacheH, hubH, hubmode;
+    bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof *this) == 0; }
+  };
+  static thread_local GraphKey cached_key;
+  static thread_local cudaGraphExec_t cached_exec = nullptr;
+  static thread_local int64_t cached_launches = 0, cached_edge_launches = 0;
+  GraphKey key;
+  memset(&key, 0, sizeof key);  // memcmp compares the padding too: set fields one by one
+  key.off = g->off.p;
+  key.adj = g->adj.p;
+  key.a = A;
+  key.b = B;
+  key.c = C;
+  key.l1 = L1;
+  key.n = n;
+  key.m = g->m;
+  key.iters = max_iters;
+  key.variant = variant;
+  key.grid = sweep_grid;
+  key.pull = pull ? 1 : 0;
+  key.cacheH = (int)cacheH;
+  key.hubH = (int)hub.H;
+  key.hubmode = hm;
+  if (g_kernel_timing || max_iters == 0) {
+    RG_CUDA(enqueue());
+  } else {
+    if (!cached_exec || !(key == cached_key)) {
+      if (cached_exec) cudaGraphExecDestroy(cached_exec);
+      cached_exec = nullptr;
+      cudaGraph_t graph = nullptr;
+      RG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t e = enqueue();
+      const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(e != cudaSuccess ? e : e2, "PageRank graph capture", __FILE__, __LINE__);
+      }
+      const cudaError_t e3 = cudaGraphInstantiate(&cached_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e3 != cudaSuccess) {
+        cached_exec = nullptr;
+        return cuda_fail(e3, "cudaGraphInstantiate", __FILE__, __LINE__);
+      }
+      cached_key = key;
+      cached_launches = launches;
+      cached_edge_launches = edge_launches;
+    }
+    RG_CUDA(cudaGraphLaunch(cached_exec, st));
+    launches = cached_launches;
+    edge_launches = cached_edge_launches;
   }
+  g_timing.kernel_launches += launches;
+  g_timing.edge_launches += edge_launches;
   RG_TRY(timer.stop());  // device work done; result copies are outside the timed span
   std::vector<uint64_t> l1h(max_iters + 1, 0);
   RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, 8 * (max_iters + 1), cudaMemcpyDeviceToHost, st));

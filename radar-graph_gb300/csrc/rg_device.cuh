@@ -79,6 +79,14 @@ struct Workspace {
 }  // namespace rg
 
 namespace rg {
+// Scheduling options (RG_OPT_*); none of them changes a result.
+struct Options {
+  int64_t direction = 0;     // RG_OPT_DIRECTION
+  int64_t hub_slots = 0;     // RG_OPT_HUB_SLOTS
+  int64_t hub_smem_kb = 48;  // RG_OPT_HUB_SMEM_KB (0 = no hub copies in the frontier push)
+  int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
+};
+
 // Per-thread execution context: the stream the calling thread's work goes
 // to, two timing events and the scratch of the engine.  Graphs are shared
 // read-only between threads, so several queries on one resident graph can be
@@ -106,6 +114,8 @@ struct rg_graph {
   std::vector<uint32_t> h_new_ids;  // same on the host (empty when not sorted)
   std::vector<uint32_t> h_deg;      // degree by internal id
   uint32_t max_deg = 0;
+  bool tuned[4] = {false, false, false, false};  // per app: PageRank, BFS, BC, Radii
+  rg::Options topt[4];                           // the autotuner's choice per app
   rg::DevGraph view() const {
     return rg::DevGraph{(uint32_t)n, (uint32_t)m, off.as<uint32_t>(), adj.as<uint32_t>()};
   }

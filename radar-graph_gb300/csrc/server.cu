@@ -11,11 +11,13 @@
 //    whose per-vertex maximum depth is exactly Radii.C's radius (a vertex's
 //    mask last changes in the round of its farthest sample);
 //  * a BC query (one source) runs BC-manyiter-v2's forward/backward phases.
-// A batch is admitted only when its estimated device memory fits the free
-// HBM budget taken at start-up; otherwise it waits for running batches to
-// release theirs (or runs alone if nothing else is running).
-// Every result equals the same query run alone through the single-query
-// entry points.
+// Results stay in device memory (stream-ordered allocations) until the client
+// fetches them with rg_server_wait, which copies one query's array straight
+// into the client's buffer.  A batch is admitted only when its working set
+// and results fit the HBM budget taken at start-up; otherwise it waits for
+// running batches and unfetched results to release theirs (or runs alone if
+// nothing else holds memory).  Every result equals the same query run alone
+// through the single-query entry points.
 
 #include <cuda_runtime.h>
 #include <string.h>
@@ -24,19 +26,13 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
 #include "app_common.cuh"
-
-namespace rg {
-rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
-                        int32_t* d_depths_out);
-rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
-                 uint32_t hub_h);
-}  // namespace rg
 
 namespace {
 
@@ -54,8 +50,17 @@ struct Query {
   double t_submit;
 };
 
+// A device allocation holding the results of one batch; freed (and its bytes
+// returned to the admission budget) when its last result has been fetched.
+struct Block {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int refs = 0;
+};
+
 struct Result {
-  std::vector<char> data;
+  std::shared_ptr<Block> block;
+  size_t offset = 0, bytes = 0;
   double latency_ms = 0;
   rg_status status = RG_OK;
   bool done = false;
@@ -84,6 +89,7 @@ struct rg_server {
 
 namespace {
 
+using rg::cuda_fail;
 using rg::fail;
 
 // Radii sample vertices of a query: hashInt(seed*64 + i) % n, i < min(n, 64)
@@ -94,20 +100,25 @@ int radii_seeds(uint64_t seed, int64_t n, uint32_t* out) {
   return k;
 }
 
-size_t estimate_bytes(const rg_graph* g, int kind, int k) {
+size_t result_bytes(const rg_graph* g, int kind, int k) {
+  const size_t n = (size_t)g->n;
+  return kind == RG_QUERY_BFS ? 4 * n * k : kind == RG_QUERY_BC ? 8 * n : 4 * n;
+}
+
+size_t working_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
   if (kind == RG_QUERY_BC) return 64 * n;
-  // masks, depths (k rows) and their original-order copy, two frontiers
-  return (size_t)(8 * k + 40) * n;
+  return (size_t)(8 * k + 40) * n;  // masks, depth rows and their original-order copy, two frontiers
 }
 
 void worker_main(rg_server* S) {
   cudaSetDevice(S->device);
-  std::vector<int32_t> depths;
+  rg::Ctx* cx = nullptr;
+  rg::get_ctx(&cx);
   std::vector<uint32_t> src;
   for (;;) {
     std::vector<Query> batch;
-    size_t need = 0;
+    size_t work = 0, res = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv_work.wait(lk, [&] { return S->stop || !S->pending.empty(); });
@@ -125,59 +136,67 @@ void worker_main(rg_server* S) {
           }
         }
       }
-      rg_graph* g = S->graphs[q0.graph];
-      need = estimate_bytes(g, q0.kind, q0.kind == RG_QUERY_BFS ? (int)batch.size() : 64);
-      // admission by free HBM: wait while the budget is taken by running work
-      S->cv_mem.wait(lk, [&] { return S->running == 0 || S->hbm_in_use + need <= S->hbm_budget; });
-      S->hbm_in_use += need;
+      const rg_graph* g = S->graphs[q0.graph];
+      const int k = q0.kind == RG_QUERY_BFS ? (int)batch.size() : 64;
+      work = working_bytes(g, q0.kind, k);
+      res = result_bytes(g, q0.kind, k);
+      // admission by free HBM: wait while running batches and unfetched
+      // results hold the budget
+      S->cv_mem.wait(lk, [&] { return S->hbm_in_use == 0 || S->hbm_in_use + work + res <= S->hbm_budget; });
+      S->hbm_in_use += work + res;
       S->running++;
     }
     rg_graph* g = S->graphs[batch[0].graph];
     const int64_t n = g->n;
     const int kind = batch[0].kind;
-    std::vector<std::vector<char>> out(batch.size());
-    rg_status st = RG_OK;
-    if (kind == RG_QUERY_BFS) {
-      const int k = (int)batch.size();
-      src.resize(k);
-      for (int i = 0; i < k; i++) src[i] = batch[i].source;
-      depths.resize((size_t)k * n);
-      st = rg::bfs_multi_run(g, src.data(), k, depths.data(), nullptr, nullptr);
-      for (int i = 0; i < k && st == RG_OK; i++) {
-        out[i].resize(4 * n);
-        memcpy(out[i].data(), depths.data() + (size_t)i * n, 4 * n);
+    cudaStream_t st = cx ? cx->stream : nullptr;
+    auto block = std::make_shared<Block>();
+    block->bytes = res;
+    rg_status status = cx ? RG_OK : RG_ENODEV;
+    if (status == RG_OK && cudaMallocAsync(&block->p, res, st) != cudaSuccess) {
+      cudaGetLastError();
+      status = fail(RG_ENOMEM, "server: result allocation of %zu bytes failed", res);
+    }
+    if (status == RG_OK) {
+      if (kind == RG_QUERY_BFS) {
+        const int k = (int)batch.size();
+        src.resize(k);
+        for (int i = 0; i < k; i++) src[i] = batch[i].source;
+        status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, static_cast<int32_t*>(block->p));
+      } else if (kind == RG_QUERY_RADII) {
+        src.resize(64);
+        const int k = radii_seeds(batch[0].source, n, src.data());
+        status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, nullptr, nullptr,
+                                   static_cast<int32_t*>(block->p));
+      } else {
+        const uint32_t s = batch[0].source;
+        status = rg::bc_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, &s, 1, nullptr, nullptr, 0,
+                            static_cast<double*>(block->p));
       }
-    } else if (kind == RG_QUERY_RADII) {
-      src.resize(64);
-      const int k = radii_seeds(batch[0].source, n, src.data());
-      depths.resize((size_t)k * n);
-      st = rg::bfs_multi_run(g, src.data(), k, depths.data(), nullptr, nullptr);
-      if (st == RG_OK) {
-        out[0].resize(4 * n);
-        int32_t* r = reinterpret_cast<int32_t*>(out[0].data());
-        for (int64_t v = 0; v < n; v++) {
-          int32_t m = -1;
-          for (int q = 0; q < k; q++) m = std::max(m, depths[(size_t)q * n + v]);
-          r[v] = m;
-        }
+      // the result is complete before any client (on another stream) copies it
+      if (status == RG_OK) {
+        const cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) status = cuda_fail(e, "server batch", __FILE__, __LINE__);
       }
-    } else {
-      out[0].resize(8 * n);
-      const uint32_t s = batch[0].source;
-      st = rg::bc_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, &s, 1, reinterpret_cast<double*>(out[0].data()), nullptr,
-                      0);
     }
     const double t_done = now_ms();
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      S->hbm_in_use -= need;
+      S->hbm_in_use -= work;
+      if (status != RG_OK) S->hbm_in_use -= res;
       S->running--;
       S->launches++;
       if (batch.size() > 1) S->batched += (int64_t)batch.size();
+      const size_t row = kind == RG_QUERY_BC ? 8 * n : 4 * n;
+      block->refs = status == RG_OK ? (int)batch.size() : 0;
       for (size_t i = 0; i < batch.size(); i++) {
         Result& r = S->results[batch[i].ticket];
-        r.status = st;
-        r.data = std::move(out[i]);
+        r.status = status;
+        if (status == RG_OK) {
+          r.block = block;
+          r.offset = i * row;
+          r.bytes = row;
+        }
         r.latency_ms = t_done - batch[i].t_submit;
         r.done = true;
         S->latencies.push_back(r.latency_ms);
@@ -186,6 +205,7 @@ void worker_main(rg_server* S) {
       }
       S->t_last = std::max(S->t_last, t_done);
     }
+    if (status != RG_OK && block->p) cudaFreeAsync(block->p, st);
     S->cv_done.notify_all();
     S->cv_mem.notify_all();
   }
@@ -214,6 +234,14 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
   size_t free_b = 0, total_b = 0;
   RG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   S->hbm_budget = (size_t)(hbm_fraction * (double)free_b);
+  // keep freed result blocks in the stream-ordered pool instead of returning
+  // them to the driver between queries
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
+    uint64_t keep = S->hbm_budget;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
   for (int i = 0; i < nworkers; i++) S->workers.emplace_back(worker_main, S);
   *out = S;
   return RG_OK;
@@ -240,6 +268,8 @@ rg_status rg_server_submit(rg_server* S, int graph, rg_query_kind kind, uint32_t
 
 rg_status rg_server_wait(rg_server* S, uint64_t ticket, void* h_result, size_t bytes, double* latency_ms) {
   if (!S) return fail(RG_EINVAL, "null server");
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
   std::unique_lock<std::mutex> lk(S->mu);
   auto it = S->results.find(ticket);
   if (it == S->results.end()) return fail(RG_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
@@ -247,13 +277,32 @@ rg_status rg_server_wait(rg_server* S, uint64_t ticket, void* h_result, size_t b
   Result r = std::move(S->results[ticket]);
   S->results.erase(ticket);
   lk.unlock();
-  if (r.status != RG_OK) return r.status;
-  if (h_result) {
-    if (bytes < r.data.size()) return fail(RG_EINVAL, "result buffer too small: need %zu bytes", r.data.size());
-    memcpy(h_result, r.data.data(), r.data.size());
+  rg_status st = r.status;
+  if (st == RG_OK && h_result && bytes < r.bytes) {
+    st = fail(RG_EINVAL, "result buffer too small: need %zu bytes", r.bytes);
   }
-  if (latency_ms) *latency_ms = r.latency_ms;
-  return RG_OK;
+  if (st == RG_OK && h_result) {
+    const cudaError_t e =
+        cudaMemcpyAsync(h_result, static_cast<char*>(r.block->p) + r.offset, r.bytes, cudaMemcpyDeviceToHost,
+                        cx->stream);
+    if (e != cudaSuccess || cudaStreamSynchronize(cx->stream) != cudaSuccess) {
+      st = cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "server result copy", __FILE__, __LINE__);
+    }
+  }
+  if (r.block) {  // the last fetch of a batch frees its block
+    bool last = false;
+    {
+      std::lock_guard<std::mutex> lk2(S->mu);
+      last = --r.block->refs == 0;
+      if (last) S->hbm_in_use -= r.block->bytes;
+    }
+    if (last) {
+      cudaFreeAsync(r.block->p, cx->stream);
+      S->cv_mem.notify_all();
+    }
+  }
+  if (st == RG_OK && latency_ms) *latency_ms = r.latency_ms;
+  return st;
 }
 
 rg_status rg_server_get_stats(rg_server* S, rg_server_stats* out) {
@@ -292,7 +341,22 @@ rg_status rg_server_free(rg_server* S) {
   }
   S->cv_work.notify_all();
   for (auto& t : S->workers) t.join();
+  // results never fetched: release their blocks
+  for (auto& kv : S->results) {
+    if (kv.second.block && kv.second.block->p && --kv.second.block->refs == 0) cudaFree(kv.second.block->p);
+  }
   delete S;
+  return RG_OK;
+}
+
+rg_status rg_pinned_alloc(size_t bytes, void** h_ptr) {
+  if (!h_ptr || bytes == 0) return fail(RG_EINVAL, "rg_pinned_alloc: bad arguments");
+  RG_CUDA(cudaHostAlloc(h_ptr, bytes, cudaHostAllocDefault));
+  return RG_OK;
+}
+
+rg_status rg_pinned_free(void* h_ptr) {
+  if (h_ptr) RG_CUDA(cudaFreeHost(h_ptr));
   return RG_OK;
 }
 

@@ -110,7 +110,43 @@ _SIGS = {
     "rg_server_get_stats": [C.c_void_p, C.c_void_p],
     "rg_server_reset_stats": [C.c_void_p],
     "rg_server_free": [C.c_void_p],
+    "rg_autotune": [C.c_void_p, C.c_int, _f64p],
+    "rg_graph_tuned_option": [C.c_void_p, C.c_int, C.c_int, _i64p],
+    "rg_graph_clear_tuning": [C.c_void_p],
+    "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
+    "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
+    "rg_pinned_free": [C.c_void_p],
 }
+
+
+class _Pinned:
+    """Owner of one page-locked host allocation backing a numpy array."""
+
+    def __init__(self, nbytes):
+        self.p = C.c_void_p()
+        _check(lib().rg_pinned_alloc(max(int(nbytes), 1), C.byref(self.p)))
+
+    def __del__(self):
+        try:
+            if self.p and self.p.value:
+                lib().rg_pinned_free(self.p)
+        except Exception:
+            pass
+
+
+class PinnedArray(np.ndarray):
+    """ndarray whose memory is page-locked; it keeps its allocation alive."""
+
+
+def pinned_empty(shape, dtype):
+    """A numpy array in page-locked host memory (fast device->host copies)."""
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape))
+    owner = _Pinned(count * dtype.itemsize)
+    buf = (C.c_char * max(count * dtype.itemsize, 1)).from_address(owner.p.value)
+    arr = np.frombuffer(buf, dtype=dtype, count=count).reshape(shape).view(PinnedArray)
+    arr._owner = owner
+    return arr
 
 QUERY_KINDS = {"bfs": 0, "bc": 1, "radii": 2}
 
@@ -308,13 +344,15 @@ class Graph:
                                  C.byref(l1)))
         return ranks, it.value, l1.value
 
-    def bfs(self, variant="push", root=0):
-        parents = np.empty(self.n, np.uint32)
-        depth = np.empty(self.n, np.int32)
+    def bfs(self, variant="push", root=0, depth_out=None, parents=True):
+        """(parents, depth, rounds, reached); depth_out: optional int32[n]
+        buffer (e.g. pinned); parents=False skips the parent array."""
+        par = np.empty(self.n, np.uint32) if parents else None
+        depth = np.empty(self.n, np.int32) if depth_out is None else depth_out
         rounds, reached = C.c_int64(), C.c_int64()
-        _check(lib().rg_bfs(self._h, _variant(variant), root, _ptr(parents, C.c_uint32), _ptr(depth, C.c_int32),
-                            C.byref(rounds), C.byref(reached)))
-        return parents, depth, rounds.value, reached.value
+        _check(lib().rg_bfs(self._h, _variant(variant), root, _ptr(par, C.c_uint32) if par is not None else None,
+                            _ptr(depth, C.c_int32), C.byref(rounds), C.byref(reached)))
+        return par, depth, rounds.value, reached.value
 
     def bc(self, variant="push", max_iters=16):
         deps = np.empty(self.n, np.float64)
@@ -322,9 +360,9 @@ class Graph:
         _check(lib().rg_bc(self._h, _variant(variant), max_iters, _ptr(deps, C.c_double), C.byref(lv)))
         return deps, lv.value
 
-    def bc_sources(self, sources, variant="push"):
+    def bc_sources(self, sources, variant="push", out=None):
         s = np.ascontiguousarray(sources, np.uint32)
-        deps = np.empty(self.n, np.float64)
+        deps = np.empty(self.n, np.float64) if out is None else out
         lv = C.c_int64()
         _check(lib().rg_bc_sources(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s),
                                    _ptr(deps, C.c_double), C.byref(lv)))
@@ -341,9 +379,9 @@ class Graph:
         _check(lib().rg_radii(self._h, _variant(variant), _ptr(r, C.c_int32), C.byref(rounds)))
         return r, rounds.value
 
-    def radii_seeds(self, seeds, variant="push"):
+    def radii_seeds(self, seeds, variant="push", out=None):
         s = np.ascontiguousarray(seeds, np.uint32)
-        r = np.empty(self.n, np.int32)
+        r = np.empty(self.n, np.int32) if out is None else out
         rounds = C.c_int64()
         _check(lib().rg_radii_seeds(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s), _ptr(r, C.c_int32),
                                     C.byref(rounds)))
@@ -360,6 +398,36 @@ def _graph_bfs_multi(self, sources):
 
 
 Graph.bfs_multi = _graph_bfs_multi
+
+
+def _graph_autotune(self, variant="radar"):
+    """Times candidate schedules per app on this graph and keeps the fastest;
+    returns {app: (best ms, {option: value})}."""
+    best = (C.c_double * 4)()
+    _check(lib().rg_autotune(self._h, _variant(variant), best))
+    out = {}
+    for a, name in enumerate(("pagerank", "bfs", "bc", "radii")):
+        opts = {}
+        for o, code in OPTIONS.items():
+            v = C.c_int64()
+            _check(lib().rg_graph_tuned_option(self._h, a, code, C.byref(v)))
+            opts[o] = v.value
+        out[name] = (best[a], opts)
+    return out
+
+
+Graph.autotune = _graph_autotune
+
+
+def _graph_set_tuning(self, tuning):
+    """Applies a tuning returned by autotune() (e.g. to a copy of the graph)."""
+    for a, name in enumerate(("pagerank", "bfs", "bc", "radii")):
+        for o, v in tuning[name][1].items():
+            if v >= 0:
+                _check(lib().rg_graph_set_tuned_option(self._h, a, OPTIONS[o], int(v)))
+
+
+Graph.set_tuning = _graph_set_tuning
 
 
 class Batch:
@@ -423,9 +491,11 @@ class Server:
         _check(lib().rg_server_submit(self._h, graph, QUERY_KINDS[kind], int(source), C.byref(t)))
         return t.value
 
-    def wait(self, ticket, graph, kind):
+    def wait(self, ticket, graph, kind, out=None):
+        """Result of `ticket` (into `out` if given, e.g. a pinned_empty array)."""
         n = self.graphs[graph].n
-        out = np.empty(n, np.float64 if kind == "bc" else np.int32)
+        if out is None:
+            out = np.empty(n, np.float64 if kind == "bc" else np.int32)
         lat = C.c_double()
         _check(lib().rg_server_wait(self._h, ticket, out.ctypes.data, out.nbytes, C.byref(lat)))
         return out, lat.value
