@@ -199,8 +199,8 @@ typedef struct rg_server rg_server;
 typedef enum rg_query_kind { RG_QUERY_BFS = 0, RG_QUERY_BC = 1, RG_QUERY_RADII = 2 } rg_query_kind;
 typedef struct rg_server_stats {
   int64_t completed;  /* queries finished since the last reset */
-  int64_t launches;   /* batches run (one traversal each) */
-  int64_t batched;    /* queries that shared a batch with others */
+  int64_t launches;   /* traversals run (a coalesced batch is one) */
+  int64_t batched;    /* queries answered by a shared multi-source traversal */
   double p50_ms;      /* submit-to-result latency percentiles */
   double p99_ms;
   double qps;         /* completed / (last completion - first submission) */
@@ -326,7 +326,11 @@ typedef enum rg_option {
    * 0 = no hub copies (HUBDUP/RADAR then update hubs with global atomics) */
   RG_OPT_HUB_SMEM_KB = 2,
   /* dense iteration when |F| + outdeg(F) > m / value (default 20, ligra.h:283) */
-  RG_OPT_DENSE_DIV = 3
+  RG_OPT_DENSE_DIV = 3,
+  /* shape of the full-graph PageRank pull sweep: 10 * (edges per lane, 4 or 8)
+   * + cache mode (0 plain loads; 1 streamed edge array; 2 streamed edge array
+   * and gathers kept in L1/L2).  Default 81.  Never changes a result. */
+  RG_OPT_SWEEP_SHAPE = 4
 } rg_option;
 rg_status rg_set_option(rg_option opt, int64_t value);
 rg_status rg_get_option(rg_option opt, int64_t* value);

@@ -1,0 +1,164 @@
+// Command-line front end shared by the PageRank, BFS, BC and Radii binaries.
+//
+// Each binary keeps the reference app's command line and run shape
+// (ligra.h:556-651, parseCommandLine.h:47-100):
+//
+//   <App> [-s] [-b] [-rounds R] [-preprocess p] [-r root] [-maxiters k]
+//         [-variant push|push-pull|degree-sorting|hubdup|radar] [-out file] <graph>
+//
+// The graph file is read (Ligra AdjacencyGraph text, or the binary
+// .config/.adj/.idx triple with -b), uploaded to the GPU and, when -preprocess
+// is 0 or 1 (the default of the degree-sorting and RADAR variants), degree
+// sorted on the device.  Compute(G, P) then runs 1 + rounds times, each timed,
+// as parallel_main does.  Results go through the C ABI in
+// include/radar_graph.h; -out writes the last round's per-vertex result in
+// original-id order, one value per line (17 significant digits for doubles).
+
+#pragma once
+
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <chrono>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "radar_graph.h"
+
+namespace rg_cli {
+
+// Flags and the trailing input file, looked up like commandLine in
+// parseCommandLine.h:47-100 (a flag's value is the argument after it).
+class commandLine {
+ public:
+  commandLine(int argc, char** argv) : argv_(argv + 1, argv + argc) {}
+  bool getOption(const char* flag) const { return find(flag) >= 0; }
+  const char* getOptionValue(const char* flag, const char* dflt) const {
+    const int i = find(flag);
+    return (i >= 0 && i + 1 < (int)argv_.size()) ? argv_[i + 1] : dflt;
+  }
+  long getOptionLongValue(const char* flag, long dflt) const {
+    const char* v = getOptionValue(flag, nullptr);
+    return v ? strtol(v, nullptr, 10) : dflt;
+  }
+  // the input file: the last argument (parseCommandLine.h:50-53)
+  const char* getArgument() const { return argv_.empty() ? nullptr : argv_.back(); }
+
+ private:
+  int find(const char* flag) const {
+    for (int i = 0; i + 1 < (int)argv_.size(); i++)  // the last argument is the file
+      if (strcmp(argv_[i], flag) == 0) return i;
+    return -1;
+  }
+  std::vector<char*> argv_;
+};
+
+struct Graph {
+  rg_graph* g = nullptr;
+  rg_variant variant = RG_RADAR;
+  int64_t n = 0, m = 0;
+  bool sorted = false;
+};
+
+inline void die(const char* what) {
+  fprintf(stderr, "%s: %s\n", what, rg_last_error());
+  exit(1);
+}
+
+inline rg_variant parse_variant(const char* s) {
+  if (!strcmp(s, "push") || !strcmp(s, "push-new-orig")) return RG_PUSH;
+  if (!strcmp(s, "push-pull")) return RG_PUSH_PULL;
+  if (!strcmp(s, "degree-sorting") || !strcmp(s, "degsort")) return RG_DEGSORT;
+  if (!strcmp(s, "hubdup")) return RG_HUBDUP;
+  if (!strcmp(s, "radar") || !strcmp(s, "RADAR")) return RG_RADAR;
+  fprintf(stderr, "unknown variant '%s'\n", s);
+  exit(2);
+}
+
+class Timer {
+ public:
+  void start() { t0_ = std::chrono::steady_clock::now(); }
+  double stop() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+  }
+
+ private:
+  std::chrono::steady_clock::time_point t0_;
+};
+
+template <class T>
+void write_output(const commandLine& P, const std::vector<T>& v) {
+  const char* path = P.getOptionValue("-out", nullptr);
+  if (!path) return;
+  FILE* f = fopen(path, "w");
+  if (!f) {
+    fprintf(stderr, "cannot write %s\n", path);
+    exit(1);
+  }
+  for (const T& x : v) {
+    if constexpr (std::is_floating_point<T>::value) {
+      fprintf(f, "%.17g\n", (double)x);
+    } else {
+      fprintf(f, "%lld\n", (long long)x);
+    }
+  }
+  fclose(f);
+}
+
+inline void report(const char* app, const Graph& G, double secs) {
+  rg_timing t;
+  if (rg_last_timing(&t) != RG_OK) memset(&t, 0, sizeof t);
+  printf("Run Time(sec) : %.6f   [%s, %s graph, device %.3f ms, %lld edges, %.2f GTEPS]\n", secs, app,
+         G.sorted ? "degree-sorted" : "original", t.total_ms, (long long)t.edges_traversed,
+         t.total_ms > 0 ? (double)t.edges_traversed / (t.total_ms * 1e6) : 0.0);
+}
+
+using ComputeFn = void (*)(Graph&, commandLine&);
+
+// parallel_main (ligra.h:556-651): load, optional degree sort, 1 + rounds runs.
+inline int run(int argc, char** argv, ComputeFn compute) {
+  commandLine P(argc, argv);
+  const char* file = P.getArgument();
+  if (argc < 2 || !file || file[0] == '-') {
+    fprintf(stderr,
+            "usage: %s [-s] [-b] [-rounds R] [-preprocess p] [-r root] [-maxiters k] "
+            "[-variant push|push-pull|degree-sorting|hubdup|radar] [-out file] <graph>\n",
+            argv[0]);
+    return 2;
+  }
+  Graph G;
+  G.variant = parse_variant(P.getOptionValue("-variant", "radar"));
+  if (!P.getOption("-s")) {
+    fprintf(stderr, "only symmetric graphs (-s) are supported\n");
+    return 2;
+  }
+  const long rounds = P.getOptionLongValue("-rounds", 3);
+  // degree-sorting and RADAR sort by default (-preprocess 1); the others do not
+  const bool sorts_by_default = G.variant == RG_DEGSORT || G.variant == RG_RADAR;
+  const long pre = P.getOptionLongValue("-preprocess", sorts_by_default ? 1 : -1);
+  uint32_t *off = nullptr, *adj = nullptr;
+  if (rg_read_graph(file, 1, P.getOption("-b") ? 1 : 0, &G.n, &G.m, &off, &adj) != RG_OK) die("read");
+  rg_graph* g0 = nullptr;
+  if (rg_graph_create(G.n, G.m, off, adj, &g0) != RG_OK) die("upload");
+  rg_host_free(off);
+  rg_host_free(adj);
+  if (pre == 0 || pre == 1) {  // symmetric: in- and out-degree coincide
+    Timer t;
+    t.start();
+    if (rg_graph_degree_sort(g0, &G.g, nullptr) != RG_OK) die("degree sort");
+    rg_synchronize();
+    printf("DegSort Time : %.6f\n", t.stop());
+    rg_graph_free(g0);
+    G.sorted = true;
+  } else {
+    G.g = g0;
+  }
+  for (long r = 0; r <= rounds; r++) compute(G, P);
+  rg_graph_free(G.g);
+  return 0;
+}
+
+}  // namespace rg_cli

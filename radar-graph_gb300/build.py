@@ -1,9 +1,10 @@
 """Build recipe for librg.so (the GB300 frontier engine).
 
 Compiles every CUDA translation unit for sm_103a only and the host C++ with
-OpenMP, in parallel, into radar-graph_gb300/_build/, and links
-radar-graph_gb300/librg.so.  Incremental: a unit is rebuilt when its source or
-any header in csrc/ is newer than its object.
+OpenMP, in parallel, into radar-graph_gb300/_build/, links
+radar-graph_gb300/librg.so, then builds the command-line apps (apps/*.cc ->
+bin/PageRank, bin/BFS, bin/BC, bin/Radii) against it.  Incremental: a unit is
+rebuilt when its source or any header in csrc/ is newer than its object.
 
     python radar-graph_gb300/build.py [-v] [--force]
 """
@@ -19,6 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg.so")
+APPS = os.path.join(HERE, "apps")
+BIN = os.path.join(HERE, "bin")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -89,7 +92,32 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    build_apps(verbose)
     return LIB
+
+
+def build_apps(verbose=False):
+    """The CLI binaries: host C++ over the C ABI, found next to librg.so at run time."""
+    os.makedirs(BIN, exist_ok=True)
+    hdr = max(os.path.getmtime(os.path.join(APPS, "cli.h")), os.path.getmtime(os.path.join(INCLUDE, "radar_graph.h")))
+    srcs = sorted(f for f in os.listdir(APPS) if f.endswith(".cc"))
+
+    def one(src):
+        exe = os.path.join(BIN, src[:-3])
+        path = os.path.join(APPS, src)
+        if (os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(path), hdr, os.path.getmtime(LIB))):
+            return exe
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, path, "-o", exe,
+               "-L", HERE, "-lrg", "-Wl,-rpath,$ORIGIN/.."]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"app build failed: {src}\n{r.stdout}\n{r.stderr}")
+        return exe
+
+    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        return list(ex.map(one, srcs))
 
 
 if __name__ == "__main__":

@@ -52,7 +52,7 @@ int max_dyn_smem();
 rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ranks, int64_t* iters_out,
                        double* l1_out, uint32_t hub_h);
 rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_parents, int32_t* h_depth,
-                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h);
+                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h, int32_t* d_depth_out = nullptr);
 rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
                  uint32_t hub_h, double* d_deps_out = nullptr);
 rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k, int32_t* h_radii,

@@ -186,7 +186,7 @@ struct BfsState {
 };
 
 rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_parents, int32_t* h_depth,
-                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h) {
+                  int64_t* rounds_out, int64_t* reached_out, uint32_t hub_h, int32_t* d_depth_out) {
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (root_orig >= (uint64_t)g->n) return fail(RG_EINVAL, "root %u >= n", root_orig);
@@ -229,6 +229,15 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
     std::swap(cur, nxt);
   }
   RG_TRY(timer.stop());
+  if (d_depth_out) {  // device copy in original-id order
+    if (g->sorted) {
+      const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
+      gather_kernel<int32_t><<<(unsigned)blocks, 256, 0, st>>>(depth, g->new_ids.as<uint32_t>(), n, d_depth_out);
+      RG_CUDA(cudaGetLastError());
+    } else {
+      RG_CUDA(cudaMemcpyAsync(d_depth_out, depth, 4 * n, cudaMemcpyDeviceToDevice, st));
+    }
+  }
   RG_TRY(download_orig<uint32_t>(g, parents, h_parents, S.tmp, st));
   RG_CUDA(cudaStreamSynchronize(st));
   RG_TRY(download_orig<int32_t>(g, depth, h_depth, S.tmp, st));
@@ -557,6 +566,12 @@ rg_status rg_set_option(rg_option opt, int64_t value) {
       if (value < 1) return fail(RG_EINVAL, "dense divisor must be >= 1");
       g_opts.dense_div = value;
       return RG_OK;
+    case RG_OPT_SWEEP_SHAPE:
+      if ((value / 10 != 4 && value / 10 != 8) || value % 10 > 2) {
+        return fail(RG_EINVAL, "sweep shape must be 40..42 or 80..82");
+      }
+      g_opts.sweep_shape = value;
+      return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -568,6 +583,7 @@ rg_status rg_get_option(rg_option opt, int64_t* value) {
     case RG_OPT_HUB_SLOTS: *value = g_opts.hub_slots; return RG_OK;
     case RG_OPT_HUB_SMEM_KB: *value = g_opts.hub_smem_kb; return RG_OK;
     case RG_OPT_DENSE_DIV: *value = g_opts.dense_div; return RG_OK;
+    case RG_OPT_SWEEP_SHAPE: *value = g_opts.sweep_shape; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }

@@ -109,17 +109,22 @@ __global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const
 
 // Dense pull over every vertex (edgeMapDense with a full frontier, the
 // push-pull variant): acc[v] = sum of contrib[u] over in-neighbours u.
-// Edge-balanced like the push sweep; a lane sums its row pieces in registers,
-// lanes holding the same row are combined by a segmented scan (rows are
-// non-decreasing across lanes), and each row piece is added to acc once.
+// Edge-balanced like the push sweep: each lane takes kItems consecutive edges
+// (one 16- or 32-byte load of the edge array) and gathers their
+// contributions; it sums its row pieces in registers, lanes holding the same
+// row are combined by a segmented scan (rows are non-decreasing across
+// lanes), and each row piece is added to acc once.  The sweep is bound by the
+// gathers' L2 requests, so kMode can stream the edge array past the caches
+// (1) and also keep gathered lines in L1/L2 (2).
 // kCache (degree-sorted graphs): the contributions of the H hubs (ids < H)
 // are copied into shared memory once per CTA -- RADAR's duplication of hub
 // data, used here for the reads of a pull instead of the writes of a push.
-template <bool kCache>
+template <bool kCache, int kItems, int kMode>
 __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
     pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v, uint32_t nchunks,
                   const uint64_t* __restrict__ contrib, unsigned long long* acc, uint32_t H,
                   const uint64_t* l1_prev) {
+  static_assert(kItems == 4 || kItems == 8, "4 or 8 edges per lane");
   if (converged(l1_prev)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* hc = reinterpret_cast<uint64_t*>(smem_raw);
@@ -127,30 +132,51 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
     for (uint32_t h = threadIdx.x; h < H; h += blockDim.x) hc[h] = contrib[h];
     __syncthreads();
   }
+  constexpr int kStep = 32 * kItems;  // edges per warp step
+  const uint64_t first = kMode >= 1 ? policy_evict_first() : 0;
+  const uint64_t keep = kMode == 2 ? policy_evict_last() : 0;
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t c = warp; c < nchunks; c += nwarps) {
     const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
 #pragma unroll
-    for (int r = 0; r < kSweepChunk / 128; r++) {
-      const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
+    for (int r = 0; r < kSweepChunk / kStep; r++) {
+      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
       uint32_t row = 0xFFFFFFFFu;
       unsigned long long part = 0;
       if (e < g.m) {
-        const uint4 u4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+        // in bounds: adj is padded by 8 entries and 32-byte aligned
+        uint32_t uu[kItems];
+        if (kItems == 8 && kMode >= 1) {
+          const U32x8 w = ld_stream_v8(g.adj + e);
+#pragma unroll
+          for (int i = 0; i < kItems; i++) uu[i] = w.v[i];
+        } else {
+#pragma unroll
+          for (int h = 0; h < kItems / 4; h++) {
+            const uint4 w = kMode >= 1 ? ld_stream_v4(g.adj + e + 4 * h, first)
+                                       : __ldg(reinterpret_cast<const uint4*>(g.adj + e + 4 * h));
+            uu[4 * h] = w.x;
+            uu[4 * h + 1] = w.y;
+            uu[4 * h + 2] = w.z;
+            uu[4 * h + 3] = w.w;
+          }
+        }
         uint32_t v = upper_index(g.off, vlo, vhi, e);
         uint32_t nxt = g.off[v + 1];
-        const uint32_t uu[4] = {u4.x, u4.y, u4.z, u4.w};
-        unsigned long long x[4];
+        unsigned long long x[kItems];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < kItems; i++) {
           const uint32_t u = uu[i];
-          x[i] = (e + i < g.m) ? ((kCache && u < H) ? hc[u] : contrib[u]) : 0ull;
+          x[i] = (e + i < g.m) ? ((kCache && u < H) ? hc[u]
+                                  : kMode == 2      ? ld_keep_u64(contrib + u, keep)
+                                                    : (unsigned long long)__ldg(contrib + u))
+                               : 0ull;
         }
         row = v;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < kItems; i++) {
           const uint32_t ee = e + i;
           if (ee >= g.m) break;
           if (ee >= nxt) {
@@ -171,6 +197,21 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
       const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
       if (row != 0xFFFFFFFFu && (lane == 31 || next_row != row) && part) atomicAdd(acc + row, part);
     }
+  }
+}
+
+using PullFn = void (*)(DevGraph, const uint32_t*, uint32_t, const uint64_t*, unsigned long long*, uint32_t,
+                        const uint64_t*);
+
+template <bool kCache>
+PullFn pull_variant(int64_t shape) {
+  switch (shape) {
+    case 41: return pr_pull_sweep<kCache, 4, 1>;
+    case 42: return pr_pull_sweep<kCache, 4, 2>;
+    case 80: return pr_pull_sweep<kCache, 8, 0>;
+    case 81: return pr_pull_sweep<kCache, 8, 1>;
+    case 82: return pr_pull_sweep<kCache, 8, 2>;
+    default: return pr_pull_sweep<kCache, 4, 0>;
   }
 }
 
@@ -255,17 +296,22 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     else RG_TRY(hub_map(g, pr_budget, hub));
     dyn = sizeof(uint64_t) * hub.H;
   }
-  const uint32_t cacheH = cache ? pr_budget : 0;
+  // the pull's hub cache holds hub_smem_kb KiB of contributions per CTA
+  const uint32_t cacheH =
+      cache ? (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_smem_kb * 1024 / (int64_t)sizeof(uint64_t)) : 0;
   auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
                   : hm == kHubMap  ? pr_push_sweep<kHubMap>
                                    : pr_push_sweep<kHubNone>;
-  auto pull_fn = cache ? pr_pull_sweep<true> : pr_pull_sweep<false>;
+  PullFn pull_fn = cache ? pull_variant<true>(g_opts.sweep_shape) : pull_variant<false>(g_opts.sweep_shape);
   const int pull_threads = cache ? 1024 : kPullThreads;
   const size_t pull_dyn = sizeof(uint64_t) * cacheH;
   const int sms = device_sms();
   int sweep_grid, per_sm = 0;
   if (pull) {
     if (pull_dyn) RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_dyn));
+    // without the hub copy the sweep uses no shared memory: give L1 the whole
+    // carve-out, it holds the hottest gathered contributions
+    RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributePreferredSharedMemoryCarveout, cache ? 100 : 0));
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pull_fn, pull_threads, pull_dyn));
     sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
                                         std::max<int64_t>((g->nchunks * 32 + pull_threads - 1) / pull_threads, 1));
@@ -323,7 +369,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   struct GraphKey {
     const void *off, *adj, *a, *b, *c, *l1;
     int64_t n, m, iters;
-    int variant, grid, pull, cacheH, hubH, hubmode;
+    int variant, grid, pull, cacheH, hubH, hubmode, shape;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof *this) == 0; }
   };
   static thread_local GraphKey cached_key;
@@ -346,6 +392,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   key.cacheH = (int)cacheH;
   key.hubH = (int)hub.H;
   key.hubmode = hm;
+  key.shape = (int)g_opts.sweep_shape;
   if (g_kernel_timing || max_iters == 0) {
     RG_CUDA(enqueue());
   } else {

@@ -32,7 +32,7 @@ struct DevGraph {
   uint32_t n;
   uint32_t m;
   const uint32_t* __restrict__ off;  // n+1
-  const uint32_t* __restrict__ adj;  // m (+4 zero padding, 16-byte aligned)
+  const uint32_t* __restrict__ adj;  // m (+8 zero padding, 32-byte aligned)
 };
 
 // A device allocation that frees itself.
@@ -85,6 +85,7 @@ struct Options {
   int64_t hub_slots = 0;     // RG_OPT_HUB_SLOTS
   int64_t hub_smem_kb = 48;  // RG_OPT_HUB_SMEM_KB (0 = no hub copies in the frontier push)
   int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
+  int64_t sweep_shape = 81;  // RG_OPT_SWEEP_SHAPE
 };
 
 // Per-thread execution context: the stream the calling thread's work goes
@@ -157,6 +158,49 @@ __device__ __forceinline__ bool bit_test(const uint32_t* bits, uint32_t v) {
 __device__ __forceinline__ void bit_set(uint32_t* bits, uint32_t v) {
   uint32_t b = 1u << (v & 31);
   if (!(__ldcg(bits + (v >> 5)) & b)) atomicOr(bits + (v >> 5), b);
+}
+
+// ---- cache-policy loads ----------------------------------------------------
+// The edge array is streamed once per sweep; the per-vertex values gathered
+// through it are re-read many times (hubs most of all).  Streaming loads skip
+// L1 and are first out of L2, so the gathered values keep the caches.
+struct U32x8 {
+  uint32_t v[8];
+};
+// 32 bytes (8 edges), 32-byte aligned: no L1 allocation, L2 evict-first.
+__device__ __forceinline__ U32x8 ld_stream_v8(const uint32_t* p) {
+  U32x8 r;
+  asm("ld.global.nc.L1::no_allocate.L2::evict_first.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+        "=r"(r.v[7])
+      : "l"(p));
+  return r;
+}
+// 16 bytes (4 edges), no L1 allocation, L2 policy `pol`.
+__device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p, uint64_t pol) {
+  uint4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+      : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
+// An L2 policy that lets lines go first (evict-first).
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+// An L2 policy that keeps lines (evict-last) for the loads that carry it.
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+// Read-only 8-byte gather kept in L1 (evict-last) and L2 (policy `pol`).
+__device__ __forceinline__ unsigned long long ld_keep_u64(const uint64_t* p, uint64_t pol) {
+  unsigned long long r;
+  asm("ld.global.nc.L1::evict_last.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
+  return r;
 }
 
 // Largest i in [lo, hi] with a[i] <= x (a non-decreasing, a[lo] <= x).

@@ -6,7 +6,11 @@
 // device -- take queries in arrival order:
 //  * BFS queries waiting for the same graph are coalesced, up to 64, into one
 //    bitmask multi-source traversal (rg_bfs_multi); a query that arrives while
-//    others are on the GPU joins the next batch (continuous batching);
+//    others are on the GPU joins the next batch (continuous batching).  A batch
+//    smaller than the graph's break-even size -- measured when the server
+//    starts: the 64-source traversal's time over one single-source BFS's --
+//    runs as single-source traversals instead, so light load costs no more
+//    than one query per launch;
 //  * a Radii query (64 seeded sample vertices) is one 64-source traversal
 //    whose per-vertex maximum depth is exactly Radii.C's radius (a vertex's
 //    mask last changes in the round of its farthest sample);
@@ -21,6 +25,8 @@
 
 #include <cuda_runtime.h>
 #include <string.h>
+
+#include <math.h>
 
 #include <algorithm>
 #include <chrono>
@@ -70,6 +76,7 @@ struct Result {
 
 struct rg_server {
   std::vector<rg_graph*> graphs;
+  std::vector<int> bfs_breakeven;  // per graph: smallest batch worth a multi-source traversal
   int device = 0;
   int max_batch = 64;
   size_t hbm_budget = 0, hbm_in_use = 0;
@@ -103,6 +110,31 @@ int radii_seeds(uint64_t seed, int64_t n, uint32_t* out) {
 size_t result_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
   return kind == RG_QUERY_BFS ? 4 * n * k : kind == RG_QUERY_BC ? 8 * n : 4 * n;
+}
+
+// Break-even batch size for one graph: time one single-source BFS and one
+// 64-source traversal (each after a warm-up run) on the calling thread.
+rg_status calibrate_bfs(rg_graph* g, int* breakeven) {
+  using namespace rg;
+  const int64_t n = g->n;
+  const int k = (int)std::min<int64_t>(n, 64);
+  std::vector<uint32_t> src(k);
+  for (int i = 0; i < k; i++) src[i] = (uint32_t)(hash_u64((uint64_t)i + 7) % (uint64_t)n);
+  DevBuf out;
+  RG_TRY(out.reserve(4 * (size_t)n * (size_t)k));
+  const int variant = g->sorted ? RG_DEGSORT : RG_PUSH;
+  double t1 = 0, tk = 0;
+  for (int rep = 0; rep < 2; rep++) {
+    auto a = Clock::now();
+    RG_TRY(bfs_run(g, variant, src[0], nullptr, nullptr, nullptr, nullptr, 0, out.as<int32_t>()));
+    auto b = Clock::now();
+    RG_TRY(bfs_multi_run(g, src.data(), k, nullptr, nullptr, out.as<int32_t>()));
+    auto c = Clock::now();
+    t1 = std::chrono::duration<double>(b - a).count();
+    tk = std::chrono::duration<double>(c - b).count();
+  }
+  *breakeven = (int)std::min<double>(65.0, std::max(2.0, std::ceil(tk / std::max(t1, 1e-9))));
+  return RG_OK;
 }
 
 size_t working_bytes(const rg_graph* g, int kind, int k) {
@@ -153,6 +185,8 @@ void worker_main(rg_server* S) {
     auto block = std::make_shared<Block>();
     block->bytes = res;
     rg_status status = cx ? RG_OK : RG_ENODEV;
+    // BFS batches below the graph's break-even size run query by query
+    const bool multi = kind == RG_QUERY_BFS && (int)batch.size() >= S->bfs_breakeven[batch[0].graph];
     if (status == RG_OK && cudaMallocAsync(&block->p, res, st) != cudaSuccess) {
       cudaGetLastError();
       status = fail(RG_ENOMEM, "server: result allocation of %zu bytes failed", res);
@@ -160,9 +194,16 @@ void worker_main(rg_server* S) {
     if (status == RG_OK) {
       if (kind == RG_QUERY_BFS) {
         const int k = (int)batch.size();
-        src.resize(k);
-        for (int i = 0; i < k; i++) src[i] = batch[i].source;
-        status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, static_cast<int32_t*>(block->p));
+        if (!multi) {
+          for (int i = 0; i < k && status == RG_OK; i++) {
+            status = rg::bfs_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, batch[i].source, nullptr, nullptr, nullptr,
+                                 nullptr, 0, static_cast<int32_t*>(block->p) + (size_t)i * (size_t)n);
+          }
+        } else {
+          src.resize(k);
+          for (int i = 0; i < k; i++) src[i] = batch[i].source;
+          status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, static_cast<int32_t*>(block->p));
+        }
       } else if (kind == RG_QUERY_RADII) {
         src.resize(64);
         const int k = radii_seeds(batch[0].source, n, src.data());
@@ -185,8 +226,12 @@ void worker_main(rg_server* S) {
       S->hbm_in_use -= work;
       if (status != RG_OK) S->hbm_in_use -= res;
       S->running--;
-      S->launches++;
-      if (batch.size() > 1) S->batched += (int64_t)batch.size();
+      if (kind == RG_QUERY_BFS && !multi) {
+        S->launches += (int64_t)batch.size();
+      } else {
+        S->launches++;
+      }
+      if (multi) S->batched += (int64_t)batch.size();
       const size_t row = kind == RG_QUERY_BC ? 8 * n : 4 * n;
       block->refs = status == RG_OK ? (int)batch.size() : 0;
       for (size_t i = 0; i < batch.size(); i++) {
@@ -234,6 +279,14 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
   size_t free_b = 0, total_b = 0;
   RG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   S->hbm_budget = (size_t)(hbm_fraction * (double)free_b);
+  S->bfs_breakeven.assign(ngraphs, 1);
+  for (int i = 0; i < ngraphs; i++) {
+    const rg_status cs = calibrate_bfs(S->graphs[i], &S->bfs_breakeven[i]);
+    if (cs != RG_OK) {
+      delete S;
+      return cs;
+    }
+  }
   // keep freed result blocks in the stream-ordered pool instead of returning
   // them to the driver between queries
   cudaMemPool_t pool;

@@ -102,6 +102,7 @@ extern "C" rg_status rg_graph_tuned_option(const rg_graph* g, int app, rg_option
     case RG_OPT_HUB_SLOTS: *value = o.hub_slots; return RG_OK;
     case RG_OPT_HUB_SMEM_KB: *value = o.hub_smem_kb; return RG_OK;
     case RG_OPT_DENSE_DIV: *value = o.dense_div; return RG_OK;
+    case RG_OPT_SWEEP_SHAPE: *value = o.sweep_shape; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -118,6 +119,7 @@ extern "C" rg_status rg_graph_set_tuned_option(rg_graph* g, int app, rg_option o
     case RG_OPT_HUB_SLOTS: o.hub_slots = value; return RG_OK;
     case RG_OPT_HUB_SMEM_KB: o.hub_smem_kb = value; return RG_OK;
     case RG_OPT_DENSE_DIV: o.dense_div = value; return RG_OK;
+    case RG_OPT_SWEEP_SHAPE: o.sweep_shape = value; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
