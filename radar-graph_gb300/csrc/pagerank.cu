@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
 using PullFn = void (*)(DevGraph, const uint32_t*, uint32_t, const uint64_t*, unsigned long long*, uint32_t,
                         const uint64_t*);
 
+
 template <bool kCache>
 PullFn pull_variant(int64_t shape) {
   switch (shape) {
@@ -280,7 +281,9 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   const uint64_t added = (uint64_t)(added_d * 9.223372036854775808e18);
   // hub set-up (host side, before the timed span).  The full sweeps run one
   // CTA per SM, so their hub copies may use the whole shared memory.
-  const int hm = hub_mode_of(variant);
+  // hub copies only with a shared-memory budget; the push kernel's hub mode is
+  // the one actually set up (a HUBDUP map kernel needs the map's arrays)
+  const int hm = g_opts.hub_smem_kb > 0 ? hub_mode_of(variant) : kHubNone;
   uint32_t pr_budget = (uint32_t)std::min<int64_t>((max_dyn_smem() - 1024) / (int)sizeof(uint64_t), n);
   if (g_opts.hub_slots > 0) pr_budget = (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_slots);
   if (hub_h) pr_budget = std::min(pr_budget, hub_h);
@@ -291,7 +294,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   const bool cache = pull && variant == RG_RADAR && g->sorted && g_opts.hub_smem_kb > 0;
   HubInfo hub;
   size_t dyn = 0;
-  if (!pull && hm != kHubNone && g_opts.hub_smem_kb > 0) {
+  if (!pull && hm != kHubNone) {
     if (hm == kHubPrefix) hub.H = pr_budget;
     else RG_TRY(hub_map(g, pr_budget, hub));
     dyn = sizeof(uint64_t) * hub.H;
@@ -299,19 +302,27 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   // the pull's hub cache holds hub_smem_kb KiB of contributions per CTA
   const uint32_t cacheH =
       cache ? (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_smem_kb * 1024 / (int64_t)sizeof(uint64_t)) : 0;
-  auto sweep_fn = hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
-                  : hm == kHubMap  ? pr_push_sweep<kHubMap>
-                                   : pr_push_sweep<kHubNone>;
+  const int push_hm = pull ? kHubNone : hm;
+  auto sweep_fn = push_hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
+                  : push_hm == kHubMap  ? pr_push_sweep<kHubMap>
+                                        : pr_push_sweep<kHubNone>;
   PullFn pull_fn = cache ? pull_variant<true>(g_opts.sweep_shape) : pull_variant<false>(g_opts.sweep_shape);
   const int pull_threads = cache ? 1024 : kPullThreads;
   const size_t pull_dyn = sizeof(uint64_t) * cacheH;
   const int sms = device_sms();
-  int sweep_grid, per_sm = 0;
+  int sweep_grid = 1, per_sm = 0;
+  // L1 caches the gathered contributions that shared memory does not: the
+  // carve-out gives shared memory only what the resident CTAs need
+  int smem_per_sm = 0;
+  RG_CUDA(cudaDeviceGetAttribute(&smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, g->device));
+  auto carveout = [&](size_t per_cta, int ctas) {
+    const size_t need = (per_cta + 1024) * (size_t)ctas;
+    return (int)std::min<size_t>(100, (need * 100 + (size_t)smem_per_sm - 1) / (size_t)std::max(smem_per_sm, 1));
+  };
   if (pull) {
     if (pull_dyn) RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_dyn));
-    // without the hub copy the sweep uses no shared memory: give L1 the whole
-    // carve-out, it holds the hottest gathered contributions
-    RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributePreferredSharedMemoryCarveout, cache ? 100 : 0));
+    RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cache ? carveout(pull_dyn, std::max(1, 2048 / pull_threads)) : 0));
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pull_fn, pull_threads, pull_dyn));
     sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
                                         std::max<int64_t>((g->nchunks * 32 + pull_threads - 1) / pull_threads, 1));
@@ -391,7 +402,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   key.pull = pull ? 1 : 0;
   key.cacheH = (int)cacheH;
   key.hubH = (int)hub.H;
-  key.hubmode = hm;
+  key.hubmode = push_hm;
   key.shape = (int)g_opts.sweep_shape;
   if (g_kernel_timing || max_iters == 0) {
     RG_CUDA(enqueue());

@@ -34,7 +34,12 @@ std::vector<Options> candidates(int app, bool hubs, const Options& base) {
       for (int64_t div : {10, 20, 40, 80}) add(1, div, 0);
       for (int64_t kb : kbs) add(0, 20, kb);
       break;
-    default:  // BC and Radii push; tune the hub budget and the dense threshold
+    case kAppRadii:  // push (hub budget x dense threshold) against pulled dense rounds
+      for (int64_t kb : kbs)
+        for (int64_t div : {20, 80}) add(0, div, kb);
+      for (int64_t div : {2, 5, 20}) add(1, div, 0);
+      break;
+    default:  // BC pushes; tune the hub budget and the dense threshold
       for (int64_t kb : kbs)
         for (int64_t div : {20, 80}) add(0, div, kb);
       break;
