@@ -56,11 +56,10 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
 rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
                  uint32_t hub_h, double* d_deps_out = nullptr);
 rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k, int32_t* h_radii,
-                    int64_t* rounds_out, uint32_t hub_h);
+                    int64_t* rounds_out, uint32_t hub_h, int32_t* d_radii_out = nullptr);
 rg_status bc_pick(const rg_graph* g, int k, uint32_t* out);
 rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
-                        int32_t* d_depths_out = nullptr, int32_t* h_max_depth = nullptr,
-                        int32_t* d_max_depth = nullptr);
+                        int32_t* d_depths_out = nullptr);
 
 // Hub slots that fit the push kernel's shared-memory budget (elem bytes each).
 uint32_t hub_budget(size_t elem, int64_t n);
@@ -154,6 +153,27 @@ rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo&
   kt_begin(st);
   kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
                               next_bits);
+  kt_end(st);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  g_timing.edge_launches++;
+  return RG_OK;
+}
+
+// One dense bitmask round over every edge (mask_pull_sweep): next_bits must be
+// cleared; the caller compacts it afterwards.
+static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
+                                          uint32_t* next_bits, cudaStream_t st) {
+  static int per_sm = 0;  // one copy per translation unit, like the kernel
+  if (!per_sm) {
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mask_pull_sweep, 256, 0));
+    RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+    per_sm = std::max(per_sm, 1);
+  }
+  const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
+  kt_begin(st);
+  mask_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+                                                                         (uint32_t)g->nchunks, visited, next, next_bits);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
   g_timing.kernel_launches++;

@@ -430,72 +430,6 @@ __global__ void radii_sync(const uint32_t* __restrict__ q, int64_t k, unsigned l
     visited[i] = next_visited[i];
   }
 }
-// Dense Radii round as a pull over every edge (edgeMapDense with Radii_F's
-// OR): next_visited[v] |= OR of visited[u] over all neighbours u.  No frontier
-// test is needed: a neighbour outside the frontier last changed two or more
-// rounds ago and pushed its (unchanged) mask to v then, so its bits are
-// already in visited[v]; the OR and the set of vertices that gain bits -- the
-// next frontier -- are exactly those of the reference's push over the
-// frontier (Radii.C:51-76).  Edge-balanced like the PageRank sweep: 8 edges
-// per lane (one streamed 32-byte load), row pieces combined by a segmented OR
-// scan, one atomicOr and activation per row piece that adds bits.
-__device__ __forceinline__ void radii_flush(const unsigned long long* __restrict__ visited,
-                                            unsigned long long* next_visited, uint32_t* next_bits, uint32_t row,
-                                            unsigned long long part) {
-  if (!part) return;
-  const unsigned long long vd = __ldg(visited + row);
-  if ((vd | part) == vd) return;
-  atomicOr(next_visited + row, part);
-  bit_set(next_bits, row);
-}
-
-__global__ void __launch_bounds__(256) radii_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
-                                                        uint32_t nchunks, const unsigned long long* __restrict__ visited,
-                                                        unsigned long long* next_visited, uint32_t* next_bits) {
-  constexpr int kItems = 8, kStep = 32 * kItems;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t c = warp; c < nchunks; c += nwarps) {
-    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
-#pragma unroll
-    for (int r = 0; r < kSweepChunk / kStep; r++) {
-      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
-      uint32_t row = kNone;
-      unsigned long long part = 0;
-      if (e < g.m) {
-        const U32x8 w = ld_stream_v8(g.adj + e);  // in bounds: adj is padded by 8 entries
-        uint32_t v = upper_index(g.off, vlo, vhi, e);
-        uint32_t nxt = g.off[v + 1];
-        unsigned long long x[kItems];
-#pragma unroll
-        for (int i = 0; i < kItems; i++) x[i] = (e + i < g.m) ? __ldg(visited + w.v[i]) : 0ull;
-        row = v;
-#pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (ee >= nxt) {
-            radii_flush(visited, next_visited, next_bits, row, part);  // a row piece that ends in this lane
-            part = 0;
-            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
-            row = v;
-          }
-          part |= x[i];
-        }
-      }
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o);
-        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
-        if (lane >= o && tr == row) part |= t;
-      }
-      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
-      if (row != kNone && (lane == 31 || next_row != row)) radii_flush(visited, next_visited, next_bits, row, part);
-    }
-  }
-}
-
 __global__ void radii_seed(const uint32_t* __restrict__ v, const unsigned long long* __restrict__ mask, int k,
                            unsigned long long* next_visited, int32_t* radii) {
   int j = threadIdx.x;
@@ -511,7 +445,7 @@ struct RadiiState {
 };
 
 rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k, int32_t* h_radii,
-                    int64_t* rounds_out, uint32_t hub_h) {
+                    int64_t* rounds_out, uint32_t hub_h, int32_t* d_radii_out) {
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (k < 0 || k > 64 || (k > 0 && !seeds_orig)) return fail(RG_EINVAL, "need 0..64 seeds");
@@ -570,20 +504,7 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
       // dense round: pull over every edge (same next masks and frontier)
       RG_CUDA(cudaMemsetAsync(nxt.bits, 0, 4 * ((n + 31) / 32), st));
       g_timing.edges_traversed += cur.degsum;
-      static int per_sm = 0;
-      if (!per_sm) {
-        RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, radii_pull_sweep, 256, 0));
-        RG_CUDA(cudaFuncSetAttribute(radii_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
-        per_sm = std::max(per_sm, 1);
-      }
-      const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
-      kt_begin(st);
-      radii_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(
-          g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks, vis, nvis, nxt.bits);
-      kt_end(st);
-      RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
-      g_timing.edge_launches++;
+      RG_TRY(launch_mask_sweep(g, vis, nvis, nxt.bits, st));
       Frontier shell;  // non-owning view of nxt for the compaction
       shell.bits.p = nxt.bits;
       RG_TRY(compact_bits(g, shell, st, true, radii, round, nullptr, nxt.queue, nxt.qoff));
@@ -598,6 +519,15 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
     std::swap(cur, nxt);
   }
   RG_TRY(timer.stop());
+  if (d_radii_out) {  // device copy in original-id order
+    if (g->sorted) {
+      const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
+      gather_kernel<int32_t><<<(unsigned)blocks, 256, 0, st>>>(radii, g->new_ids.as<uint32_t>(), n, d_radii_out);
+      RG_CUDA(cudaGetLastError());
+    } else {
+      RG_CUDA(cudaMemcpyAsync(d_radii_out, radii, 4 * n, cudaMemcpyDeviceToDevice, st));
+    }
+  }
   RG_TRY(download_orig<int32_t>(g, radii, h_radii, S.tmp, st));
   RG_CUDA(cudaStreamSynchronize(st));
   g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 16 * n + 4 * n;

@@ -387,6 +387,77 @@ __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t*
 }
 
 // ---------------------------------------------------------------------------
+// Dense round of a bitmask traversal (Radii, multi-source BFS) as a pull over
+// every edge: next[v] |= (OR of visited[u] over all neighbours u) & ~visited[v],
+// and v joins the next frontier when that adds bits.  `visited` is the mask
+// each vertex had when the round began (Radii's synced Visited, the BFS
+// `seen` set).  No frontier test is needed: a neighbour outside the frontier
+// last changed two or more rounds ago and pushed its unchanged mask to v
+// then, so its bits are already in visited[v]; the new bits and the next
+// frontier are exactly those of the push over the frontier (Radii.C:51-76).
+// Edge-balanced like the PageRank sweep: 8 edges per lane (one streamed
+// 32-byte load), row pieces combined by a segmented OR scan, one atomicOr and
+// activation per row piece that adds bits.
+// ---------------------------------------------------------------------------
+static __device__ __forceinline__ void mask_flush(const unsigned long long* __restrict__ visited,
+                                            unsigned long long* next_visited, uint32_t* next_bits, uint32_t row,
+                                            unsigned long long part) {
+  if (!part) return;
+  const unsigned long long vd = __ldg(visited + row);
+  const unsigned long long w = part & ~vd;
+  if (!w) return;
+  atomicOr(next_visited + row, w);
+  bit_set(next_bits, row);
+}
+
+static __global__ void __launch_bounds__(256) mask_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                        uint32_t nchunks, const unsigned long long* __restrict__ visited,
+                                                        unsigned long long* next_visited, uint32_t* next_bits) {
+  constexpr int kItems = 8, kStep = 32 * kItems;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / kStep; r++) {
+      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
+      uint32_t row = kNone;
+      unsigned long long part = 0;
+      if (e < g.m) {
+        const U32x8 w = ld_stream_v8(g.adj + e);  // in bounds: adj is padded by 8 entries
+        uint32_t v = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[v + 1];
+        unsigned long long x[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) x[i] = (e + i < g.m) ? __ldg(visited + w.v[i]) : 0ull;
+        row = v;
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {
+            mask_flush(visited, next_visited, next_bits, row, part);  // a row piece that ends in this lane
+            part = 0;
+            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+            row = v;
+          }
+          part |= x[i];
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o);
+        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
+        if (lane >= o && tr == row) part |= t;
+      }
+      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
+      if (row != kNone && (lane == 31 || next_row != row)) mask_flush(visited, next_visited, next_bits, row, part);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // pull (edgeMapDense + decodeInNghBreakEarly), a group of kG lanes per vertex
 // ---------------------------------------------------------------------------
 template <class Op, int kG>

@@ -68,43 +68,6 @@ struct OpMsBfs {
   }
 };
 
-// Dense level as a pull: a group of 8 lanes per vertex still missing bits
-// ORs the frontier masks of its neighbours and stops once every missing bit
-// has arrived (the early exit of decodeInNghBreakEarly, per source bit).
-__global__ void __launch_bounds__(256) ms_pull(DevGraph g, const uint32_t* __restrict__ fbits,
-                                               const unsigned long long* __restrict__ F,
-                                               const unsigned long long* __restrict__ seen, unsigned long long* N,
-                                               unsigned long long all, uint32_t* next_bits) {
-  constexpr int kG = 8;
-  const int lane = threadIdx.x & 31;
-  const int gl = lane % kG;
-  const unsigned gmask = ((1u << kG) - 1u) << (lane - gl);
-  const uint64_t group = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / kG;
-  const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / kG;
-  for (uint64_t vv = group; vv < g.n; vv += ngroups) {
-    const uint32_t v = (uint32_t)vv;
-    const unsigned long long sv = seen[v];
-    if (sv == all) continue;
-    const uint32_t b = g.off[v], e = g.off[v + 1];
-    unsigned long long acc = 0;
-    for (uint32_t j0 = b; j0 < e; j0 += kG) {
-      const uint32_t j = j0 + gl;
-      if (j < e) {
-        const uint32_t u = g.adj[j];
-        if (bit_test(fbits, u)) acc |= F[u];
-      }
-#pragma unroll
-      for (int o = kG / 2; o > 0; o >>= 1) acc |= __shfl_xor_sync(gmask, acc, o);
-      if ((acc | sv) == all) break;
-    }
-    const unsigned long long w = acc & ~sv;
-    if (gl == 0 && w) {
-      N[v] = w;
-      atomicOr(next_bits + (v >> 5), 1u << (v & 31));
-    }
-  }
-}
-
 __global__ void ms_clear_frontier(const uint32_t* __restrict__ q, int64_t k, unsigned long long* F) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j < k) F[q[j]] = 0ull;
@@ -150,18 +113,6 @@ __global__ void ms_gather(const int32_t* __restrict__ in, const uint32_t* __rest
   }
 }
 
-// out[v] = max over rows q of depth(q, v), in original-id order: a vertex's
-// Radii mask last grows in the round of its farthest sample (Radii.C:188-196).
-__global__ void ms_max_rows(const int32_t* __restrict__ depth, int64_t n, int k,
-                            const uint32_t* __restrict__ new_ids, int32_t* __restrict__ out) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t u = new_ids ? new_ids[v] : v;
-    int32_t m = -1;
-    for (int q = 0; q < k; q++) m = max(m, depth[(int64_t)q * n + u]);
-    out[v] = m;
-  }
-}
-
 struct MsState {
   DevBuf F, N, seen, depth, src, out;
   Frontier f[2];
@@ -170,7 +121,7 @@ struct MsState {
 }  // namespace
 
 rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
-                        int32_t* d_depths_out, int32_t* h_max_depth, int32_t* d_max_depth) {
+                        int32_t* d_depths_out) {
   if (!g) return fail(RG_EINVAL, "null graph");
   if (k < 1 || k > 64 || !src_orig) return fail(RG_EINVAL, "need 1..64 sources");
   OptScope opt_scope(g, kAppBfs);
@@ -194,7 +145,6 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
     src[q] = to_internal(g, src_orig[q]);
     if (std::find(uniq.begin(), uniq.end(), src[q]) == uniq.end()) uniq.push_back(src[q]);
   }
-  const unsigned long long all = k == 64 ? ~0ull : ((1ull << k) - 1ull);
   CallTimer timer(g);
   unsigned long long* F = S.F.as<unsigned long long>();
   unsigned long long* N = S.N.as<unsigned long long>();
@@ -219,14 +169,9 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
     if (dense && cur.degsum > 0) {
       RG_CUDA(cudaMemsetAsync(nxt.bits, 0, 4 * nwords, st));
       g_timing.edges_traversed += cur.degsum;
-      const int64_t blocks = std::min<int64_t>((n + 31) / 32, (int64_t)device_sms() * 16);
-      kt_begin(st);
-      ms_pull<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), cur.bits, F, seen, N, all,
-                                                                      nxt.bits);
-      kt_end(st);
-      RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
-      g_timing.edge_launches++;
+      // dense level: the bitmask pull over every edge (seen is stable during
+      // the level; N receives only the new bits)
+      RG_TRY(launch_mask_sweep(g, seen, N, nxt.bits, st));
       Frontier shell;
       shell.bits.p = nxt.bits;
       RG_TRY(compact_bits(g, shell, st, true, nullptr, 0, nullptr, nxt.queue, nxt.qoff));
@@ -250,17 +195,6 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
     std::swap(cur, nxt);
   }
   RG_TRY(timer.stop());
-  if (h_max_depth || d_max_depth) {
-    int32_t* dst = d_max_depth;
-    if (!dst) {
-      RG_TRY(S.out.reserve(4 * n));
-      dst = S.out.as<int32_t>();
-    }
-    const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)device_sms() * 32);
-    ms_max_rows<<<(unsigned)blocks, 256, 0, st>>>(depth, n, k, g->sorted ? g->new_ids.as<uint32_t>() : nullptr, dst);
-    RG_CUDA(cudaGetLastError());
-    if (h_max_depth) RG_CUDA(cudaMemcpyAsync(h_max_depth, dst, 4 * n, cudaMemcpyDeviceToHost, st));
-  }
   const int32_t* res = depth;
   if (g->sorted && (h_depths || d_depths_out)) {
     RG_TRY(S.out.reserve(4 * n * k));

@@ -11,9 +11,8 @@
 //    starts: the 64-source traversal's time over one single-source BFS's --
 //    runs as single-source traversals instead, so light load costs no more
 //    than one query per launch;
-//  * a Radii query (64 seeded sample vertices) is one 64-source traversal
-//    whose per-vertex maximum depth is exactly Radii.C's radius (a vertex's
-//    mask last changes in the round of its farthest sample);
+//  * a Radii query (64 seeded sample vertices) is one 64-bit mask traversal
+//    (Radii.C), the same run as rg_radii_seeds;
 //  * a BC query (one source) runs BC-manyiter-v2's forward/backward phases.
 // Results stay in device memory (stream-ordered allocations) until the client
 // fetches them with rg_server_wait, which copies one query's array straight
@@ -140,6 +139,7 @@ rg_status calibrate_bfs(rg_graph* g, int* breakeven) {
 size_t working_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
   if (kind == RG_QUERY_BC) return 64 * n;
+  if (kind == RG_QUERY_RADII) return 40 * n;  // two masks, radii, two frontiers
   return (size_t)(8 * k + 40) * n;  // masks, depth rows and their original-order copy, two frontiers
 }
 
@@ -207,8 +207,8 @@ void worker_main(rg_server* S) {
       } else if (kind == RG_QUERY_RADII) {
         src.resize(64);
         const int k = radii_seeds(batch[0].source, n, src.data());
-        status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, nullptr, nullptr,
-                                   static_cast<int32_t*>(block->p));
+        status = rg::radii_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, src.data(), k, nullptr, nullptr, 0,
+                               static_cast<int32_t*>(block->p));
       } else {
         const uint32_t s = batch[0].source;
         status = rg::bc_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, &s, 1, nullptr, nullptr, 0,
