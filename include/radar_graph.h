@@ -316,8 +316,9 @@ rg_status rg_bfs_depth_noalloc(const uint32_t* d_off, const uint32_t* d_adj, int
 typedef enum rg_option {
   /* 0 (default): each variant's own direction, as in the reference: push
    * variants push in dense iterations (dense_forward), push-pull pulls.
-   * 1: auto -- dense iterations pull when the operator has an early-exit or
-   * gather form that is cheaper on the GPU (BFS, PageRank), push otherwise. */
+   * 1: dense iterations pull in every variant (no atomics; BFS exits at the
+   * first frontier neighbour; Radii and multi-source BFS OR every neighbour's
+   * mask).  Results are identical either way. */
   RG_OPT_DIRECTION = 0,
   /* hub copies per CTA for HUBDUP/RADAR; 0 = as many as the budget allows */
   RG_OPT_HUB_SLOTS = 1,

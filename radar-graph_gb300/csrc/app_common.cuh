@@ -193,9 +193,9 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
     g_timing.edges_traversed += in.degsum;
     const bool dense = in.count + in.degsum > threshold;
     uint32_t* nb = out ? out->bits : nullptr;
-    // auto direction: BFS's pull exits at the first frontier neighbour, so a
-    // dense BFS level pulls whatever the variant
-    const bool pull = dense && (!o.dense_forward || (g_opts.direction == 1 && Op::kPull == kPullFirst));
+    // direction 1 pulls dense levels whatever the variant (no atomics; BFS's
+    // pull also exits at the first frontier neighbour)
+    const bool pull = dense && (!o.dense_forward || g_opts.direction == 1);
     if (pull) {
       const int64_t groups_per_block = 256 / 8;
       int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);

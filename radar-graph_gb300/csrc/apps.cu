@@ -367,7 +367,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
       // edge_map pulls a push-pull level above this size, and the pull reads
       // the level as a bitmap: build it with the same threshold
       const int64_t threshold = g->m / std::max<int64_t>(g_opts.dense_div, 1);
-      if (variant == RG_PUSH_PULL && lv.count + lv.degsum > threshold) {
+      if ((variant == RG_PUSH_PULL || g_opts.direction == 1) && lv.count + lv.degsum > threshold) {
         Frontier shell;
         shell.queue.p = lv.queue;
         shell.bits.p = lv.bits;

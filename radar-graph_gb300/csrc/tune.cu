@@ -39,7 +39,7 @@ std::vector<Options> candidates(int app, bool hubs, const Options& base) {
         for (int64_t div : {20, 80}) add(0, div, kb);
       for (int64_t div : {2, 5, 20}) add(1, div, 0);
       break;
-    default:  // BC pushes; tune the hub budget and the dense threshold
+    default:  // BC pushes (its pull scans every unvisited vertex: measured slower)
       for (int64_t kb : kbs)
         for (int64_t div : {20, 80}) add(0, div, kb);
       break;
