@@ -139,6 +139,17 @@ def allreduce(pg, x, op):
     return float(t.item())
 
 
+def measured_traffic(kernel, scale):
+    """DRAM bytes (read + write) of one launch of `kernel` on the RMAT graph of
+    this scale, from the ncu capture recorded in profiles/traffic.json (None
+    when no capture of that kernel and workload is recorded)."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    rec = json.load(open(p)).get(kernel, {})
+    return rec.get("dram_bytes_per_launch") if rec.get("scale") == scale else None
+
+
 def make_graph(rg, scale, ef, seed, uniform=False):
     src, dst = rg.generate_edges(scale, ef, seed, uniform)
     return rg.csr_from_edges(1 << scale, src, dst)
@@ -440,6 +451,11 @@ def main():
     sweep_bytes = 4 * m + 4 * (n + 1) + 8 * n + 8 * n
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
     pr_dir = tuning["pagerank"][1]["direction"]
+    sweep_kernel = "pr_pull_sweep" if pr_dir == 1 else "pr_push_sweep"
+    # the graph's gather ceiling: stream the edge array and gather 8 bytes per
+    # edge, nothing else -- what any pull over this graph must at least do
+    gather_ms = gs.gather_probe(5)
+    traffic = measured_traffic(sweep_kernel, args.scale)
     apps = {}
     for k, s in stats.items():
         apps[k] = {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3), "ms": round(s["ms"] / args.steps, 3),
@@ -503,10 +519,12 @@ def main():
                        "parallelism": "replicas", "l2": "inputs larger than L2 (no flush)",
                        "graph_build_s": round(gen_s, 1)},
             "apps": apps,
-            "roofline": {"bound": "hbm", "kernel": "pr_pull_sweep" if pr_dir == 1 else "pr_push_sweep",
+            "roofline": {"bound": "hbm", "kernel": sweep_kernel,
                          "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                         "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
-                         "bytes_per_launch": sweep_bytes, "avg_launch_ms": round(sweep_ms, 4)},
+                         "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_launch": sweep_bytes, "avg_launch_ms": round(sweep_ms, 4),
+                         "gather_ceiling_ms": round(gather_ms, 4),
+                         "frac_of_gather_ceiling": round(gather_ms / sweep_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),

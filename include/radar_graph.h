@@ -365,6 +365,13 @@ rg_status rg_last_timing(rg_timing* t);
  * by CUDA events on its stream and rg_timing.edge_ms reports their sum. */
 rg_status rg_set_kernel_timing(int on);
 
+/* Gather ceiling of g (no counterpart in the reference; a measurement aid):
+ * the best of `reps` timed passes that stream g's edge array and gather one
+ * 8-byte value per edge with perfect balance and no other work.  Every pull
+ * over g does at least this, so kernels are compared with it beside the HBM
+ * copy bandwidth. */
+rg_status rg_gather_probe(rg_graph* g, int reps, double* best_ms);
+
 #ifdef __cplusplus
 }
 #endif

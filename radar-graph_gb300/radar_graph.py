@@ -115,6 +115,7 @@ _SIGS = {
     "rg_graph_clear_tuning": [C.c_void_p],
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
+    "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
     "rg_pinned_free": [C.c_void_p],
 }
 
@@ -417,6 +418,17 @@ def _graph_autotune(self, variant="radar"):
 
 
 Graph.autotune = _graph_autotune
+
+
+def _graph_gather_probe(self, reps=5):
+    """Best time (ms) to stream the edge array and gather 8 bytes per edge:
+    the ceiling of any pull over this graph."""
+    ms = C.c_double()
+    _check(lib().rg_gather_probe(self._h, reps, C.byref(ms)))
+    return ms.value
+
+
+Graph.gather_probe = _graph_gather_probe
 
 
 def _graph_set_tuning(self, tuning):
