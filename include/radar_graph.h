@@ -129,6 +129,14 @@ rg_status rg_graph_free(rg_graph* g);
 rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks,
                       int64_t* iters_out, double* l1_out);
 
+/* PageRankDelta (PageRankDelta.C:98-155): only vertices whose delta is
+ * still above 1% of their rank propagate (vertexFilter); stops at
+ * max_iters or when sum |Delta| < 1e-7.  h_ranks: n doubles (original ids),
+ * may be NULL; iters_out: the reference's printed round count; l1_out: the
+ * last sum |Delta|. */
+rg_status rg_pagerank_delta(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks,
+                            int64_t* iters_out, double* l1_out);
+
 /* BFS (BFS.C:122-188) from ORIGINAL id `root` (-r).  h_parents (n, may be
  * NULL): parent in internal id space, UINT32_MAX if unreached.  h_depth (n,
  * may be NULL): BFS depth, -1 if unreached (bit-exact across variants). */

@@ -318,6 +318,37 @@ struct PrF {
 };
 
 // ---------------------------------------------------------------------------
+// PageRankDelta (PageRankDelta.C:29-155; RADAR hubs :44-85, hubdup hubs
+// src/hubdup/Ligra/apps/PageRankDelta.C:53-91).  nghSum[d] += Delta[s]/deg(s).
+// ---------------------------------------------------------------------------
+struct PrDeltaF {
+  const Csr* g; const double* delta; double* ngh; uint8_t* next = nullptr;
+  const Hubs* hubs; std::vector<std::vector<double>>* dup; std::vector<uint8_t>* do_merge;
+  bool cond(uint32_t) const { return true; }
+  void update(uint32_t s, uint32_t d) { ngh[d] += delta[s] / g->deg(s); }
+  void update_atomic(uint32_t s, uint32_t d, int tid) {
+    int32_t h = hubs->slot(d);
+    if (h >= 0) {
+      (*dup)[tid][h] += delta[s] / g->deg(s);
+      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+    } else {
+      add_f64(&ngh[d], delta[s] / g->deg(s));
+    }
+  }
+  void merge() {  // only hubs some thread wrote (doMerge), then reset the copies
+    if (hubs->count == 0) return;
+    int T = (int)dup->size();
+#pragma omp parallel for
+    for (int64_t h = 0; h < hubs->count; h++) {
+      if (!(*do_merge)[h]) continue;
+      (*do_merge)[h] = 0;
+      uint32_t d = hubs->vertex_of[h];
+      for (int t = 0; t < T; t++) { ngh[d] += (*dup)[t][h]; (*dup)[t][h] = 0.0; }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
 // BFS (BFS.C:28-188; push-pull variant src/push-pull/Ligra/apps/BFS.C:28-48).
 // ---------------------------------------------------------------------------
 struct BfsF {
@@ -569,6 +600,62 @@ int orc_pagerank(int64_t n, const uint32_t* off, const uint32_t* adj, int varian
   }
   memcpy(ranks, broke ? p_next : p_curr, 8 * n);
   if (iters_out) *iters_out = iter;
+  if (l1_out) *l1_out = l1;
+  return 0;
+}
+
+// PageRankDelta Compute (PageRankDelta.C:98-155).  Round 1 filters with
+// PR_Vertex_F_FirstRound (:46-61), later rounds with PR_Vertex_F (:63-76); the
+// L1 norm is the sum of |Delta| over all vertices (:140-143) and the run stops
+// when it drops below 1e-7.  push-pull pulls its dense rounds (no
+// dense_forward, src/push-pull/Ligra/apps/PageRankDelta.C:130).
+// iters_out = the reference's printed round count.
+int orc_pagerank_delta(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
+                       int64_t max_iters, int nthreads, double* ranks, int64_t* iters_out,
+                       double* l1_out) {
+  ThreadScope ts(nthreads);
+  Csr g{n, (int64_t)off[n], off, adj};
+  const double damping = 0.85, eps = 0.0000001, eps2 = 0.01;
+  const double one_over_n = 1 / (double)n;
+  const double added = (1 - damping) * one_over_n;
+  std::vector<double> p(n, 0.0), delta(n, one_over_n), ngh(n, 0.0);
+  int T = omp_get_max_threads();
+  Hubs hubs = make_hubs(g, variant, T, sizeof(double), variant == kHubDup ? 6 : 1);
+  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  std::vector<uint8_t> do_merge(hubs.count, 0);
+  std::vector<uint8_t> active(n);
+  Frontier fr = Frontier::all(n);
+  int64_t round = 0;
+  double l1 = 0.0;
+  while (round++ < max_iters) {
+    PrDeltaF f{&g, delta.data(), ngh.data(), nullptr, &hubs, &dup, &do_merge};
+    edge_map(g, fr, f, g.m / 20, false, variant != kPushPull);
+    if (round == 1) {
+#pragma omp parallel for
+      for (int64_t i = 0; i < n; i++) {
+        delta[i] = damping * ngh[i] + added;
+        p[i] += delta[i];
+        delta[i] -= one_over_n;
+        active[i] = fabs(delta[i]) > eps2 * p[i];
+      }
+    } else {
+#pragma omp parallel for
+      for (int64_t i = 0; i < n; i++) {
+        delta[i] = ngh[i] * damping;
+        active[i] = fabs(delta[i]) > eps2 * p[i];
+        if (active[i]) p[i] += delta[i];
+      }
+    }
+    l1 = 0.0;
+#pragma omp parallel for reduction(+ : l1)
+    for (int64_t i = 0; i < n; i++) l1 += fabs(delta[i]);
+    if (l1 < eps) break;
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) ngh[i] = 0.0;
+    fr = Frontier::from_bits(n, active);
+  }
+  memcpy(ranks, p.data(), 8 * n);
+  if (iters_out) *iters_out = round;
   if (l1_out) *l1_out = l1;
   return 0;
 }

@@ -93,6 +93,17 @@ def pagerank(off, adj, variant="push", max_iters=20, threads=0):
     return r, it.value, l1.value
 
 
+def pagerank_delta(off, adj, variant="push", max_iters=20, threads=0):
+    """PageRankDelta (PageRankDelta.C): (ranks, printed round count, L1)."""
+    off, adj = _u32(off), _u32(adj)
+    n = len(off) - 1
+    r = np.empty(n, np.float64)
+    it, l1 = C.c_int64(), C.c_double()
+    lib().orc_pagerank_delta(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], max_iters, threads,
+                             _p(r, C.c_double), C.byref(it), C.byref(l1))
+    return r, it.value, l1.value
+
+
 def bfs(off, adj, root, variant="push", threads=0):
     off, adj = _u32(off), _u32(adj)
     n = len(off) - 1

@@ -130,6 +130,39 @@ struct OpBfs {
   }
 };
 
+// PageRankDelta's PR_F (PageRankDelta.C:29-46): nghSum[d] += Delta[s]/deg(s),
+// no output.  `c` holds Delta[s]/deg(s) for the frontier (the same IEEE
+// quotient the reference forms per edge), 0 elsewhere.  FP64 like the
+// reference: deltas shrink geometrically, below what fixed point resolves.
+struct OpPrDelta {
+  const double* __restrict__ c;
+  double* ngh;
+  using HubT = double;
+  static constexpr int kPull = kPullSum;
+  static constexpr bool kOutput = false;
+  __device__ __forceinline__ bool cond(uint32_t) const { return true; }
+  __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
+    atomicAdd(ngh + d, c[s]);
+    return false;
+  }
+  __device__ static HubT hub_identity() { return 0.0; }
+  __device__ __forceinline__ void hub_push(HubT* hs, uint32_t slot, uint32_t s, uint32_t) const {
+    atomicAdd(hs + slot, c[s]);
+  }
+  __device__ __forceinline__ bool hub_merge(uint32_t v, HubT x) const {
+    if (x != 0.0) atomicAdd(ngh + v, x);
+    return false;
+  }
+  using PullT = double;
+  __device__ static PullT pull_identity() { return 0.0; }
+  __device__ __forceinline__ PullT pull_val(uint32_t u) const { return c[u]; }
+  __device__ static PullT combine(PullT a, PullT b) { return a + b; }
+  __device__ __forceinline__ bool pull_apply(uint32_t v, PullT x) const {
+    ngh[v] += x;
+    return false;
+  }
+};
+
 // BC_F (BC-manyiter-v2.C:32-101): num_paths[d] += num_paths[s] for unvisited
 // d; d joins the next frontier when it receives its first paths.
 struct OpBcFwd {

@@ -116,6 +116,7 @@ _SIGS = {
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
     "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
+    "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
     "rg_pinned_free": [C.c_void_p],
 }
 
@@ -343,6 +344,14 @@ class Graph:
         it, l1 = C.c_int64(), C.c_double()
         _check(lib().rg_pagerank(self._h, _variant(variant), max_iters, _ptr(ranks, C.c_double), C.byref(it),
                                  C.byref(l1)))
+        return ranks, it.value, l1.value
+
+    def pagerank_delta(self, variant="push", max_iters=100):
+        """PageRankDelta: (ranks, printed round count, final L1)."""
+        ranks = np.empty(self.n, np.float64)
+        it, l1 = C.c_int64(), C.c_double()
+        _check(lib().rg_pagerank_delta(self._h, _variant(variant), max_iters, _ptr(ranks, C.c_double),
+                                       C.byref(it), C.byref(l1)))
         return ranks, it.value, l1.value
 
     def bfs(self, variant="push", root=0, depth_out=None, parents=True):

@@ -130,6 +130,24 @@ def make(name, n, src, dst, hub_threads, workdir, out):
     res["pr200_push"] = pr_of(cap)
     res["pr200_iters"] = np.array([int(so.split("Num Iters = ")[1].split()[0])], np.int64)
 
+    # PageRankDelta: p is freed third-from-last among the n-double blocks
+    # (PageRankDelta.C:148-154 frees p, then Delta and nghSum)
+    def prd_of(cap):
+        blocks = [c for c in cap if len(c) == 8 * n]
+        return np.frombuffer(blocks[-3], np.float64).copy()
+
+    def iters_of(stdout):
+        return int(stdout.split("Num Iters = ")[1].split()[0])
+
+    for variant, pre in (("push", False), ("push-pull", False), ("degree-sorting", True)):
+        vdir = {"push": "push-new-orig"}.get(variant, variant)
+        _, _, nid, cap, so = run(vdir, "PageRankDelta", gpath, ["-maxiters", "20"], T, workdir)
+        res[f"prd_{variant}"] = to_orig(prd_of(cap), nid, pre)
+        res[f"prd_iters_{variant}"] = np.array([iters_of(so)], np.int64)
+    _, _, _, cap, so = run("push-new-orig", "PageRankDelta", gpath, ["-maxiters", "5"], T, workdir)
+    res["prd5_push"] = prd_of(cap)  # stopped by -maxiters before the L1 break
+    res["prd5_iters"] = np.array([iters_of(so)], np.int64)
+
     # BFS: depths from the reference parents (internal ids), per root
     for variant, pre in (("push", False), ("push-pull", False), ("degree-sorting", True)):
         vdir = {"push": "push-new-orig"}.get(variant, variant)
@@ -155,6 +173,9 @@ def make(name, n, src, dst, hub_threads, workdir, out):
             vdir = {"radar": "RADAR"}.get(variant, variant)
             _, _, nid, cap, _ = run(vdir, "PageRank", gpath, ["-maxiters", "20"], hub_threads, workdir)
             res[f"pr_{variant}"] = to_orig(pr_of(cap), nid, pre)
+            _, _, nid, cap, so = run(vdir, "PageRankDelta", gpath, ["-maxiters", "20"], hub_threads, workdir)
+            res[f"prd_{variant}"] = to_orig(prd_of(cap), nid, pre)
+            res[f"prd_iters_{variant}"] = np.array([iters_of(so)], np.int64)
             # hubdup BC is skipped: it builds its hub bitmap without clearing
             # it (hubdup/Ligra/apps/BC-manyiter-v2.C:267, no hubMap.reset()),
             # so its output depends on uninitialised heap memory

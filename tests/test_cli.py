@@ -98,3 +98,14 @@ def test_cli_preprocess_flag(golden, tmp_path):
         assert r.returncode == 0, r.stderr
         assert ("DegSort Time" in r.stdout) == (pre == "1")
         assert np.array_equal(np.loadtxt(out, dtype=np.int64), g["bfs0_push"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", sorted(VARIANTS))
+def test_cli_pagerank_delta(golden, tmp_path, variant):
+    g = golden["rmat12"]
+    path = _write_raw(golden, "rmat12", tmp_path)
+    out = tmp_path / "out.txt"
+    r = _run("PageRankDelta", "-s", "-rounds", "0", "-maxiters", "20", "-variant", variant, "-out", out, path)
+    assert r.returncode == 0, r.stderr
+    assert_close(np.loadtxt(out), g[f"prd_{variant}"], what="PageRankDelta via CLI")

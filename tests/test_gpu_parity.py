@@ -97,6 +97,24 @@ def test_bfs(golden, dev, name, variant):
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
 @pytest.mark.parametrize("variant", VARIANTS)
+def test_pagerank_delta(golden, dev, name, variant):
+    g = golden[name]
+    r, it, l1 = dev[name].pick(variant).pagerank_delta(variant, 20)
+    key = f"prd_{variant}" if f"prd_{variant}" in g else "prd_push"
+    assert it == int(g[f"prd_iters_{variant}" if f"prd_iters_{variant}" in g else "prd_iters_push"][0])
+    assert_close(r, g[key], what=f"prd {name} {variant}")
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_pagerank_delta_maxiters_cutoff(golden, dev, name):
+    g = golden[name]
+    r, it, _ = dev[name].g.pagerank_delta("push", 5)
+    assert it == int(g["prd5_iters"][0])
+    assert_close(r, g["prd5_push"], what=f"prd5 {name}")
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("k", [1, 4])
 def test_bc(golden, dev, name, variant, k):
     g = golden[name]
@@ -137,6 +155,16 @@ def test_s16_pagerank_vs_oracle(s16, variant):
     ro, ito, _ = orc.pagerank(s16.off, s16.adj, "push", 20, 0)
     assert it == ito
     assert_close(r, ro, what=f"s16 pr {variant}")
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_s16_pagerank_delta_vs_oracle(s16, variant):
+    G = s16.pick(variant)
+    r, it, l1 = G.pagerank_delta(variant, 100)
+    ro, ito, l1o = orc.pagerank_delta(s16.off, s16.adj, "push", 100, 0)
+    assert it == ito
+    assert_close(r, ro, what=f"s16 prd {variant}")
+    assert abs(l1 - l1o) <= 1e-9 * l1o
 
 
 @pytest.mark.parametrize("variant", VARIANTS)

@@ -41,6 +41,7 @@ class G:
         self.g = g
         self.deg = np.diff(self.off.astype(np.int64)).astype(np.uint32)
         self.pr = orc.pagerank(self.off, self.adj, "push", 20, 0)
+        self.prd = orc.pagerank_delta(self.off, self.adj, "push", 30, 0)
         self.root = int(orc.bc_sources(self.deg, 1)[0])
         self.depth = orc.bfs_depths(self.off, self.adj, self.root)
         self.bc_src = orc.bc_sources(self.deg, 2)
@@ -74,6 +75,17 @@ def test_radii_and_bfs_schedules(graph, div, direction, variant):
         _, depth, _, _ = G_.bfs(variant, graph.root)
     assert np.array_equal(r, graph.radii)
     assert np.array_equal(depth, graph.depth)
+
+
+@pytest.mark.parametrize("div", [2, 20, 80])
+@pytest.mark.parametrize("direction,kb", [(0, 0), (0, 16), (1, 0)])
+@pytest.mark.parametrize("variant", ["radar", "hubdup", "push-pull", "push"])
+def test_pagerank_delta_schedules(graph, div, direction, kb, variant):
+    G_ = graph.gs if variant == "radar" else graph.g
+    with options(dense_div=div, direction=direction, hub_smem_kb=kb):
+        r, it, _ = G_.pagerank_delta(variant, 30)
+    assert it == graph.prd[1]
+    assert_close(r, graph.prd[0], what=f"prd {variant} div {div} dir {direction} kb {kb}")
 
 
 @pytest.mark.parametrize("div", [5, 20, 80])

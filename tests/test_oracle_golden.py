@@ -69,6 +69,29 @@ def test_pagerank_l1_break(graphs, name):
 
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
+@pytest.mark.parametrize("variant", ["push", "push-pull", "degree-sorting", "hubdup", "radar"])
+def test_pagerank_delta(graphs, name, variant):
+    G = graphs[name]
+    key = f"prd_{variant}"
+    if key not in G["g"]:
+        pytest.skip("no golden for this variant on this graph")
+    o, a = _pick(G, variant)
+    r, it, l1 = orc.pagerank_delta(o, a, variant, 20, 4)
+    if variant in SORTED:
+        r = r[G["ids"]]
+    assert it == int(G["g"][f"prd_iters_{variant}"][0])
+    assert_close(r, G["g"][key], what=key)
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_pagerank_delta_maxiters_cutoff(graphs, name):
+    G = graphs[name]
+    r, it, _ = orc.pagerank_delta(G["off"], G["adj"], "push", 5, 4)
+    assert it == int(G["g"]["prd5_iters"][0])
+    assert_close(r, G["g"]["prd5_push"], what="prd5")
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
 @pytest.mark.parametrize("variant", ["push", "push-pull", "degree-sorting", "radar"])
 def test_bfs_depths(graphs, name, variant):
     G = graphs[name]
