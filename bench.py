@@ -328,7 +328,16 @@ def bench_serving(rg, graphs, rates=(200, 800, 3200), per_rate=300, seed=5, work
 # CPU baseline: the oracle port (OpenMP, all host cores)
 # ---------------------------------------------------------------------------
 
-def cpu_sample(off, adj, pr_iters=2):
+def workload_name(scale):
+    return (f"RADAR PageRank(20 it)+BFS+BC(1 src)+Radii(64) on RMAT s{scale} ef16 seed 1, symmetric, "
+            "degree-sorted, autotuned schedule")
+
+
+def cpu_sample(off, adj, pr_iters=2, with_delta=True):
+    """The oracle port on all host cores, on the bench graph: RADAR PageRank
+    (pr_iters iterations), BFS, BC (1 source), Radii (64 samples) and
+    PageRankDelta (3 rounds).  Returns seconds and edges traversed per app
+    (edges counted by the oracle's own edgeMap, as the GPU counts them)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     cores = os.cpu_count() or 1
@@ -336,22 +345,23 @@ def cpu_sample(off, adj, pr_iters=2):
     n, m = len(off) - 1, len(adj)
     root = pick_root(off)
     deg = np.diff(off.astype(np.int64)).astype(np.uint32)
-    sdeg = np.diff(so.astype(np.int64))
     src = orc.bc_sources(deg, 1)
     seeds = orc.radii_seeds(n)
     t, e = {}, {}
-    t0 = time.time()
-    orc.pagerank(so, sa, "radar", pr_iters, cores)
-    t["pagerank"], e["pagerank"] = time.time() - t0, pr_iters * m
-    t0 = time.time()
-    par, _ = orc.bfs(so, sa, int(ids[root]), "radar", cores)
-    t["bfs"], e["bfs"] = time.time() - t0, int(sdeg[par != 0xFFFFFFFF].sum())
-    t0 = time.time()
-    d, _ = orc.bc(so, sa, ids[src], "radar", cores)
-    t["bc"], e["bc"] = time.time() - t0, 2 * int(sdeg[~np.isnan(d)].sum())
-    t0 = time.time()
-    orc.radii(so, sa, ids[seeds], "radar", cores)
-    t["radii"] = time.time() - t0
+    runs = {
+        "pagerank": lambda: orc.pagerank(so, sa, "radar", pr_iters, cores),
+        "bfs": lambda: orc.bfs(so, sa, int(ids[root]), "radar", cores),
+        "bc": lambda: orc.bc(so, sa, ids[src], "radar", cores),
+        "radii": lambda: orc.radii(so, sa, ids[seeds], "radar", cores),
+    }
+    if with_delta:
+        runs["pagerank_delta_3"] = lambda: orc.pagerank_delta(so, sa, "radar", 3, cores)
+    for k, fn in runs.items():
+        orc.take_edges()
+        t0 = time.time()
+        fn()
+        t[k] = time.time() - t0
+        e[k] = orc.take_edges()
     return t, e, cores
 
 
@@ -366,9 +376,7 @@ def reference_arm(args):
     n, m = len(off) - 1, len(adj)
     steps = []
     for i in range(args.warmup + args.steps):
-        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters)
-        if "radii" not in e:  # Radii's edge count is deterministic: take it from the GPU-free restatement once
-            e["radii"] = e.get("radii", 0)
+        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters, with_delta=False)  # the headline: four apps
         if i >= args.warmup:
             steps.append((t, e))
     tot_t = sum(sum(t.values()) for t, _ in steps)
@@ -378,11 +386,11 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GTEPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tot_t / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"RADAR PageRank({args.cpu_pr_iters} it)+BFS+BC(1)+Radii(64), RMAT s{args.scale} ef16 "
-                               "seed 1, symmetric, degree-sorted", "n": n, "m": m},
+        "config": {"workload": workload_name(args.scale), "n": n, "m": m, "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (no flush)"},
         "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
                          "sample": f"PageRank {args.cpu_pr_iters} iterations + BFS + BC 1 source + Radii 64 "
-                                   "sources per step on the full graph (Radii edges not counted)"},
+                                   "sources per step on the full graph, edges counted by the port's edgeMap"},
         "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -487,6 +495,19 @@ def main():
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms / args.steps, 3)}
 
     extra = {}
+    # PageRankDelta (the first row past the four apps) on the same graph
+    prd = {}
+    for i in range(4):
+        _, prd_rounds, _ = gs.pagerank_delta("radar", 100)
+        t = rg.last_timing()
+        if i:
+            prd.setdefault("ms", []).append(t["total_ms"])
+            prd["edges"], prd["bytes"] = t["edges_traversed"], t["algorithmic_bytes"]
+    prd_ms = min(prd["ms"])
+    extra["pagerank_delta"] = {"gteps": round(prd["edges"] / (prd_ms / 1e3) / 1e9, 3), "ms": round(prd_ms, 3),
+                               "rounds": prd_rounds,
+                               "hbm_frac_of_measured": round(prd["bytes"] / (prd_ms / 1e3) / 1e9 / hbm, 4),
+                               "variant": "radar", "max_iters": 100}
     if rank == 0 and not args.no_extra:
         extra["batched"] = bench_batched(rg)
         gsv = []
@@ -502,8 +523,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters)
-        e["radii"] = stats["radii"]["edges"] / args.steps  # identical traversal, deterministic
+        t_prd, e_prd = t.pop("pagerank_delta_3"), e.pop("pagerank_delta_3")
         tot_t = sum(t.values())
+        extra["pagerank_delta"]["cpu_port_gteps_3_rounds"] = round(e_prd / t_prd / 1e9, 4)
         cpu = {"value": round(sum(e.values()) / tot_t / 1e9, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
                "sample": "oracle port, OpenMP, all host cores: RADAR PageRank 2 iterations + BFS + BC 1 source + "
                          f"Radii 64 sources on the full graph ({tot_t:.1f} s)",
@@ -514,8 +536,7 @@ def main():
             "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"RADAR PageRank(20 it)+BFS+BC(1 src)+Radii(64) on RMAT s{args.scale} ef16 seed 1, "
-                                   "symmetric, degree-sorted, autotuned schedule", "n": n, "m": m,
+            "config": {"workload": workload_name(args.scale), "n": n, "m": m,
                        "parallelism": "replicas", "l2": "inputs larger than L2 (no flush)",
                        "graph_build_s": round(gen_s, 1)},
             "apps": apps,

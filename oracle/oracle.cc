@@ -182,6 +182,10 @@ struct Frontier {
 //   void merge()                                     mergeDuplicates
 //   uint8_t* next                                    next byte map or nullptr
 // ---------------------------------------------------------------------------
+// Edges traversed by edge_map calls (sum of the frontiers' out-degrees, the
+// work the reference's edgeMap does), for the CPU baseline's edges/second.
+std::atomic<int64_t> g_edges{0};
+
 template <class F>
 Frontier edge_map(const Csr& g, Frontier& fr, F& f, int64_t threshold, bool output,
                   bool dense_forward) {
@@ -193,6 +197,7 @@ Frontier edge_map(const Csr& g, Frontier& fr, F& f, int64_t threshold, bool outp
   int64_t out_deg = 0;
 #pragma omp parallel for reduction(+ : out_deg)
   for (int64_t i = 0; i < k; i++) out_deg += g.deg(fr.ids[i]);
+  g_edges += out_deg;
   if (out_deg == 0) return Frontier::from_ids(n, {});  // ligra.h:301
   if (k + out_deg > threshold) {
     fr.to_dense();
@@ -778,6 +783,9 @@ int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
   if (rounds_out) *rounds_out = round;
   return 0;
 }
+
+// Edges traversed by every edge_map since the last call (then reset).
+int64_t orc_take_edges() { return g_edges.exchange(0); }
 
 // BC source selection (BC-manyiter-v2.C:253-271, 279-280): mt19937 seeded with
 // 27491095, uniform_int_distribution<long>(0, n-1), redrawn while the vertex has

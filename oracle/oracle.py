@@ -141,6 +141,13 @@ def bc_sources(deg_orig, k):
     return out
 
 
+def take_edges():
+    """Edges the oracle's edgeMap calls traversed since the last call."""
+    f = lib().orc_take_edges
+    f.restype = C.c_int64
+    return int(f())
+
+
 def radii_seeds(n):
     out = np.empty(64, np.uint32)
     k = lib().orc_radii_seeds(n, _p(out, C.c_uint32))

@@ -81,6 +81,57 @@ __global__ void __launch_bounds__(256) prd_filter(uint32_t n, const uint32_t* __
   }
 }
 
+// Dense round as a pull over every edge: nghSum[v] = sum of c[u] over all
+// neighbours.  c is 0 for vertices outside the frontier (the filter writes
+// it so), so no frontier test is needed and the sum is the push's over the
+// frontier.  Edge-balanced like the PageRank sweep (8 edges per lane, edge
+// array streamed), FP64 sums in a fixed order, one add per row piece.
+__global__ void __launch_bounds__(256) prd_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                      uint32_t nchunks, const double* __restrict__ c, double* ngh) {
+  constexpr int kItems = 8, kStep = 32 * kItems;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
+    const uint32_t vlo = chunk_v[ch], vhi = chunk_v[ch + 1];
+#pragma unroll
+    for (int r = 0; r < kSweepChunk / kStep; r++) {
+      const uint32_t e = ch * kSweepChunk + r * kStep + lane * kItems;
+      uint32_t row = kNone;
+      double part = 0.0;
+      if (e < g.m) {
+        const U32x8 w = ld_stream_v8(g.adj + e);  // in bounds: adj is padded by 8 entries
+        uint32_t v = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[v + 1];
+        double x[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) x[i] = (e + i < g.m) ? __ldg(c + w.v[i]) : 0.0;
+        row = v;
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {
+            if (part != 0.0) atomicAdd(ngh + row, part);  // a row piece that ends in this lane
+            part = 0.0;
+            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+            row = v;
+          }
+          part += x[i];
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, part, o);
+        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
+        if (lane >= o && tr == row) part += t;
+      }
+      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
+      if (row != kNone && (lane == 31 || next_row != row) && part != 0.0) atomicAdd(ngh + row, part);
+    }
+  }
+}
+
 struct PrdState {
   DevBuf p, delta, ngh, c, l1, tmp;
   Frontier f[2];
@@ -93,6 +144,7 @@ rg_status pagerank_delta_run(rg_graph* g, int variant, int64_t max_iters, double
   if (!g) return fail(RG_EINVAL, "null graph");
   if (variant < 0 || variant > 4) return fail(RG_EINVAL, "bad variant %d", variant);
   if (max_iters < 0) return fail(RG_EINVAL, "max_iters < 0");
+  OptScope opt_scope(g, kAppPagerank);  // the PageRank schedule: same kind of sweep
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;
@@ -125,7 +177,26 @@ rg_status pagerank_delta_run(rg_graph* g, int variant, int64_t max_iters, double
   int64_t round = 0;
   double l1 = 0.0;
   while (round++ < max_iters) {
-    RG_TRY(edge_map(g, cur, OpPrDelta{c, ngh}, nullptr, o, st));
+    const bool dense = cur.count + cur.degsum > g->m / std::max<int64_t>(g_opts.dense_div, 1);
+    if (dense && g->m > 0 && (variant == RG_PUSH_PULL || g_opts.direction == 1)) {
+      static int per_sm = 0;
+      if (!per_sm) {
+        RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prd_pull_sweep, 256, 0));
+        RG_CUDA(cudaFuncSetAttribute(prd_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+        per_sm = std::max(per_sm, 1);
+      }
+      const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
+      g_timing.edges_traversed += cur.degsum;
+      kt_begin(st);
+      prd_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+                                                                             (uint32_t)g->nchunks, c, ngh);
+      kt_end(st);
+      RG_CUDA(cudaGetLastError());
+      g_timing.kernel_launches++;
+      g_timing.edge_launches++;
+    } else {
+      RG_TRY(edge_map(g, cur, OpPrDelta{c, ngh}, nullptr, o, st));
+    }
     RG_CUDA(cudaMemsetAsync(d_l1, 0, 8, st));
     if (round == 1) {
       prd_filter<true><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), p, delta, ngh, c, one_over_n,
