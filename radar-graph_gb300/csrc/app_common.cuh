@@ -66,7 +66,6 @@ uint32_t hub_budget(size_t elem, int64_t n);
 // HUBDUP hub set (identifyHubs): bitmap + vertex->slot + slot->vertex.
 rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info);
 int hub_mode_of(int variant);
-uint32_t to_internal(const rg_graph* g, uint32_t orig);
 
 // out[v] = in[new_ids[v]]: results in original-id order (writeOutputToFile).
 template <class T>

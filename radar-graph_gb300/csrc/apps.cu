@@ -122,7 +122,8 @@ rg_status hub_map(const rg_graph* g, uint32_t H, HubInfo& info) {
   HubCache* hc = nullptr;
   for (HubCache* c : g_hub_cache) if (c->g == g && c->requested == H) hc = c;
   if (!hc) {
-    std::vector<uint32_t> d(g->h_deg);
+    RG_TRY(host_arrays(g));
+    std::vector<uint32_t> d(g->h_deg.begin(), g->h_deg.end());
     std::sort(d.begin(), d.end(), std::greater<uint32_t>());
     uint32_t thresh = H < (uint32_t)g->n ? d[H] : 0;
     int64_t nwords = (g->n + 31) / 32;
@@ -168,9 +169,6 @@ int hub_mode_of(int variant) {
   return variant == RG_RADAR ? kHubPrefix : variant == RG_HUBDUP ? kHubMap : kHubNone;
 }
 
-uint32_t to_internal(const rg_graph* g, uint32_t orig) {
-  return g->sorted ? g->h_new_ids[orig] : orig;
-}
 
 constexpr double kDamping = 0.85;  // PR_Vertex_F damping (PageRank.C:126), engine-level vertexMap
 
@@ -201,7 +199,8 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   RG_TRY(S.visited.reserve(4 * ((n + 31) / 32 + 8)));
   RG_TRY(frontier_alloc(g, S.f[0]));
   RG_TRY(frontier_alloc(g, S.f[1]));
-  const uint32_t root = to_internal(g, root_orig);
+  uint32_t root;
+  RG_TRY(lookup_ids(g, &root_orig, 1, true, &root, nullptr));
   CallTimer timer(g);
   uint32_t* parents = S.parents.as<uint32_t>();
   int32_t* depth = S.depth.as<int32_t>();
@@ -314,7 +313,8 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
   int64_t total_levels = 0;
   std::vector<int64_t> lstart, lcount, ldeg;
   for (int it = 0; it < nsrc; it++) {
-    const uint32_t start = to_internal(g, src_orig[it]);
+    uint32_t start, start_deg;
+    RG_TRY(lookup_ids(g, &src_orig[it], 1, true, &start, &start_deg));
     RG_CUDA(cudaMemsetAsync(np, 0, 8 * n, st));
     set_f64<<<1, 1, 0, st>>>(np, start, 1.0);
     RG_CUDA(cudaMemsetAsync(visited, 0, 4 * nwords, st));
@@ -322,7 +322,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     g_timing.kernel_launches += 2;
     // level 0 = {start}
     uint32_t q0[2] = {start, 0};
-    uint32_t qo0[2] = {0, g->h_deg[start]};
+    uint32_t qo0[2] = {0, start_deg};
     RG_CUDA(cudaMemcpyAsync(LQ, q0, 4, cudaMemcpyHostToDevice, st));
     RG_CUDA(cudaMemcpyAsync(LQO, qo0, 8, cudaMemcpyHostToDevice, st));
     RG_CUDA(cudaMemsetAsync(S.bits0.p, 0, 4 * nwords, st));
@@ -330,8 +330,8 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     RG_CUDA(cudaStreamSynchronize(st));  // q0/qo0 live on this stack frame
     lstart.assign(1, 0);
     lcount.assign(1, 1);
-    ldeg.assign(1, g->h_deg[start]);
-    FView cur{LQ, LQO, S.bits0.as<uint32_t>(), 1, (int64_t)g->h_deg[start]};
+    ldeg.assign(1, start_deg);
+    FView cur{LQ, LQO, S.bits0.as<uint32_t>(), 1, (int64_t)start_deg};
     uint32_t* spare_bits = S.bits1.as<uint32_t>();
     int64_t round = 0, qpos = 1;
     OpBcFwd fop{np, visited};
@@ -406,6 +406,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
 // id) has degree 0.
 rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
   if (!g || k < 0 || (k > 0 && !out)) return fail(RG_EINVAL, "bad arguments");
+  RG_TRY(host_arrays(g));
   bool any = false;
   for (int64_t v = 0; v < g->n && !any; v++) any = g->h_deg[v] > 0;
   if (!any && k > 0) return fail(RG_EINVAL, "graph has no edges; no BC source can be drawn");
@@ -413,7 +414,7 @@ rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
   std::uniform_int_distribution<long> ud(0, g->n - 1);
   for (int i = 0; i < k; i++) {
     long s;
-    do { s = ud(rng); } while (g->h_deg[to_internal(g, (uint32_t)s)] == 0);
+    do { s = ud(rng); } while (g->h_deg[g->sorted ? g->h_new_ids[s] : (uint32_t)s] == 0);
     out[i] = (uint32_t)s;
   }
   return RG_OK;
@@ -466,10 +467,9 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
   // on a collision the largest i wins (the single-thread order)
   std::vector<uint32_t> starts(k), uv;
   std::vector<unsigned long long> um;
+  RG_TRY(lookup_ids(g, seeds_orig, k, true, starts.data(), nullptr));
   for (int i = 0; i < k; i++) {
-    if (seeds_orig[i] >= (uint64_t)n) return fail(RG_EINVAL, "seed %u >= n", seeds_orig[i]);
-    uint32_t v = to_internal(g, seeds_orig[i]);
-    starts[i] = v;
+    const uint32_t v = starts[i];
     auto it = std::find(uv.begin(), uv.end(), v);
     if (it == uv.end()) { uv.push_back(v); um.push_back(1ull << i); }
     else um[it - uv.begin()] = 1ull << i;

@@ -15,6 +15,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include "rg_device.cuh"
@@ -48,7 +50,12 @@ rg_status DevBuf::reserve(size_t b) {
   if (b <= bytes && p) return RG_OK;
   release();
   size_t want = b < 256 ? 256 : b;
-  RG_CUDA(cudaMalloc(&p, want));
+  if (pooled) {  // usable from every stream once the allocating stream has it
+    RG_CUDA(cudaMallocAsync(&p, want, 0));
+    RG_CUDA(cudaStreamSynchronize(0));
+  } else {
+    RG_CUDA(cudaMalloc(&p, want));
+  }
   bytes = want;
   return RG_OK;
 }
@@ -77,6 +84,14 @@ rg_status get_ctx(Ctx** out) {
   Ctx* c = new (std::nothrow) Ctx();
   if (!c) return fail(RG_ENOMEM, "host allocation failed");
   c->device = dev;
+  {  // freed pool blocks stay mapped for reuse (graph images are large)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaHostAlloc((void**)&c->ws.h_info, 64, cudaHostAllocDefault) != cudaSuccess ||
@@ -354,16 +369,84 @@ rg_status frontier_bits_from_queue(const rg_graph* g, Frontier& f, cudaStream_t 
   return RG_OK;
 }
 
+__global__ void lookup_kernel(const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ ids, int64_t k, uint32_t* __restrict__ out_id,
+                              uint32_t* __restrict__ out_deg) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) {
+    const uint32_t v = new_ids ? new_ids[ids[i]] : ids[i];
+    out_id[i] = v;
+    out_deg[i] = off[v + 1] - off[v];
+  }
+}
+
+rg_status host_arrays(const rg_graph* g) {
+  std::lock_guard<std::mutex> lk(g->host_mu);
+  if (g->host_ready) return RG_OK;
+  const int64_t n = g->n;
+  HostU32 off(n + 1);
+  RG_CUDA(cudaMemcpy(off.data(), g->off.p, 4 * (n + 1), cudaMemcpyDeviceToHost));
+  g->h_deg.resize(n);
+#pragma omp parallel for
+  for (int64_t v = 0; v < n; v++) g->h_deg[v] = off[v + 1] - off[v];
+  if (g->sorted) {
+    g->h_new_ids.resize(n);
+    RG_CUDA(cudaMemcpy(g->h_new_ids.data(), g->new_ids.p, 4 * n, cudaMemcpyDeviceToHost));
+  }
+  g->host_ready = true;
+  return RG_OK;
+}
+
+rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool orig, uint32_t* internal_out,
+                     uint32_t* deg_out) {
+  for (int64_t i = 0; i < k; i++) {
+    if (ids[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "vertex id %u >= n", ids[i]);
+  }
+  const bool map = orig && g->sorted;
+  bool ready;
+  {
+    std::lock_guard<std::mutex> lk(g->host_mu);
+    ready = g->host_ready;
+  }
+  if (ready || k > 4096) {
+    RG_TRY(host_arrays(g));
+    for (int64_t i = 0; i < k; i++) {
+      const uint32_t v = map ? g->h_new_ids[ids[i]] : ids[i];
+      if (internal_out) internal_out[i] = v;
+      if (deg_out) deg_out[i] = g->h_deg[v];
+    }
+    return RG_OK;
+  }
+  if (k == 0) return RG_OK;
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
+  RG_TRY(cx->ws.lookup.reserve(12 * (size_t)k));
+  uint32_t* d = cx->ws.lookup.as<uint32_t>();
+  std::vector<uint32_t> back(2 * k);
+  RG_CUDA(cudaMemcpyAsync(d, ids, 4 * k, cudaMemcpyHostToDevice, st));
+  lookup_kernel<<<(unsigned)((k + 255) / 256), 256, 0, st>>>(map ? g->new_ids.as<uint32_t>() : nullptr,
+                                                             g->off.as<uint32_t>(), d, k, d + k, d + 2 * k);
+  RG_CUDA(cudaGetLastError());
+  RG_CUDA(cudaMemcpyAsync(back.data(), d + k, 8 * k, cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  for (int64_t i = 0; i < k; i++) {
+    if (internal_out) internal_out[i] = back[i];
+    if (deg_out) deg_out[i] = back[k + i];
+  }
+  return RG_OK;
+}
+
 rg_status frontier_from_host(const rg_graph* g, Frontier& f, const uint32_t* ids, int64_t k,
                              cudaStream_t st) {
   RG_TRY(frontier_alloc(g, f));
   if (k > g->n + 64) return fail(RG_EINVAL, "frontier larger than n+64 entries");
-  std::vector<uint32_t> qo(k + 1);
+  std::vector<uint32_t> qo(k + 1), deg(k);
+  RG_TRY(lookup_ids(g, ids, k, false, nullptr, deg.data()));
   uint64_t acc = 0;
   for (int64_t i = 0; i < k; i++) {
-    if (ids[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "frontier id %u >= n", ids[i]);
     qo[i] = (uint32_t)acc;
-    acc += g->h_deg[ids[i]];
+    acc += deg[i];
   }
   qo[k] = (uint32_t)acc;
   if (k) RG_CUDA(cudaMemcpyAsync(f.queue.p, ids, 4 * k, cudaMemcpyHostToDevice, st));
@@ -427,6 +510,8 @@ static rg_status new_graph(rg_graph** out) {
   RG_TRY(get_ctx(&c));
   rg_graph* g = new (std::nothrow) rg_graph();
   if (!g) return fail(RG_ENOMEM, "host allocation failed");
+  static std::atomic<uint64_t> next_uid{1};
+  g->uid = next_uid++;
   g->device = c->device;
   *out = g;
   return RG_OK;
@@ -446,11 +531,12 @@ static rg_status graph_create_common(int64_t n, int64_t m, const uint32_t* off, 
   if (m >= 0xFFFFFFFFll || n >= 0xFFFFFFFFll) {
     return fail(RG_EUNSUPPORTED, "rg_graph_create: >= 2^32 edges or vertices");
   }
-  std::vector<uint32_t> h_off(n + 1);
-  if (kind == cudaMemcpyHostToDevice) {
-    memcpy(h_off.data(), off, 4 * (n + 1));
-  } else {
-    RG_CUDA(cudaMemcpy(h_off.data(), off, 4 * (n + 1), cudaMemcpyDeviceToHost));
+  HostU32 dev_off_copy;  // a host copy of the offsets only when they live on the device
+  const uint32_t* h_off = off;
+  if (kind != cudaMemcpyHostToDevice) {
+    dev_off_copy.resize(n + 1);
+    RG_CUDA(cudaMemcpy(dev_off_copy.data(), off, 4 * (n + 1), cudaMemcpyDeviceToHost));
+    h_off = dev_off_copy.data();
   }
   if (h_off[0] != 0 || h_off[n] != (uint32_t)m) return fail(RG_EINVAL, "offsets must start at 0 and end at m");
   rg_graph* g = nullptr;
@@ -458,27 +544,44 @@ static rg_status graph_create_common(int64_t n, int64_t m, const uint32_t* off, 
   g->n = n;
   g->m = m;
   g->h_deg.resize(n);
-  uint32_t mx = 0;
-  for (int64_t v = 0; v < n; v++) {
-    if (h_off[v + 1] < h_off[v]) { delete g; return fail(RG_EINVAL, "offsets not monotone at %lld", (long long)v); }
-    g->h_deg[v] = h_off[v + 1] - h_off[v];
-    mx = std::max(mx, g->h_deg[v]);
-  }
-  g->max_deg = mx;
   rg_status s;
   if ((s = g->off.reserve(4 * (n + 1))) != RG_OK || (s = g->adj.reserve(4 * (m + 8))) != RG_OK) {
     delete g;
     return s;
   }
+  // host degrees and the monotonicity check run on a helper thread (all
+  // cores) while this thread uploads the CSR
+  int64_t bad_at = -1;
+  uint32_t mx = 0;
+  std::thread degrees([&] {
+    int64_t bad = INT64_MAX;
+    uint32_t m_loc = 0;
+#pragma omp parallel for reduction(max : m_loc) reduction(min : bad)
+    for (int64_t v = 0; v < n; v++) {
+      if (h_off[v + 1] < h_off[v]) bad = std::min(bad, v);
+      const uint32_t d = h_off[v + 1] - h_off[v];
+      g->h_deg[v] = d;
+      m_loc = std::max(m_loc, d);
+    }
+    mx = m_loc;
+    bad_at = bad == INT64_MAX ? -1 : bad;
+  });
   cudaStream_t st = ctx().stream;
-  cudaError_t e = cudaMemcpyAsync(g->off.p, h_off.data(), 4 * (n + 1), cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(g->off.p, off, 4 * (n + 1), kind, st);
   if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(g->adj.p, adj, 4 * m, kind, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(g->adj.as<uint32_t>() + m, 0, 32, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  degrees.join();
   if (e != cudaSuccess) {
     delete g;
     return cuda_fail(e, "graph upload", __FILE__, __LINE__);
   }
+  if (bad_at >= 0) {
+    delete g;
+    return fail(RG_EINVAL, "offsets not monotone at %lld", (long long)bad_at);
+  }
+  g->max_deg = mx;
+  g->host_ready = true;  // an uploaded graph's host degrees are complete (it has no permutation)
   if ((s = finish_graph(g)) != RG_OK) { delete g; return s; }
   *out = g;
   return RG_OK;
@@ -499,7 +602,11 @@ void drop_hub_cache(const rg_graph* g);
 }
 
 extern "C" rg_status rg_graph_free(rg_graph* g) {
-  if (g) rg::drop_hub_cache(g);
+  if (!g) return RG_OK;
+  rg::drop_hub_cache(g);
+  // no work may still read the graph when its pooled buffers go back
+  // (cudaFree would synchronize the device the same way)
+  cudaDeviceSynchronize();
   delete g;
   return RG_OK;
 }
@@ -517,7 +624,7 @@ extern "C" rg_status rg_graph_download(const rg_graph* g, uint32_t* h_off, uint3
   if (h_off) RG_CUDA(cudaMemcpy(h_off, g->off.p, 4 * (g->n + 1), cudaMemcpyDeviceToHost));
   if (h_adj && g->m) RG_CUDA(cudaMemcpy(h_adj, g->adj.p, 4 * g->m, cudaMemcpyDeviceToHost));
   if (h_new_ids) {
-    if (g->sorted) memcpy(h_new_ids, g->h_new_ids.data(), 4 * g->n);
+    if (g->sorted) RG_CUDA(cudaMemcpy(h_new_ids, g->new_ids.p, 4 * g->n, cudaMemcpyDeviceToHost));
     else for (int64_t i = 0; i < g->n; i++) h_new_ids[i] = (uint32_t)i;
   }
   return RG_OK;
@@ -650,7 +757,8 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
   RG_TRY(get_ctx(&c));
   cudaStream_t st = c->stream;
   Workspace& ws = c->ws;
-  DevBuf k0, v0, k1, v1, hist, new_deg;
+  // temporaries from the stream-ordered pool, released in order on `st`
+  DevBuf k0{true, st}, v0{true, st}, k1{true, st}, v1{true, st}, hist{true, st}, new_deg{true, st};
   const int64_t nblocks = (n + kSortTile - 1) / kSortTile;
   RG_TRY(k0.reserve(4 * n)); RG_TRY(v0.reserve(4 * n));
   RG_TRY(k1.reserve(4 * n)); RG_TRY(v1.reserve(4 * n));
@@ -704,18 +812,12 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
     return cuda_fail(e, "degree sort", __FILE__, __LINE__);
   }
   ng->sorted = true;
-  ng->h_new_ids.resize(n);
-  e = cudaMemcpy(ng->h_new_ids.data(), ng->new_ids.p, 4 * n, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) { delete ng; return cuda_fail(e, "new_ids download", __FILE__, __LINE__); }
-  ng->h_deg.resize(n);
-  uint32_t mx = 0;
-  for (int64_t v = 0; v < n; v++) {
-    ng->h_deg[ng->h_new_ids[v]] = g->h_deg[v];
-    mx = std::max(mx, g->h_deg[v]);
+  ng->max_deg = g->max_deg;  // host arrays: on first full use (host_arrays)
+  if (h_new_ids) {
+    e = cudaMemcpy(h_new_ids, ng->new_ids.p, 4 * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { delete ng; return cuda_fail(e, "new_ids download", __FILE__, __LINE__); }
   }
-  ng->max_deg = mx;
   if ((s = finish_graph(ng)) != RG_OK) { delete ng; return s; }
-  if (h_new_ids) memcpy(h_new_ids, ng->h_new_ids.data(), 4 * n);
   *out = ng;
   return RG_OK;
 }

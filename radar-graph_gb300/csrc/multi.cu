@@ -141,8 +141,8 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
   RG_TRY(frontier_alloc(g, S.f[0]));
   RG_TRY(frontier_alloc(g, S.f[1]));
   std::vector<uint32_t> src(k), uniq;
+  RG_TRY(lookup_ids(g, src_orig, k, true, src.data(), nullptr));
   for (int q = 0; q < k; q++) {
-    src[q] = to_internal(g, src_orig[q]);
     if (std::find(uniq.begin(), uniq.end(), src[q]) == uniq.end()) uniq.push_back(src[q]);
   }
   CallTimer timer(g);

@@ -377,8 +377,11 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     }
     return cudaGetLastError();
   };
+  // the captured launches bake in every pointer below; the graph's uid keeps
+  // a new graph whose buffers reuse a freed graph's addresses from matching
   struct GraphKey {
-    const void *off, *adj, *a, *b, *c, *l1;
+    uint64_t uid;
+    const void *off, *adj, *chunk_v, *hub_bits, *hub_slot, *hub_vertex, *a, *b, *c, *l1;
     int64_t n, m, iters;
     int variant, grid, pull, cacheH, hubH, hubmode, shape;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof *this) == 0; }
@@ -388,8 +391,13 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   static thread_local int64_t cached_launches = 0, cached_edge_launches = 0;
   GraphKey key;
   memset(&key, 0, sizeof key);  // memcmp compares the padding too: set fields one by one
+  key.uid = g->uid;
   key.off = g->off.p;
   key.adj = g->adj.p;
+  key.chunk_v = g->chunk_v.p;
+  key.hub_bits = hub.bits;
+  key.hub_slot = hub.slot;
+  key.hub_vertex = hub.vertex;
   key.a = A;
   key.b = B;
   key.c = C;

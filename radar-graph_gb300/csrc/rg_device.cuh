@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "rg_host.h"
@@ -27,6 +30,26 @@ rg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line)
     if (s_ != RG_OK) return s_;     \
   } while (0)
 
+// Host arrays of n entries that are always overwritten in full: growing them
+// does not zero the memory first (a 67 MB zero-fill per graph otherwise).
+template <class T>
+struct NoInit : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInit<U>;
+  };
+  NoInit() = default;
+  template <class U>
+  NoInit(const NoInit<U>&) {}
+  template <class U>
+  void construct(U*) noexcept {}
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+using HostU32 = std::vector<uint32_t, NoInit<uint32_t>>;
+
 // Kernel view of a symmetric CSR graph.
 struct DevGraph {
   uint32_t n;
@@ -35,16 +58,25 @@ struct DevGraph {
   const uint32_t* __restrict__ adj;  // m (+8 zero padding, 32-byte aligned)
 };
 
-// A device allocation that frees itself.
+// A device allocation that frees itself.  `pooled` buffers (a graph's CSR
+// image) come from the device's stream-ordered pool, which keeps freed blocks
+// mapped for the next graph instead of returning them to the driver; their
+// owner makes sure no work still uses them when they are released.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool pooled = false;
+  cudaStream_t free_stream = nullptr;  // pooled: the release is ordered after this stream's work
   DevBuf() = default;
+  explicit DevBuf(bool from_pool, cudaStream_t stream = nullptr) : pooled(from_pool), free_stream(stream) {}
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (pooled) cudaFreeAsync(p, free_stream);
+      else cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -72,6 +104,7 @@ struct Workspace {
   DevBuf scan_tmp;
   DevBuf tiles;          // push tile -> first frontier entry
   DevBuf counters;       // small device scalars
+  DevBuf lookup;         // lookup_ids staging
   uint64_t* h_info = nullptr;  // pinned host mirror of level info (count, degsum, ...)
   ~Workspace();
 };
@@ -106,14 +139,21 @@ Ctx& ctx();  // only after a successful get_ctx on this thread
 
 struct rg_graph {
   int device = 0;
+  uint64_t uid = 0;  // unique per graph in the process (device addresses can repeat)
   int64_t n = 0, m = 0;
-  rg::DevBuf off, adj;          // CSR on the device
-  rg::DevBuf chunk_v;           // sweep partition: first vertex of every kSweepChunk edges
+  rg::DevBuf off{true}, adj{true};  // CSR on the device
+  rg::DevBuf chunk_v{true};         // sweep partition: first vertex of every kSweepChunk edges
   int64_t nchunks = 0;
   bool sorted = false;
-  rg::DevBuf new_ids;           // orig -> internal (when sorted)
-  std::vector<uint32_t> h_new_ids;  // same on the host (empty when not sorted)
-  std::vector<uint32_t> h_deg;      // degree by internal id
+  rg::DevBuf new_ids{true};         // orig -> internal (when sorted)
+  // Host copies of new_ids and of the degree by internal id.  An uploaded
+  // graph has its degrees from creation; a degree-sorted graph copies both
+  // on first full use (host_arrays) -- most calls need a few entries (a root,
+  // the sources), which lookup_ids reads from the device instead.
+  mutable rg::HostU32 h_new_ids;
+  mutable rg::HostU32 h_deg;
+  mutable bool host_ready = false;
+  mutable std::mutex host_mu;
   uint32_t max_deg = 0;
   bool tuned[4] = {false, false, false, false};  // per app: PageRank, BFS, BC, Radii
   rg::Options topt[4];                           // the autotuner's choice per app
@@ -141,7 +181,15 @@ rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool syn
                        int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr,
                        uint32_t* queue_out = nullptr, uint32_t* qoff_out = nullptr);
 
-// Sets a frontier from host ids (queue + qoff from host degrees + bitmap).
+// Fills g's host arrays (h_new_ids when sorted, h_deg) if not yet there.
+rg_status host_arrays(const rg_graph* g);
+// For k host ids (ORIGINAL ids when `orig`, else internal): the internal id
+// and/or the degree (either output may be null).  Few ids are gathered on
+// the device; many, or a graph whose host arrays exist, use the host arrays.
+rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool orig, uint32_t* internal_out,
+                     uint32_t* deg_out);
+
+// Sets a frontier from host ids (queue + qoff from their degrees + bitmap).
 rg_status frontier_from_host(const rg_graph* g, Frontier& f, const uint32_t* ids, int64_t k,
                              cudaStream_t st);
 rg_status frontier_alloc(const rg_graph* g, Frontier& f);

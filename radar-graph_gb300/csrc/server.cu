@@ -287,13 +287,8 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
       return cs;
     }
   }
-  // keep freed result blocks in the stream-ordered pool instead of returning
-  // them to the driver between queries
-  cudaMemPool_t pool;
-  if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
-    uint64_t keep = S->hbm_budget;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-  }
+  // freed result blocks stay in the stream-ordered pool (the library keeps
+  // the device pool's freed memory mapped for reuse)
   cudaGetLastError();
   for (int i = 0; i < nworkers; i++) S->workers.emplace_back(worker_main, S);
   *out = S;

@@ -301,13 +301,20 @@ class Graph:
         return cls(h)
 
     def degree_sort(self):
-        """New graph relabelled by degree (preprocessGraph); .new_ids set."""
+        """New graph relabelled by degree (preprocessGraph); its permutation
+        is `.new_ids` (copied from the device on first access)."""
         h = C.c_void_p()
-        ids = np.empty(self.n, np.uint32)
-        _check(lib().rg_graph_degree_sort(self._h, C.byref(h), _ptr(ids, C.c_uint32)))
-        g = Graph(h)
-        g.new_ids = ids
-        return g
+        _check(lib().rg_graph_degree_sort(self._h, C.byref(h), None))
+        return Graph(h)
+
+    @property
+    def new_ids(self):
+        """new_ids[original id] = internal id (identity when not sorted)."""
+        if getattr(self, "_new_ids", None) is None:
+            ids = np.empty(self.n, np.uint32)
+            _check(lib().rg_graph_download(self._h, None, None, _ptr(ids, C.c_uint32)))
+            self._new_ids = ids
+        return self._new_ids
 
     def download(self):
         off = np.empty(self.n + 1, np.uint32)
@@ -339,8 +346,9 @@ class Graph:
         return self._h
 
     # -- apps ---------------------------------------------------------------
-    def pagerank(self, variant="push", max_iters=100):
-        ranks = np.empty(self.n, np.float64)
+    def pagerank(self, variant="push", max_iters=100, out=None):
+        """(ranks, iterations, L1); out: optional float64[n] buffer (e.g. pinned)."""
+        ranks = np.empty(self.n, np.float64) if out is None else out
         it, l1 = C.c_int64(), C.c_double()
         _check(lib().rg_pagerank(self._h, _variant(variant), max_iters, _ptr(ranks, C.c_double), C.byref(it),
                                  C.byref(l1)))
@@ -356,8 +364,12 @@ class Graph:
 
     def bfs(self, variant="push", root=0, depth_out=None, parents=True):
         """(parents, depth, rounds, reached); depth_out: optional int32[n]
-        buffer (e.g. pinned); parents=False skips the parent array."""
-        par = np.empty(self.n, np.uint32) if parents else None
+        buffer (e.g. pinned); parents: True, False (skip the parent array) or
+        a uint32[n] buffer to fill."""
+        if isinstance(parents, np.ndarray):
+            par = parents
+        else:
+            par = np.empty(self.n, np.uint32) if parents else None
         depth = np.empty(self.n, np.int32) if depth_out is None else depth_out
         rounds, reached = C.c_int64(), C.c_int64()
         _check(lib().rg_bfs(self._h, _variant(variant), root, _ptr(par, C.c_uint32) if par is not None else None,
@@ -383,8 +395,8 @@ class Graph:
         _check(lib().rg_bc_pick_sources(self._h, k, _ptr(out, C.c_uint32)))
         return out
 
-    def radii(self, variant="push"):
-        r = np.empty(self.n, np.int32)
+    def radii(self, variant="push", out=None):
+        r = np.empty(self.n, np.int32) if out is None else out
         rounds = C.c_int64()
         _check(lib().rg_radii(self._h, _variant(variant), _ptr(r, C.c_int32), C.byref(rounds)))
         return r, rounds.value

@@ -280,3 +280,26 @@ def test_edgemap_api_bfs_loop(golden):
         L.rg_frontier_free(fa)
         L.rg_frontier_free(fb)
         L.rg_device_free(dp)
+
+
+def test_recreated_graphs_do_not_reuse_stale_launches():
+    """Graphs freed and re-created with the same sizes get the same pooled
+    device addresses; cached PageRank launches must still follow the new
+    graph (a cache keyed by addresses alone replayed a freed graph's sweep
+    partition)."""
+    for rep in range(3):
+        for seed in (1, 2):
+            off, adj = rg.rmat_csr(13, 8, seed=seed)
+            with rg.Graph.from_csr(off, adj) as g, g.degree_sort() as gs:
+                for opts in ({"direction": 1, "hub_smem_kb": 0}, {"direction": 0, "hub_smem_kb": 48}):
+                    old = {k: rg.get_option(k) for k in opts}
+                    for k, v in opts.items():
+                        rg.set_option(k, v)
+                    try:
+                        r, it, _ = gs.pagerank("radar", 20)
+                    finally:
+                        for k, v in old.items():
+                            rg.set_option(k, v)
+                    ro, ito, _ = orc.pagerank(off, adj, "push", 20, 0)
+                    assert it == ito
+                    assert_close(r, ro, what=f"recreated graph seed {seed} rep {rep} {opts}")
