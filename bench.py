@@ -150,6 +150,36 @@ def measured_traffic(kernel, scale):
     return rec.get("dram_bytes_per_launch") if rec.get("scale") == scale else None
 
 
+def bench_input(rg, scale, ef=16, seed=1, reps=3):
+    """The symmetric loader's clean-up (both directions, sort, drop repeats
+    and self loops) on the host (the oracle-equivalent rg_csr_from_edges,
+    OpenMP) against the device build (rg_graph_create_from_edges), on the
+    same edge list, with the results compared."""
+    src, dst = rg.generate_edges(scale, ef, seed, False)
+    n = 1 << scale
+    t0 = time.perf_counter()
+    off, adj = rg.csr_from_edges(n, src, dst)
+    host_s = time.perf_counter() - t0
+    src_p, dst_p = rg.pinned_empty(len(src), np.uint32), rg.pinned_empty(len(dst), np.uint32)
+    src_p[:], dst_p[:] = src, dst
+    dev_ms = []
+    for i in range(reps + 1):
+        rg.lib().rg_synchronize()
+        t0 = time.perf_counter()
+        g = rg.Graph.from_edges(n, src_p, dst_p)
+        rg.lib().rg_synchronize()
+        if i:
+            dev_ms.append((time.perf_counter() - t0) * 1e3)
+        if i == reps:
+            o2, a2, _ = g.download()
+            identical = bool(np.array_equal(o2, off) and np.array_equal(a2, adj))
+        g.free()
+    return {"edges_in": int(len(src)), "n": n, "m": int(len(adj)), "host_cleanup_s": round(host_s, 3),
+            "host_threads": os.cpu_count(), "device_build_ms": round(min(dev_ms), 2),
+            "speedup": round(host_s * 1e3 / min(dev_ms), 1), "identical": identical,
+            "input": "edge list in pinned host memory (upload included)"}
+
+
 def make_graph(rg, scale, ef, seed, uniform=False):
     src, dst = rg.generate_edges(scale, ef, seed, uniform)
     return rg.csr_from_edges(1 << scale, src, dst)
@@ -516,6 +546,7 @@ def main():
                                "hbm_frac_of_measured": round(prd["bytes"] / (prd_ms / 1e3) / 1e9 / hbm, 4),
                                "variant": "radar", "max_iters": 100}
     if rank == 0 and not args.no_extra:
+        extra["graph_build"] = bench_input(rg, args.scale)
         extra["batched"] = bench_batched(rg)
         gsv = []
         for sc in (20, 22):

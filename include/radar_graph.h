@@ -97,6 +97,13 @@ rg_status rg_write_adjacency(const char* path, int64_t n, int64_t m, const uint3
  * in the reference either).  Result arrays as in rg_csr_from_edges. */
 rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_out,
                         int64_t* m_out, uint32_t** h_off_out, uint32_t** h_adj_out);
+/* Reads a GAP serialized graph (.sg, GAP/src/reader.h:251-304): bool
+ * directed, int64 directed-entry count, int64 n, int64 offsets[n+1], int32
+ * neighbours.  GAP's builder already cleaned it, so it is returned as is
+ * (bounds-checked); directed graphs give RG_EUNSUPPORTED.  Result arrays as
+ * in rg_csr_from_edges. */
+rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** h_off_out,
+                     uint32_t** h_adj_out);
 void rg_host_free(void* p);
 
 /* ------------------------------------------------------------------------
@@ -106,6 +113,14 @@ void rg_host_free(void* p);
 /* Uploads a symmetric CSR (h_off: n+1, h_adj: m) to the current device. */
 rg_status rg_graph_create(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
                           rg_graph** out);
+/* Builds the symmetric CSR on the device from an edge list (src/dst:
+ * num_edges ids < n, on the device when on_device != 0, else host arrays):
+ * both directions of every edge, neighbour lists sorted, repeats and self
+ * loops dropped -- the symmetric loader's clean-up (IO.h:429-474), the same
+ * result as rg_csr_from_edges + rg_graph_create, computed by device radix
+ * sorts instead of on the host. */
+rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_t* src,
+                                     const uint32_t* dst, int on_device, rg_graph** out);
 /* Uploads from arrays already on the device (copied; caller keeps ownership). */
 rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
                                  const uint32_t* d_adj, rg_graph** out);

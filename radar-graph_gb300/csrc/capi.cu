@@ -52,6 +52,11 @@ rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_
   return read_graph(path, symmetric, binary, n_out, m_out, h_off_out, h_adj_out);
 }
 
+rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** h_off_out,
+                     uint32_t** h_adj_out) {
+  return read_sg(path, n_out, m_out, h_off_out, h_adj_out);
+}
+
 void rg_host_free(void* p) { free(p); }
 
 rg_status rg_device_alloc(size_t bytes, void** d_ptr) {

@@ -821,3 +821,182 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
   *out = ng;
   return RG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// CSR construction on the device (the symmetric loader's clean-up, IO.h:429-474,
+// for an edge list): both directions of every edge become directed entries
+// (a, b); two stable radix sorts order them by (a, b); self loops and repeats
+// are dropped; a scan compacts the survivors into the neighbour array, and
+// each vertex's offset is the position of its first entry.  The result is
+// bit-identical to rg_csr_from_edges.
+// ---------------------------------------------------------------------------
+namespace rg {
+
+__global__ void csr_keep(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, int64_t k,
+                         uint32_t* __restrict__ keep) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t ai = a[i], bi = b[i];
+    keep[i] = (ai != bi && (i == 0 || a[i - 1] != ai || b[i - 1] != bi)) ? 1u : 0u;
+  }
+}
+
+__global__ void csr_compact(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                            const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos, int64_t k,
+                            uint32_t* __restrict__ a_out, uint32_t* __restrict__ adj) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+    if (keep[i]) {
+      a_out[pos[i]] = a[i];
+      adj[pos[i]] = b[i];
+    }
+  }
+}
+
+// off[v] = first position whose source is >= v, for v in [0, n]: position p
+// (0 <= p <= m) fills the vertices between the previous source and its own.
+__global__ void csr_offsets(const uint32_t* __restrict__ a, int64_t m, int64_t n, uint32_t* __restrict__ off) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= m; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = p == 0 ? 0 : (int64_t)a[p - 1] + 1;
+    const int64_t hi = p == m ? n : (int64_t)a[p];
+    for (int64_t v = lo; v <= hi; v++) off[v] = (uint32_t)p;
+  }
+}
+
+__global__ void max_value(const uint32_t* __restrict__ x, int64_t k, unsigned int* out) {
+  unsigned int mx = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+    mx = max(mx, x[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+__global__ void max_degree(const uint32_t* __restrict__ off, int64_t n, unsigned int* out) {
+  unsigned int mx = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    mx = max(mx, off[v + 1] - off[v]);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+// Stable LSD radix sort of k (key, val) pairs on the `bits` low key bits;
+// the result ends in (key, val) (the buffers are swapped as needed).
+static rg_status radix_pairs(Workspace& ws, DevBuf& key, DevBuf& val, DevBuf& key2, DevBuf& val2, int64_t k, int bits,
+                             DevBuf& hist, cudaStream_t st) {
+  const int64_t nblocks = (k + kSortTile - 1) / kSortTile;
+  RG_TRY(hist.reserve(4 * (256 * nblocks + 1)));
+  uint32_t *ka = key.as<uint32_t>(), *va = val.as<uint32_t>(), *kb = key2.as<uint32_t>(), *vb = val2.as<uint32_t>();
+  const int passes = (bits + 7) / 8;
+  for (int p = 0; p < passes; p++) {
+    sort_hist<<<(unsigned)nblocks, kSortThreads, 0, st>>>(ka, k, 8 * p, nblocks, hist.as<uint32_t>());
+    RG_TRY(scan_u32(ws, hist.as<uint32_t>(), hist.as<uint32_t>(), 256 * nblocks, st));
+    sort_scatter<<<(unsigned)nblocks, kSortThreads, 0, st>>>(ka, va, k, 8 * p, nblocks, hist.as<uint32_t>(), kb, vb);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  RG_CUDA(cudaGetLastError());
+  if (passes % 2) {  // the sorted pairs are in the second buffers: swap ownership
+    std::swap(key.p, key2.p);
+    std::swap(key.bytes, key2.bytes);
+    std::swap(val.p, val2.p);
+    std::swap(val.bytes, val2.bytes);
+  }
+  return RG_OK;
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                                int on_device, rg_graph** out) {
+  if (!out || n <= 0 || num_edges < 0 || (num_edges > 0 && (!src || !dst))) {
+    return fail(RG_EINVAL, "rg_graph_create_from_edges: bad arguments");
+  }
+  if (n >= 0xFFFFFFFFll || 2 * num_edges >= 0xFFFFFFFFll) {
+    return fail(RG_EUNSUPPORTED, "rg_graph_create_from_edges: >= 2^32 vertices or directed entries");
+  }
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
+  cudaStream_t st = c->stream;
+  int sms = 0;
+  RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const int64_t k = 2 * num_edges;
+  // entries (a, b): a = [src, dst], b = [dst, src]; temporaries from the pool
+  DevBuf a{true, st}, b{true, st}, a2{true, st}, b2{true, st}, hist{true, st}, info{true, st};
+  RG_TRY(a.reserve(4 * (size_t)k));
+  RG_TRY(b.reserve(4 * (size_t)k));
+  RG_TRY(a2.reserve(4 * (size_t)k));
+  RG_TRY(b2.reserve(4 * (size_t)k));
+  RG_TRY(info.reserve(8));
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (num_edges > 0) {
+    RG_CUDA(cudaMemcpyAsync(a.as<uint32_t>(), src, 4 * num_edges, kind, st));
+    RG_CUDA(cudaMemcpyAsync(a.as<uint32_t>() + num_edges, dst, 4 * num_edges, kind, st));
+    RG_CUDA(cudaMemcpyAsync(b.as<uint32_t>(), dst, 4 * num_edges, kind, st));
+    RG_CUDA(cudaMemcpyAsync(b.as<uint32_t>() + num_edges, src, 4 * num_edges, kind, st));
+  }
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((k + 255) / 256, (int64_t)sms * 32));
+  if (k > 0) {  // every id must be < n: the offsets below are indexed by them
+    uint32_t mx_id = 0;
+    RG_CUDA(cudaMemsetAsync(info.p, 0, 4, st));
+    max_value<<<blocks, 256, 0, st>>>(a.as<uint32_t>(), k, info.as<unsigned int>());
+    RG_CUDA(cudaGetLastError());
+    RG_CUDA(cudaMemcpyAsync(&mx_id, info.p, 4, cudaMemcpyDeviceToHost, st));
+    RG_CUDA(cudaStreamSynchronize(st));
+    if (mx_id >= (uint64_t)n) return fail(RG_EINVAL, "edge endpoint %u >= n", mx_id);
+  }
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)(n - 1) >> bits) != 0) bits++;
+  uint32_t* keep = a2.as<uint32_t>();
+  uint32_t* src_c = b2.as<uint32_t>();  // compacted sources
+  DevBuf scan{true, st};                 // exclusive scan of keep, k+1 entries
+  int64_t m = 0;
+  if (k > 0) {
+    // by (a, b): stable sort on b, then on a
+    RG_TRY(radix_pairs(c->ws, b, a, b2, a2, k, bits, hist, st));
+    RG_TRY(radix_pairs(c->ws, a, b, a2, b2, k, bits, hist, st));
+    keep = a2.as<uint32_t>();  // a2/b2 are free again after the sorts
+    src_c = b2.as<uint32_t>();
+    csr_keep<<<blocks, 256, 0, st>>>(a.as<uint32_t>(), b.as<uint32_t>(), k, keep);
+    RG_CUDA(cudaGetLastError());
+    RG_TRY(scan.reserve(4 * (size_t)(k + 1)));
+    RG_TRY(scan_u32(c->ws, keep, scan.as<uint32_t>(), k, st));
+    uint32_t m32 = 0;
+    RG_CUDA(cudaMemcpyAsync(&m32, scan.as<uint32_t>() + k, 4, cudaMemcpyDeviceToHost, st));
+    RG_CUDA(cudaStreamSynchronize(st));
+    m = (int64_t)m32;
+  }
+  rg_graph* g = nullptr;
+  RG_TRY(new_graph(&g));
+  g->n = n;
+  g->m = m;
+  rg_status s;
+  if ((s = g->off.reserve(4 * (n + 1))) != RG_OK || (s = g->adj.reserve(4 * (m + 8))) != RG_OK) {
+    delete g;
+    return s;
+  }
+  cudaError_t e = cudaSuccess;
+  if (k > 0) {
+    csr_compact<<<blocks, 256, 0, st>>>(a.as<uint32_t>(), b.as<uint32_t>(), keep, scan.as<uint32_t>(), k, src_c,
+                                       g->adj.as<uint32_t>());
+  }
+  const int oblocks = (int)std::max<int64_t>(1, std::min<int64_t>((m + 1 + 255) / 256, (int64_t)sms * 32));
+  csr_offsets<<<oblocks, 256, 0, st>>>(src_c, m, n, g->off.as<uint32_t>());
+  e = cudaMemsetAsync(g->adj.as<uint32_t>() + m, 0, 32, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(info.p, 0, 4, st);
+  if (e == cudaSuccess) {
+    const int dblocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16));
+    max_degree<<<dblocks, 256, 0, st>>>(g->off.as<uint32_t>(), n, info.as<unsigned int>());
+    e = cudaGetLastError();
+  }
+  uint32_t mx = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, info.p, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    delete g;
+    return cuda_fail(e, "device CSR build", __FILE__, __LINE__);
+  }
+  g->max_deg = mx;  // host degree array: on first full use (host_arrays)
+  if ((s = finish_graph(g)) != RG_OK) { delete g; return s; }
+  *out = g;
+  return RG_OK;
+}

@@ -308,4 +308,48 @@ rg_status read_graph(const char* path, int symmetric, int binary, int64_t* n_out
   return clean_and_pack((int64_t)n, off, tmp, off_out, adj_out, m_out);
 }
 
+// GAP serialized graph (.sg, GAP/src/reader.h:251-304, written by
+// writer.h): bool directed; int64 num_edges (directed entries); int64
+// num_nodes; int64 offsets[num_nodes+1]; int32 neighbours[num_edges].  GAP's
+// builder has already sorted and deduplicated it (builder.h:188-244), so it
+// is taken as is after bounds checks.  Directed graphs are refused.
+rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** off_out, uint32_t** adj_out) {
+  if (!path || !n_out || !m_out || !off_out || !adj_out) return fail(RG_EINVAL, "rg_read_sg: null argument");
+  std::vector<char> f;
+  if (!read_file(path, f)) return fail(RG_EIO, "rg_read_sg: cannot open %s", path);
+  const size_t head = 1 + 8 + 8;
+  if (f.size() < head) return fail(RG_EFORMAT, "rg_read_sg: file too short");
+  const bool directed = f[0] != 0;
+  int64_t m = 0, n = 0;
+  memcpy(&m, f.data() + 1, 8);
+  memcpy(&n, f.data() + 9, 8);
+  if (directed) return fail(RG_EUNSUPPORTED, "rg_read_sg: directed graphs are not supported");
+  if (n <= 0 || m < 0) return fail(RG_EFORMAT, "rg_read_sg: bad node or edge count");
+  if (n >= 0xFFFFFFFFll || m >= 0xFFFFFFFFll) return fail(RG_EUNSUPPORTED, "rg_read_sg: >= 2^32 nodes or edges");
+  const size_t need = head + 8 * (size_t)(n + 1) + 4 * (size_t)m;
+  if (f.size() != need) return fail(RG_EFORMAT, "rg_read_sg: file size %zu, expected %zu", f.size(), need);
+  uint32_t* o = (uint32_t*)malloc(4 * (n + 1));
+  uint32_t* a = (uint32_t*)malloc(4 * (m + 4));
+  if (!o || !a) { free(o); free(a); return fail(RG_ENOMEM, "host malloc failed"); }
+  const char* offs = f.data() + head;
+  const char* nbrs = offs + 8 * (n + 1);
+  bool bad = false;
+  for (int64_t i = 0; i <= n && !bad; i++) {
+    int64_t x;
+    memcpy(&x, offs + 8 * i, 8);
+    bad = x < 0 || x > m || (i > 0 && (uint32_t)x < o[i - 1]) || (i == 0 && x != 0) || (i == n && x != m);
+    o[i] = (uint32_t)x;
+  }
+  for (int64_t j = 0; j < m && !bad; j++) {
+    int32_t v;
+    memcpy(&v, nbrs + 4 * j, 4);
+    bad = v < 0 || v >= n;
+    a[j] = (uint32_t)v;
+  }
+  if (bad) { free(o); free(a); return fail(RG_EFORMAT, "rg_read_sg: offsets or neighbour ids out of range"); }
+  memset(a + m, 0, 16);
+  *n_out = n; *m_out = m; *off_out = o; *adj_out = a;
+  return RG_OK;
+}
+
 }  // namespace rg

@@ -116,6 +116,8 @@ _SIGS = {
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
     "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
+    "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
+    "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
     "rg_pinned_free": [C.c_void_p],
 }
@@ -262,6 +264,13 @@ def write_adjacency(path, off, adj):
                                     _ptr(adj, C.c_uint32)))
 
 
+def read_sg(path):
+    """GAP serialized undirected graph (.sg) -> CSR (off, adj)."""
+    n, m, po, pa = C.c_int64(), C.c_int64(), _u32p(), _u32p()
+    _check(lib().rg_read_sg(str(path).encode(), C.byref(n), C.byref(m), C.byref(po), C.byref(pa)))
+    return _take_host_csr(n.value, m.value, po, pa)
+
+
 def read_graph(path, symmetric=True, binary=False):
     """Ligra text (or binary) graph -> cleaned symmetric CSR (off, adj)."""
     n, m, po, pa = C.c_int64(), C.c_int64(), _u32p(), _u32p()
@@ -298,6 +307,19 @@ class Graph:
         h = C.c_void_p()
         _check(lib().rg_graph_create(len(off) - 1, len(adj), _ptr(off, C.c_uint32), _ptr(adj, C.c_uint32),
                                      C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_edges(cls, n, src, dst):
+        """Symmetric CSR built on the device from an edge list (the loader's
+        clean-up: both directions, sorted, no repeats or self loops)."""
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        if len(src) != len(dst):
+            raise ValueError("src and dst differ in length")
+        h = C.c_void_p()
+        _check(lib().rg_graph_create_from_edges(n, len(src), src.ctypes.data if len(src) else None,
+                                                dst.ctypes.data if len(dst) else None, 0, C.byref(h)))
         return cls(h)
 
     def degree_sort(self):

@@ -1,0 +1,88 @@
+"""Fast input paths: GAP serialized graphs (.sg) on the host, and the CSR
+built on the device from an edge list, which must equal the host clean-up
+(rg_csr_from_edges, the symmetric loader's IO.h:429-474) bit for bit."""
+
+import struct
+
+import numpy as np
+import pytest
+
+import radar_graph as rg
+
+
+def _write_sg(path, off, adj, directed=False, bad_size=False):
+    """GAP's layout (writer.h): bool directed, int64 edges, int64 nodes,
+    int64 offsets[n+1], int32 neighbours[m]."""
+    n, m = len(off) - 1, len(adj)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<?qq", directed, m, n))
+        f.write(np.asarray(off, np.int64).tobytes())
+        f.write(np.asarray(adj, np.int32).tobytes()[: (4 * m - 4) if bad_size else None])
+
+
+def test_sg_round_trip(tmp_path):
+    off, adj = rg.rmat_csr(10, 8, seed=4)
+    p = tmp_path / "g.sg"
+    _write_sg(p, off, adj)
+    o2, a2 = rg.read_sg(p)
+    assert np.array_equal(o2, off) and np.array_equal(a2, adj)
+
+
+def test_sg_errors(tmp_path):
+    off, adj = rg.rmat_csr(8, 4, seed=1)
+    p = tmp_path / "d.sg"
+    _write_sg(p, off, adj, directed=True)
+    with pytest.raises(rg.RgError, match="directed"):
+        rg.read_sg(p)
+    _write_sg(p, off, adj, bad_size=True)
+    with pytest.raises(rg.RgError, match="size"):
+        rg.read_sg(p)
+    bad = np.array(adj, copy=True)
+    bad[3] = len(off) + 5  # neighbour id >= n
+    _write_sg(p, off, bad)
+    with pytest.raises(rg.RgError, match="range"):
+        rg.read_sg(p)
+    with pytest.raises(rg.RgError):
+        rg.read_sg(tmp_path / "missing.sg")
+
+
+def test_device_build_rejects_bad_arguments():
+    with pytest.raises(rg.RgError):
+        rg.Graph.from_edges(0, np.zeros(1, np.uint32), np.zeros(1, np.uint32))
+    with pytest.raises(ValueError):
+        rg.Graph.from_edges(4, np.zeros(2, np.uint32), np.zeros(1, np.uint32))
+
+
+def _cases():
+    yield "tiny", 12, np.array([0, 0, 1, 2, 2, 3, 4, 5, 5, 6, 7, 8, 1, 0, 4], np.uint32), \
+        np.array([1, 1, 2, 0, 2, 4, 5, 3, 6, 7, 8, 6, 3, 0, 4], np.uint32)
+    yield "loops_only", 5, np.array([0, 1, 1, 4], np.uint32), np.array([0, 1, 1, 4], np.uint32)
+    yield "no_edges", 7, np.zeros(0, np.uint32), np.zeros(0, np.uint32)
+    yield "one_vertex", 1, np.zeros(3, np.uint32), np.zeros(3, np.uint32)
+    yield "isolated_tail", 100, np.array([0, 1, 2], np.uint32), np.array([1, 2, 0], np.uint32)
+    for sc, ef, seed, uni in ((10, 16, 1, False), (12, 8, 2, True), (14, 16, 3, False), (16, 16, 1, False)):
+        s, d = rg.generate_edges(sc, ef, seed, uni)
+        yield f"{'er' if uni else 'rmat'}{sc}", 1 << sc, s, d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
+def test_device_build_equals_host_cleanup(case):
+    _, n, s, d = case
+    off, adj = rg.csr_from_edges(n, s, d)
+    with rg.Graph.from_edges(n, s, d) as g:
+        assert (g.n, g.m) == (n, len(adj))
+        o2, a2, _ = g.download()
+        assert np.array_equal(o2, off)
+        assert np.array_equal(a2, adj)
+        if len(adj):  # and the apps run on it like on an uploaded graph
+            r, it, _ = g.pagerank("push", 5)
+            with rg.Graph.from_csr(off, adj) as g2:
+                r2, it2, _ = g2.pagerank("push", 5)
+            assert it == it2 and np.array_equal(r, r2)
+
+
+@pytest.mark.gpu
+def test_device_build_rejects_ids_out_of_range():
+    with pytest.raises(rg.RgError, match="endpoint"):
+        rg.Graph.from_edges(4, np.array([0, 1], np.uint32), np.array([2, 9], np.uint32))
