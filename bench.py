@@ -180,6 +180,35 @@ def bench_input(rg, scale, ef=16, seed=1, reps=3):
             "input": "edge list in pinned host memory (upload included)"}
 
 
+def bench_triangles(rg, gs, with_cpu, small_scale=20):
+    """Triangle counting (GAP tc_local): the GPU on the bench graph, and GPU
+    against the oracle port (all host cores) on a smaller RMAT graph."""
+    out = {}
+    ms = []
+    for i in range(3):
+        _, total = gs.triangles()
+        if i:
+            ms.append(rg.last_timing()["total_ms"])
+    out["s_bench"] = {"triangles": int(total), "ms": round(min(ms), 2)}
+    off, adj = make_graph(rg, small_scale, 16, 1)
+    with rg.Graph.from_csr(off, adj) as g:
+        g.triangles()
+        t0 = time.perf_counter()
+        _, tg = g.triangles()
+        gpu_s = time.perf_counter() - t0
+    small = {"scale": small_scale, "triangles": int(tg), "gpu_ms": round(gpu_s * 1e3, 2)}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        t0 = time.perf_counter()
+        _, tc = orc.triangles(off, adj, os.cpu_count() or 1)
+        small["cpu_port_s"] = round(time.perf_counter() - t0, 3)
+        small["cpu_threads"] = os.cpu_count()
+        small["identical"] = int(tc) == int(tg)
+    out["s_small"] = small
+    return out
+
+
 def make_graph(rg, scale, ef, seed, uniform=False):
     src, dst = rg.generate_edges(scale, ef, seed, uniform)
     return rg.csr_from_edges(1 << scale, src, dst)
@@ -547,6 +576,7 @@ def main():
                                "variant": "radar", "max_iters": 100}
     if rank == 0 and not args.no_extra:
         extra["graph_build"] = bench_input(rg, args.scale)
+        extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
         extra["batched"] = bench_batched(rg)
         gsv = []
         for sc in (20, 22):

@@ -152,6 +152,13 @@ rg_status rg_pagerank(rg_graph* g, rg_variant variant, int64_t max_iters, double
 rg_status rg_pagerank_delta(rg_graph* g, rg_variant variant, int64_t max_iters, double* h_ranks,
                             int64_t* iters_out, double* l1_out);
 
+/* Triangle counting (GAP tc_local, src/<variant>/GAP/src/tc_local.cc): *total_out =
+ * number of triangles; h_counts (n, may be NULL) = triangles containing each
+ * vertex, by ORIGINAL id (they sum to 3 * total).  Needs a cleaned symmetric
+ * graph (the loaders' output).  Works on any graph handle: the degree order
+ * with sorted neighbour lists is built internally. */
+rg_status rg_triangle_count(rg_graph* g, uint64_t* h_counts, uint64_t* total_out);
+
 /* BFS (BFS.C:122-188) from ORIGINAL id `root` (-r).  h_parents (n, may be
  * NULL): parent in internal id space, UINT32_MAX if unreached.  h_depth (n,
  * may be NULL): BFS depth, -1 if unreached (bit-exact across variants). */

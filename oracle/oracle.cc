@@ -784,6 +784,57 @@ int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
   return 0;
 }
 
+// Triangle counting, GAP tc_local (src/*/GAP/src/tc_local.cc:49-125 OrderedCount
+// on the graph relabelled by degree, builder.h:247-282 RelabelByDegree: degree
+// descending, ties by descending id, neighbour lists sorted).  A triangle is
+// counted once, as u > v > w in the relabelled ids; counts[x] is the number
+// of triangles containing x, returned by ORIGINAL id (it does not depend on
+// the labelling).  Needs a cleaned symmetric graph (sorted, no repeats, no
+// self loops), which is what the loaders produce.
+int orc_triangles(int64_t n, const uint32_t* off, const uint32_t* adj, int nthreads, uint64_t* counts,
+                  uint64_t* total_out) {
+  ThreadScope ts(nthreads);
+  std::vector<std::pair<uint32_t, uint32_t>> p(n);
+  for (int64_t v = 0; v < n; v++) p[v] = {off[v + 1] - off[v], (uint32_t)v};
+  std::sort(p.begin(), p.end(), std::greater<std::pair<uint32_t, uint32_t>>());
+  std::vector<uint32_t> ids(n), roff(n + 1), radj(off[n]);
+  for (int64_t r = 0; r < n; r++) ids[p[r].second] = (uint32_t)r;
+  uint64_t acc = 0;
+  for (int64_t r = 0; r < n; r++) { roff[r] = (uint32_t)acc; acc += p[r].first; }
+  roff[n] = (uint32_t)acc;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t v = 0; v < n; v++) {
+    const uint32_t r = ids[v];
+    uint32_t* row = radj.data() + roff[r];
+    for (uint32_t j = off[v]; j < off[v + 1]; j++) row[j - off[v]] = ids[adj[j]];
+    std::sort(row, row + (off[v + 1] - off[v]));
+  }
+  std::vector<uint64_t> tri(n, 0);
+  uint64_t total = 0;
+#pragma omp parallel for reduction(+ : total) schedule(dynamic, 64)
+  for (int64_t u = 0; u < n; u++) {
+    for (uint32_t j = roff[u]; j < roff[u + 1]; j++) {
+      const uint32_t v = radj[j];
+      if (v > u) break;
+      uint32_t it = roff[u];
+      for (uint32_t k = roff[v]; k < roff[v + 1]; k++) {
+        const uint32_t w = radj[k];
+        if (w > v) break;
+        while (radj[it] < w) it++;  // stops at v (< u, in u's list) at the latest
+        if (radj[it] == w) {
+          total++;
+          __atomic_fetch_add(&tri[u], 1, __ATOMIC_RELAXED);
+          __atomic_fetch_add(&tri[v], 1, __ATOMIC_RELAXED);
+          __atomic_fetch_add(&tri[w], 1, __ATOMIC_RELAXED);
+        }
+      }
+    }
+  }
+  for (int64_t v = 0; v < n; v++) counts[v] = tri[ids[v]];
+  if (total_out) *total_out = total;
+  return 0;
+}
+
 // Edges traversed by every edge_map since the last call (then reset).
 int64_t orc_take_edges() { return g_edges.exchange(0); }
 

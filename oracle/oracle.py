@@ -141,6 +141,16 @@ def bc_sources(deg_orig, k):
     return out
 
 
+def triangles(off, adj, threads=0):
+    """GAP tc_local: (per-vertex triangle counts by original id, total)."""
+    off, adj = _u32(off), _u32(adj)
+    n = len(off) - 1
+    c = np.empty(n, np.uint64)
+    tot = C.c_uint64()
+    lib().orc_triangles(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), threads, _p(c, C.c_uint64), C.byref(tot))
+    return c, tot.value
+
+
 def take_edges():
     """Edges the oracle's edgeMap calls traversed since the last call."""
     f = lib().orc_take_edges

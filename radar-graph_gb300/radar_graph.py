@@ -116,6 +116,7 @@ _SIGS = {
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
     "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
+    "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
     "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
@@ -375,6 +376,13 @@ class Graph:
         _check(lib().rg_pagerank(self._h, _variant(variant), max_iters, _ptr(ranks, C.c_double), C.byref(it),
                                  C.byref(l1)))
         return ranks, it.value, l1.value
+
+    def triangles(self):
+        """(per-vertex triangle counts by original id, total)."""
+        counts = np.empty(self.n, np.uint64)
+        total = C.c_uint64()
+        _check(lib().rg_triangle_count(self._h, _ptr(counts, C.c_uint64), C.byref(total)))
+        return counts, total.value
 
     def pagerank_delta(self, variant="push", max_iters=100):
         """PageRankDelta: (ranks, printed round count, final L1)."""

@@ -188,6 +188,20 @@ def make(name, n, src, dst, hub_threads, workdir, out):
             _, _, nid, cap, _ = run("RADAR", "BFS", gpath, ["-r", str(r)], hub_threads, workdir)
             par = np.frombuffer(cap[-1], np.uint32).copy()
             res[f"bfs{ri}_radar"] = to_orig(orc.depths_from_parents(par), nid, True)
+    # triangle count (GAP tc_local, undirected edge list, -s symmetrises)
+    el = os.path.join(workdir, name + ".el")
+    with open(el, "w") as f:
+        for u in range(len(off) - 1):
+            for v in cadj[off[u]:off[u + 1]]:
+                if u < v:
+                    f.write(f"{u} {int(v)}\n")
+    if os.path.getsize(el) > 0:
+        r = subprocess.run([os.path.join(REFBIN, "gap", "tc_local"), "-f", el, "-s", "-n", "1", "-a"],
+                           capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS="8"))
+        if r.returncode != 0:
+            raise RuntimeError(f"tc_local failed:\n{r.stdout}\n{r.stderr}")
+        tri = [ln for ln in r.stdout.splitlines() if ln.strip().endswith(" triangles")]
+        res["tc_total"] = np.array([int(tri[-1].split()[0])], np.int64)
     np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
     print(f"{name}: n={n} m={len(cadj)} keys={len(res)}")
 

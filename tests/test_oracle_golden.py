@@ -146,3 +146,31 @@ def test_radii_seed_hash_matches_python():
     import radar_graph as rg
     for n in (12, 1000, 1 << 20):
         assert np.array_equal(orc.radii_seeds(n), rg.radii_seeds_orig(n))
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_triangles(graphs, name):
+    """GAP tc_local's total (the reference binary) and the per-vertex counts'
+    invariant (tc_local.cc:119-126: they sum to three times the total)."""
+    G = graphs[name]
+    counts, total = orc.triangles(G["off"], G["adj"], 4)
+    assert total == int(G["g"]["tc_total"][0])
+    assert int(counts.sum()) == 3 * total
+
+
+def test_triangles_brute_force():
+    import radar_graph as rg
+    off, adj = rg.rmat_csr(9, 8, seed=5)
+    counts, total = orc.triangles(off, adj, 2)
+    n = len(off) - 1
+    nb = [set(adj[off[v]:off[v + 1]].tolist()) for v in range(n)]
+    want = np.zeros(n, np.uint64)
+    t = 0
+    for u in range(n):
+        for v in nb[u]:
+            if v > u:
+                for w in nb[u] & nb[v]:
+                    if w > v:
+                        t += 1
+                        want[[u, v, w]] += 1
+    assert total == t and np.array_equal(counts, want)
