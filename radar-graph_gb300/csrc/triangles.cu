@@ -5,7 +5,8 @@
 // order of builder.h:247-282 and of the degree sort) with every neighbour
 // list sorted ascending; a triangle is then counted once, as u > v > w: for
 // every edge (u, v) with v < u, the common neighbours w < v of u and v are
-// found by merging u's list before v with v's list before v.  In this order
+// found by merging u's list before v with v's list below v (or, when one is
+// far longer, by searching the short one's elements in it).  In this order
 // both lists hold only higher-degree neighbours, so they stay short even on
 // skewed graphs.  Per-vertex counts (triangles containing each vertex) are
 // returned by original id; the counts of the H highest-degree vertices
@@ -78,22 +79,50 @@ __global__ void __launch_bounds__(256) count_triangles(DevGraph g, const uint32_
       const uint32_t u = upper_index(g.off, vlo, vhi, e);
       const uint32_t v = g.adj[e];
       if (v >= u) continue;  // each triangle once: u > v > w
-      // u's neighbours before v (all < v) against v's neighbours below v
-      uint32_t ia = g.off[u], ib = g.off[v];
-      const uint32_t ea = e, eb = g.off[v] + lower[v];
+      // u's neighbours before v (all < v) against v's neighbours below v:
+      // merged, unless one list is far longer -- then each element of the
+      // short one is searched in the long one (min * log(max) steps)
+      uint32_t sa = g.off[u], ea = e, sb = g.off[v], eb = g.off[v] + lower[v];
+      if (ea - sa > eb - sb) {
+        const uint32_t t0 = sa, t1 = ea;
+        sa = sb;
+        ea = eb;
+        sb = t0;
+        eb = t1;
+      }
       uint32_t cnt = 0;
-      while (ia < ea && ib < eb) {
-        const uint32_t x = g.adj[ia], y = g.adj[ib];
-        if (x == y) {
-          cnt++;
-          if (kHub && x < H) atomicAdd(hs + x, 1ull);
-          else atomicAdd(tri + x, 1ull);
-          ia++;
-          ib++;
-        } else if (x < y) {
-          ia++;
-        } else {
-          ib++;
+      if (eb - sb > 16 * (ea - sa)) {
+        uint32_t lo = sb;  // the short list ascends: each search starts past the last one
+        for (uint32_t i = sa; i < ea && lo < eb; i++) {
+          const uint32_t x = g.adj[i];
+          uint32_t hi = eb;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (g.adj[mid] < x) lo = mid + 1;
+            else hi = mid;
+          }
+          if (lo < eb && g.adj[lo] == x) {
+            cnt++;
+            if (kHub && x < H) atomicAdd(hs + x, 1ull);
+            else atomicAdd(tri + x, 1ull);
+            lo++;
+          }
+        }
+      } else {
+        uint32_t ia = sa, ib = sb;
+        while (ia < ea && ib < eb) {
+          const uint32_t x = g.adj[ia], y = g.adj[ib];
+          if (x == y) {
+            cnt++;
+            if (kHub && x < H) atomicAdd(hs + x, 1ull);
+            else atomicAdd(tri + x, 1ull);
+            ia++;
+            ib++;
+          } else if (x < y) {
+            ia++;
+          } else {
+            ib++;
+          }
         }
       }
       if (cnt) {
