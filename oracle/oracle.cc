@@ -41,12 +41,29 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;  // UINT_E_MAX in Ligra (parallel.h:113-
 
 enum Variant { kPush = 0, kPushPull = 1, kDegSort = 2, kHubDup = 3, kRadar = 4 };
 
+// Out-edges (off/adj) and in-edges (in_off/in_adj; the same arrays for a
+// symmetric graph).  Pushes follow out-edges, pulls read in-edges, and a
+// transpose swaps the two (graph.h:78-86).
 struct Csr {
   int64_t n, m;
   const uint32_t* off;  // n+1
   const uint32_t* adj;  // m
+  const uint32_t* in_off = nullptr;
+  const uint32_t* in_adj = nullptr;
   uint32_t deg(int64_t v) const { return off[v + 1] - off[v]; }
+  Csr transposed() const { return Csr{n, m, in_off, in_adj, off, adj}; }
 };
+
+// In-edges for the next app calls on a directed graph (null: symmetric).
+const uint32_t* g_in_off = nullptr;
+const uint32_t* g_in_adj = nullptr;
+
+Csr make_csr(int64_t n, const uint32_t* off, const uint32_t* adj) {
+  Csr g{n, (int64_t)off[n], off, adj};
+  g.in_off = g_in_off ? g_in_off : off;
+  g.in_adj = g_in_off ? g_in_adj : adj;
+  return g;
+}
 
 // ---------------------------------------------------------------------------
 // Atomics.  The reference uses __sync CAS (utils.h:311-324) and a CAS loop for
@@ -216,12 +233,12 @@ Frontier edge_map(const Csr& g, Frontier& fr, F& f, int64_t threshold, bool outp
         }
       }
       f.merge();
-    } else {  // edgeMapDense (pull); symmetric graphs: in-edges == out-edges
+    } else {  // edgeMapDense (pull) over in-edges
 #pragma omp parallel for schedule(dynamic, 64)
       for (int64_t v = 0; v < n; v++) {
         if (!f.cond((uint32_t)v)) continue;
-        for (uint32_t j = g.off[v]; j < g.off[v + 1]; j++) {
-          uint32_t u = g.adj[j];
+        for (uint32_t j = g.in_off[v]; j < g.in_off[v + 1]; j++) {
+          uint32_t u = g.in_adj[j];
           if (fr.in(u)) f.update(u, (uint32_t)v);
           if (!f.cond((uint32_t)v)) break;
         }
@@ -576,7 +593,7 @@ int orc_pagerank(int64_t n, const uint32_t* off, const uint32_t* adj, int varian
                  int64_t max_iters, int nthreads, double* ranks, int64_t* iters_out,
                  double* l1_out) {
   ThreadScope ts(nthreads);
-  Csr g{n, (int64_t)off[n], off, adj};
+  Csr g = make_csr(n, off, adj);
   const double damping = 0.85, eps = 0.0000001;
   std::vector<double> a(n, 1.0 / (double)n), b(n, 0.0);
   double* p_curr = a.data();
@@ -619,7 +636,7 @@ int orc_pagerank_delta(int64_t n, const uint32_t* off, const uint32_t* adj, int 
                        int64_t max_iters, int nthreads, double* ranks, int64_t* iters_out,
                        double* l1_out) {
   ThreadScope ts(nthreads);
-  Csr g{n, (int64_t)off[n], off, adj};
+  Csr g = make_csr(n, off, adj);
   const double damping = 0.85, eps = 0.0000001, eps2 = 0.01;
   const double one_over_n = 1 / (double)n;
   const double added = (1 - damping) * one_over_n;
@@ -670,7 +687,7 @@ int orc_pagerank_delta(int64_t n, const uint32_t* off, const uint32_t* adj, int 
 int orc_bfs(int64_t n, const uint32_t* off, const uint32_t* adj, int variant, uint32_t root,
             int nthreads, uint32_t* parents, int64_t* rounds_out) {
   ThreadScope ts(nthreads);
-  Csr g{n, (int64_t)off[n], off, adj};
+  Csr g = make_csr(n, off, adj);
   for (int64_t i = 0; i < n; i++) parents[i] = kNone;
   parents[root] = root;
   int T = omp_get_max_threads();
@@ -700,9 +717,9 @@ int orc_bfs(int64_t n, const uint32_t* off, const uint32_t* adj, int variant, ui
 int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
            const uint32_t* sources, int nsrc, int nthreads, double* deps, int64_t* levels_out) {
   ThreadScope ts(nthreads);
-  Csr g{n, (int64_t)off[n], off, adj};
+  const Csr g0 = make_csr(n, off, adj);
   int T = omp_get_max_threads();
-  Hubs hubs = make_hubs(g, variant, T, sizeof(double), 1 + (variant == kHubDup ? 5 : 0));
+  Hubs hubs = make_hubs(g0, variant, T, sizeof(double), 1 + (variant == kHubDup ? 5 : 0));
   std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
   std::vector<uint8_t> do_merge(hubs.count, 0);
   std::vector<double> num_paths(n);
@@ -710,6 +727,12 @@ int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
   for (int64_t i = 0; i < n; i++) deps[i] = 0.0;
   int64_t total_levels = 0;
   for (int it = 0; it < nsrc; it++) {
+    // the reference transposes the graph before every backward phase and
+    // never back (BC-manyiter-v2.C:334): source it's forward phase runs on
+    // the graph transposed `it` times (a no-op for symmetric graphs)
+    const Csr gf = (it % 2) ? g0.transposed() : g0;
+    const Csr& g = gf;
+    const Csr gb = gf.transposed();
     uint32_t start = sources[it];
     std::fill(num_paths.begin(), num_paths.end(), 0.0);
     num_paths[start] = 1.0;
@@ -737,7 +760,7 @@ int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
     cur.for_each(back_vertex);
     for (int64_t r = round - 2; r >= 0; r--) {
       BcBackF f{deps, visited.data(), nullptr, &hubs, &dup, &do_merge};
-      edge_map(g, cur, f, -1, false, variant != kPushPull);
+      edge_map(gb, cur, f, -1, false, variant != kPushPull);
       cur = levels[r];
       cur.for_each(back_vertex);
     }
@@ -756,7 +779,7 @@ int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
               const uint32_t* seeds, int nseeds, int nthreads, int32_t* radii,
               int64_t* rounds_out) {
   ThreadScope ts(nthreads);
-  Csr g{n, (int64_t)off[n], off, adj};
+  Csr g = make_csr(n, off, adj);
   std::vector<int64_t> visited(n, 0), next_visited(n, 0);
   for (int64_t i = 0; i < n; i++) radii[i] = -1;
   std::vector<uint32_t> starts(nseeds);
@@ -835,6 +858,33 @@ int orc_triangles(int64_t n, const uint32_t* off, const uint32_t* adj, int nthre
   return 0;
 }
 
+// In-edges (in_off n+1, in_adj m) for the following calls on a directed
+// graph; null pointers return to symmetric graphs.
+void orc_set_in_edges(const uint32_t* in_off, const uint32_t* in_adj) {
+  g_in_off = in_off;
+  g_in_adj = in_adj;
+}
+
+// Directed clean-up of the text loader (IO.h:287-474 without symmetry):
+// every out-list sorted, repeats and self loops dropped.  `off` has n
+// entries (start offsets).  Returns the new edge count; out_off has n+1.
+int64_t orc_dedup_directed(int64_t n, int64_t m, const uint32_t* off, const uint32_t* adj, uint32_t* out_off,
+                           uint32_t* out_adj) {
+  return orc_dedup_symmetric(n, m, off, adj, out_off, out_adj);  // the per-list rule is the same
+}
+
+// In-edges of a CSR (the reference's CSC, IO.h:287-345): in_adj lists the
+// sources of each vertex in increasing order.
+void orc_transpose(int64_t n, const uint32_t* off, const uint32_t* adj, uint32_t* in_off, uint32_t* in_adj) {
+  const int64_t m = off[n];
+  std::vector<uint32_t> cnt(n + 1, 0);
+  for (int64_t j = 0; j < m; j++) cnt[adj[j] + 1]++;
+  for (int64_t v = 0; v < n; v++) cnt[v + 1] += cnt[v];
+  for (int64_t v = 0; v <= n; v++) in_off[v] = cnt[v];
+  for (int64_t s = 0; s < n; s++)
+    for (uint32_t j = off[s]; j < off[s + 1]; j++) in_adj[cnt[adj[j]]++] = (uint32_t)s;
+}
+
 // Edges traversed by every edge_map since the last call (then reset).
 int64_t orc_take_edges() { return g_edges.exchange(0); }
 
@@ -853,6 +903,22 @@ void orc_bc_sources(int64_t n, const uint32_t* deg_orig, int k, uint32_t* out_or
 }
 
 // Radii seeds (Radii.C:159-169): vertex hashInt((ulong)i) % n for i < min(n,64).
+// The same draws on a directed graph: the reference checks the out-degree of
+// the graph as it stands, and its BC transposes the graph once per source
+// (BC-manyiter-v2.C:264-270, :334), so draw i rejects on out-degree for even
+// i and in-degree for odd i.
+void orc_bc_sources_directed(int64_t n, const uint32_t* outdeg_orig, const uint32_t* indeg_orig, int k,
+                             uint32_t* out_orig) {
+  std::mt19937 rng(27491095);
+  std::uniform_int_distribution<long> ud(0, n - 1);
+  for (int i = 0; i < k; i++) {
+    const uint32_t* deg = (i % 2) ? indeg_orig : outdeg_orig;
+    long s;
+    do { s = ud(rng); } while (deg[s] == 0);
+    out_orig[i] = (uint32_t)s;
+  }
+}
+
 int orc_radii_seeds(int64_t n, uint32_t* out_orig) {
   int k = (int)std::min<int64_t>(n, 64);
   for (int i = 0; i < k; i++) out_orig[i] = (uint32_t)(hash_u64((uint64_t)i) % (uint64_t)n);

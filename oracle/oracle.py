@@ -83,54 +83,95 @@ def degree_sort(off, adj):
     return ids, no, na[:len(adj)].copy()
 
 
-def pagerank(off, adj, variant="push", max_iters=20, threads=0):
+class _InEdges:
+    """In-edges of a directed graph for the calls inside the block."""
+
+    def __init__(self, in_off, in_adj):
+        self.arrays = (_u32(in_off), _u32(in_adj)) if in_off is not None else None
+
+    def __enter__(self):
+        if self.arrays:
+            lib().orc_set_in_edges(_p(self.arrays[0], C.c_uint32), _p(self.arrays[1], C.c_uint32))
+
+    def __exit__(self, *a):
+        lib().orc_set_in_edges(None, None)
+
+
+def transpose(off, adj):
+    """In-edges (in_off, in_adj) of a CSR, sources ascending per vertex."""
+    off, adj = _u32(off), _u32(adj)
+    n = len(off) - 1
+    io, ia = np.empty(n + 1, np.uint32), np.empty(len(adj), np.uint32)
+    lib().orc_transpose(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), _p(io, C.c_uint32), _p(ia, C.c_uint32))
+    return io, ia
+
+
+def dedup_directed(n, off_n, adj):
+    """Directed clean-up of the text loader: sorted out-lists, no repeats or
+    self loops (off_n: n start offsets)."""
+    return dedup_symmetric(n, off_n, adj)
+
+
+def bc_sources_directed(outdeg, indeg, k):
+    outdeg, indeg = _u32(outdeg), _u32(indeg)
+    out = np.empty(k, np.uint32)
+    lib().orc_bc_sources_directed(len(outdeg), _p(outdeg, C.c_uint32), _p(indeg, C.c_uint32), k, _p(out, C.c_uint32))
+    return out
+
+
+def pagerank(off, adj, variant="push", max_iters=20, threads=0, in_off=None, in_adj=None):
     off, adj = _u32(off), _u32(adj)
     n = len(off) - 1
     r = np.empty(n, np.float64)
     it, l1 = C.c_int64(), C.c_double()
-    lib().orc_pagerank(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], max_iters, threads,
-                       _p(r, C.c_double), C.byref(it), C.byref(l1))
+    with _InEdges(in_off, in_adj):
+        lib().orc_pagerank(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], max_iters, threads,
+                           _p(r, C.c_double), C.byref(it), C.byref(l1))
     return r, it.value, l1.value
 
 
-def pagerank_delta(off, adj, variant="push", max_iters=20, threads=0):
+def pagerank_delta(off, adj, variant="push", max_iters=20, threads=0, in_off=None, in_adj=None):
     """PageRankDelta (PageRankDelta.C): (ranks, printed round count, L1)."""
     off, adj = _u32(off), _u32(adj)
     n = len(off) - 1
     r = np.empty(n, np.float64)
     it, l1 = C.c_int64(), C.c_double()
-    lib().orc_pagerank_delta(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], max_iters, threads,
-                             _p(r, C.c_double), C.byref(it), C.byref(l1))
+    with _InEdges(in_off, in_adj):
+        lib().orc_pagerank_delta(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], max_iters, threads,
+                                 _p(r, C.c_double), C.byref(it), C.byref(l1))
     return r, it.value, l1.value
 
 
-def bfs(off, adj, root, variant="push", threads=0):
+def bfs(off, adj, root, variant="push", threads=0, in_off=None, in_adj=None):
     off, adj = _u32(off), _u32(adj)
     n = len(off) - 1
     par = np.empty(n, np.uint32)
     rounds = C.c_int64()
-    lib().orc_bfs(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], root, threads,
-                  _p(par, C.c_uint32), C.byref(rounds))
+    with _InEdges(in_off, in_adj):
+        lib().orc_bfs(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], root, threads,
+                      _p(par, C.c_uint32), C.byref(rounds))
     return par, rounds.value
 
 
-def bc(off, adj, sources, variant="push", threads=0):
+def bc(off, adj, sources, variant="push", threads=0, in_off=None, in_adj=None):
     off, adj, s = _u32(off), _u32(adj), _u32(sources)
     n = len(off) - 1
     d = np.empty(n, np.float64)
     lv = C.c_int64()
-    lib().orc_bc(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], _p(s, C.c_uint32), len(s),
-                 threads, _p(d, C.c_double), C.byref(lv))
+    with _InEdges(in_off, in_adj):
+        lib().orc_bc(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], _p(s, C.c_uint32), len(s),
+                     threads, _p(d, C.c_double), C.byref(lv))
     return d, lv.value
 
 
-def radii(off, adj, seeds, variant="push", threads=0):
+def radii(off, adj, seeds, variant="push", threads=0, in_off=None, in_adj=None):
     off, adj, s = _u32(off), _u32(adj), _u32(seeds)
     n = len(off) - 1
     r = np.empty(n, np.int32)
     rounds = C.c_int64()
-    lib().orc_radii(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], _p(s, C.c_uint32), len(s),
-                    threads, _p(r, C.c_int32), C.byref(rounds))
+    with _InEdges(in_off, in_adj):
+        lib().orc_radii(n, _p(off, C.c_uint32), _p(adj, C.c_uint32), VARIANTS[variant], _p(s, C.c_uint32), len(s),
+                        threads, _p(r, C.c_int32), C.byref(rounds))
     return r, rounds.value
 
 
@@ -200,3 +241,27 @@ def check_bfs_tree(off, adj, root, parents, depth):
         if p not in nb:
             return False
     return True
+
+
+def degree_sort_directed(off, adj, in_off, in_adj, by_in=True):
+    """Directed preprocessGraph (IO.h:739-842): rank by in-degree (-preprocess
+    1) or out-degree (0), descending, ties by descending id; out- and in-lists
+    relabelled, their order kept.  Returns (new_ids, off, adj, in_off, in_adj)."""
+    off, adj, in_off, in_adj = (np.asarray(a, np.int64) for a in (off, adj, in_off, in_adj))
+    n = len(off) - 1
+    outdeg, indeg = np.diff(off), np.diff(in_off)
+    key = (indeg if by_in else outdeg) * n + np.arange(n)
+    order = np.argsort(-key, kind="stable")
+    new_ids = np.empty(n, np.int64)
+    new_ids[order] = np.arange(n)
+
+    def relabel(o, a, deg):
+        no = np.zeros(n + 1, np.int64)
+        no[1:] = np.cumsum(deg[order])
+        starts = o[order]
+        idx = np.repeat(starts - no[:-1], deg[order]) + np.arange(no[-1])
+        return no.astype(np.uint32), new_ids[a[idx]].astype(np.uint32)
+
+    so, sa = relabel(off, adj, outdeg)
+    sio, sia = relabel(in_off, in_adj, indeg)
+    return new_ids.astype(np.uint32), so, sa, sio, sia

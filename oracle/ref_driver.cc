@@ -19,9 +19,10 @@
 //    the final results.  Every per-vertex output dump in the apps is
 //    commented out (PageRank.C:178 ...), which is why this is needed.
 //
-// Usage: <bin> -s [-preprocess p] [-maxiters k] [-r root] -dump <out> <graph>
+// Usage: <bin> [-s] [-preprocess p] [-maxiters k] [-r root] -dump <out> <graph>
 // Output file: repeated records {u64 nbytes; bytes}: the loaded graph's CSR
-// offsets (n+1 x u32) and neighbours (m x u32), the new_ids permutation
+// offsets (n+1 x u32) and neighbours (m x u32) -- followed, for a directed
+// graph (no -s), by the in-lists in the same form -- the new_ids permutation
 // (n x u32), then every captured block in free() order.
 
 #include <cmath>
@@ -68,34 +69,30 @@ static void put(FILE* f, const void* p, uint64_t nbytes) {
   if (nbytes) fwrite(p, 1, nbytes, f);
 }
 
-int main(int argc, char* argv[]) {
-  commandLine P(argc, argv, " [-s] -dump <out> <inFile>");
-  char* iFile = P.getArgument(0);
-  bool symmetric = P.getOptionValue("-s");
-  bool binary = P.getOptionValue("-b");
-  char* dump = P.getOptionValue("-dump");
-  int preprocess = P.getOptionIntValue("-preprocess", -1);
-  if (!symmetric || dump == nullptr) {
-    fprintf(stderr, "ref_driver: needs -s and -dump\n");
-    return 2;
-  }
-  graph<symmetricVertex> G = readGraph<symmetricVertex>(iFile, false, symmetric, binary, false);
+// Loads, optionally degree-sorts, runs Compute once and dumps (templated on
+// the reference's vertex type: symmetricVertex, or asymmetricVertex for a
+// directed graph, whose in-lists are dumped after the out-lists).
+template <class vertex>
+int run(commandLine& P, char* iFile, bool symmetric, bool binary, int preprocess, const char* dump) {
+  graph<vertex> G = readGraph<vertex>(iFile, false, symmetric, binary, false);
   pvector<uintE> new_ids(G.n, 0);
   FILE* f = fopen(dump, "wb");
-  {  // the loaded (cleaned) graph as CSR: offsets (n+1) then neighbours (m)
-    std::vector<uint32_t> off(G.n + 1), adj;
-    adj.reserve(G.m);
-    for (long v = 0; v < G.n; v++) {
-      off[v] = (uint32_t)adj.size();
-      for (uintT j = 0; j < G.V[v].getOutDegree(); j++) adj.push_back(G.V[v].getOutNeighbor(j));
+  {  // the loaded (cleaned) graph: out-lists as CSR, then (directed) in-lists
+    for (int in = 0; in < (symmetric ? 1 : 2); in++) {
+      std::vector<uint32_t> off(G.n + 1), adj;
+      adj.reserve(G.m);
+      for (long v = 0; v < G.n; v++) {
+        off[v] = (uint32_t)adj.size();
+        const uintT d = in ? G.V[v].getInDegree() : G.V[v].getOutDegree();
+        for (uintT j = 0; j < d; j++) adj.push_back(in ? G.V[v].getInNeighbor(j) : G.V[v].getOutNeighbor(j));
+      }
+      off[G.n] = (uint32_t)adj.size();
+      put(f, off.data(), 4ull * off.size());
+      put(f, adj.data(), 4ull * adj.size());
     }
-    off[G.n] = (uint32_t)adj.size();
-    put(f, off.data(), 4ull * off.size());
-    put(f, adj.data(), 4ull * adj.size());
   }
   if (preprocess == 0 || preprocess == 1) {
-    graph<symmetricVertex> newG =
-        preprocessGraph<symmetricVertex>(G, symmetric, (preprocess == 0), new_ids);
+    graph<vertex> newG = preprocessGraph<vertex>(G, symmetric, (preprocess == 0), new_ids);
     G.del();
     put(f, new_ids.data(), 4ull * newG.n);
     Compute(newG, P, new_ids);
@@ -108,4 +105,19 @@ int main(int argc, char* argv[]) {
   for (auto& b : rgref::g_captured) put(f, b.data(), b.size());
   fclose(f);
   return 0;
+}
+
+int main(int argc, char* argv[]) {
+  commandLine P(argc, argv, " [-s] -dump <out> <inFile>");
+  char* iFile = P.getArgument(0);
+  bool symmetric = P.getOptionValue("-s");
+  bool binary = P.getOptionValue("-b");
+  char* dump = P.getOptionValue("-dump");
+  int preprocess = P.getOptionIntValue("-preprocess", -1);
+  if (dump == nullptr) {
+    fprintf(stderr, "ref_driver: needs -dump\n");
+    return 2;
+  }
+  if (symmetric) return run<symmetricVertex>(P, iFile, true, binary, preprocess, dump);
+  return run<asymmetricVertex>(P, iFile, false, binary, preprocess, dump);
 }

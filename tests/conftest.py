@@ -9,7 +9,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "radar-graph_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-GOLDEN_NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+ALL_GOLDEN = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# directed graphs carry their in-lists; the rest are symmetric
+DIRECTED_NAMES = [n for n in ALL_GOLDEN if "in_off" in np.load(os.path.join(GOLDEN, n + ".npz")).files]
+GOLDEN_NAMES = [n for n in ALL_GOLDEN if n not in DIRECTED_NAMES]
 
 # Tolerance for double results (PageRank ranks, BC dependencies): relative
 # 1e-9, the bar the reference comparison is held to.  Integer results (BFS
@@ -24,6 +27,11 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def golden():
     return {n: dict(np.load(os.path.join(GOLDEN, n + ".npz"))) for n in GOLDEN_NAMES}
+
+
+@pytest.fixture(scope="session")
+def golden_directed():
+    return {n: dict(np.load(os.path.join(GOLDEN, n + ".npz"))) for n in DIRECTED_NAMES}
 
 
 def assert_close(a, b, rtol=RTOL, what=""):

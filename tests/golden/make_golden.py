@@ -206,6 +206,86 @@ def make(name, n, src, dst, hub_threads, workdir, out):
     print(f"{name}: n={n} m={len(cadj)} keys={len(res)}")
 
 
+# directed graphs: name -> (scale, edge_factor, seed, uniform, hub_threads)
+DIRECTED = {
+    "drmat10": (10, 8, 11, False, None),
+    "der10": (10, 8, 12, True, None),
+    "drmat13": (13, 8, 13, False, 1024),
+}
+
+
+def run_directed(variant, app, gpath, args, threads, workdir):
+    """Like run() without -s: the dump holds out-lists, in-lists, new_ids."""
+    exe = os.path.join(REFBIN, variant, app + ".dump")
+    out = os.path.join(workdir, f"d_{variant}_{app}.bin")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    pre = ["-preprocess", "1"] if variant in ("degree-sorting", "RADAR") else []
+    cmd = [exe] + pre + args + ["-dump", out, gpath]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, cwd=workdir)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd} failed:\n{r.stdout}\n{r.stderr}")
+    recs = read_dump(out)
+    arrs = [np.frombuffer(recs[i], np.uint32).copy() for i in range(5)]
+    return arrs, recs[5:], r.stdout
+
+
+def make_directed(name, n, src, dst, hub_threads, workdir, out):
+    """Directed golden vectors: the raw out-lists (src -> dst, with repeats
+    and self loops) as a Ligra file, the reference apps run without -s."""
+    order = np.argsort(src, kind="stable")
+    s, d = src[order].astype(np.int64), dst[order].astype(np.uint32)
+    off_n = np.searchsorted(s, np.arange(n), side="left").astype(np.uint32)
+    gpath = os.path.join(workdir, name + ".adj")
+    write_text(gpath, off_n, d)
+    res = {"raw_off": off_n, "raw_adj": d}
+    T = 8
+    (off, adj, in_off, in_adj, _), cap, _ = run_directed("push-new-orig", "PageRank", gpath, ["-maxiters", "20"], T,
+                                                         workdir)
+    res.update(off=off, adj=adj, in_off=in_off, in_adj=in_adj)
+    outdeg = np.diff(off.astype(np.int64))
+    nz = np.nonzero(outdeg)[0]
+    roots = [int(nz[0]), int(nz[len(nz) // 2])]
+    res["bfs_roots"] = np.array(roots, np.uint32)
+
+    def pr_of(cap):
+        a, b = (np.frombuffer(c, np.float64) for c in cap[:2])
+        return a.copy() if not np.any(b) else b.copy()
+
+    def prd_of(cap):
+        blocks = [c for c in cap if len(c) == 8 * n]
+        return np.frombuffer(blocks[-3], np.float64).copy()
+
+    res["pr_push"] = pr_of(cap)
+    variants = (("push", "push-new-orig", False), ("push-pull", "push-pull", False),
+                ("degree-sorting", "degree-sorting", True))
+    for variant, vdir, pre in variants:
+        if variant != "push":
+            (_, _, _, _, nid), cap, _ = run_directed(vdir, "PageRank", gpath, ["-maxiters", "20"], T, workdir)
+            res[f"pr_{variant}"] = to_orig(pr_of(cap), nid, pre)
+            if pre:
+                res["new_ids"] = nid  # in-degree order (-preprocess 1)
+        (_, _, _, _, nid), cap, so = run_directed(vdir, "PageRankDelta", gpath, ["-maxiters", "20"], T, workdir)
+        res[f"prd_{variant}"] = to_orig(prd_of(cap), nid, pre)
+        res[f"prd_iters_{variant}"] = np.array([int(so.split("Num Iters = ")[1].split()[0])], np.int64)
+        for ri, r in enumerate(roots):
+            (_, _, _, _, nid), cap, _ = run_directed(vdir, "BFS", gpath, ["-r", str(r)], T, workdir)
+            par = np.frombuffer(cap[-1], np.uint32).copy()
+            res[f"bfs{ri}_{variant}"] = to_orig(orc.depths_from_parents(par), nid, pre)
+        for k in (1, 2, 3):
+            (_, _, _, _, nid), cap, _ = run_directed(vdir, "BC-manyiter-v2", gpath, ["-maxiters", str(k)], T,
+                                                     workdir)
+            res[f"bc{k}_{variant}"] = to_orig(np.frombuffer(cap[2], np.float64).copy(), nid, pre)
+        (_, _, _, _, nid), cap, _ = run_directed(vdir, "Radii", gpath, [], 1, workdir)
+        res[f"radii_{variant}"] = to_orig(np.frombuffer(cap[2], np.int32).copy(), nid, pre)
+    if hub_threads:
+        for variant, vdir, pre in (("hubdup", "hubdup", False), ("radar", "RADAR", True)):
+            (_, _, _, _, nid), cap, _ = run_directed(vdir, "PageRank", gpath, ["-maxiters", "20"], hub_threads,
+                                                     workdir)
+            res[f"pr_{variant}"] = to_orig(pr_of(cap), nid, pre)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **res)
+    print(f"{name}: n={n} m={len(adj)} keys={len(res)} (directed)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=HERE)
@@ -218,6 +298,9 @@ def main():
         for name, (scale, ef, seed, uni, ht) in GRAPHS.items():
             s, d = rg.generate_edges(scale, ef, seed, uni)
             make(name, 1 << scale, s, d, ht, wd, a.out)
+        for name, (scale, ef, seed, uni, ht) in DIRECTED.items():
+            s, d = rg.generate_edges(scale, ef, seed, uni)
+            make_directed(name, 1 << scale, s, d, ht, wd, a.out)
 
 
 if __name__ == "__main__":
