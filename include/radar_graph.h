@@ -121,6 +121,14 @@ rg_status rg_graph_create(int64_t n, int64_t m, const uint32_t* h_off, const uin
  * sorts instead of on the host. */
 rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_t* src,
                                      const uint32_t* dst, int on_device, rg_graph** out);
+/* A DIRECTED graph from its cleaned out-lists (h_off: n+1, h_adj: m, e.g.
+ * from rg_read_graph with symmetric = 0); the in-lists (the reference's CSC,
+ * IO.h:287-345) are built on the device.  Pushes follow out-edges, pulls read
+ * in-edges, and BC transposes per source as BC-manyiter-v2.C:334 does.
+ * Triangle counting and serving take undirected graphs only. */
+rg_status rg_graph_create_directed(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                                   rg_graph** out);
+rg_status rg_graph_is_directed(const rg_graph* g, int* directed);
 /* Uploads from arrays already on the device (copied; caller keeps ownership). */
 rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
                                  const uint32_t* d_adj, rg_graph** out);
@@ -128,6 +136,10 @@ rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
  * (degree desc, id desc), relabel every neighbour list (order kept).  The new
  * graph remembers new_ids; h_new_ids (n entries, may be NULL) receives it. */
 rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids);
+/* The same with the key chosen: out-degree (by_out_degree = 1, -preprocess 0)
+ * or, for a directed graph, in-degree (0, -preprocess 1, what
+ * rg_graph_degree_sort does; IO.h:739-750). */
+rg_status rg_graph_degree_sort_by(const rg_graph* g, int by_out_degree, rg_graph** out, uint32_t* h_new_ids);
 rg_status rg_graph_info(const rg_graph* g, int64_t* n, int64_t* m, int* degree_sorted);
 /* Copies the device CSR back (h_off: n+1, h_adj: m) -- for checking. */
 rg_status rg_graph_download(const rg_graph* g, uint32_t* h_off, uint32_t* h_adj,

@@ -7,7 +7,8 @@
 //         [-variant push|push-pull|degree-sorting|hubdup|radar] [-out file] <graph>
 //
 // The graph file is read (Ligra AdjacencyGraph text, or the binary
-// .config/.adj/.idx triple with -b), uploaded to the GPU and, when -preprocess
+// .config/.adj/.idx triple with -b; symmetric with -s, else directed),
+// uploaded to the GPU and, when -preprocess
 // is 0 or 1 (the default of the degree-sorting and RADAR variants), degree
 // sorted on the device.  Compute(G, P) then runs 1 + rounds times, each timed,
 // as parallel_main does.  Results go through the C ABI in
@@ -131,24 +132,25 @@ inline int run(int argc, char** argv, ComputeFn compute) {
   }
   Graph G;
   G.variant = parse_variant(P.getOptionValue("-variant", "radar"));
-  if (!P.getOption("-s")) {
-    fprintf(stderr, "only symmetric graphs (-s) are supported\n");
-    return 2;
-  }
+  const bool symmetric = P.getOption("-s");  // without -s the graph is directed
   const long rounds = P.getOptionLongValue("-rounds", 3);
   // degree-sorting and RADAR sort by default (-preprocess 1); the others do not
   const bool sorts_by_default = G.variant == RG_DEGSORT || G.variant == RG_RADAR;
   const long pre = P.getOptionLongValue("-preprocess", sorts_by_default ? 1 : -1);
   uint32_t *off = nullptr, *adj = nullptr;
-  if (rg_read_graph(file, 1, P.getOption("-b") ? 1 : 0, &G.n, &G.m, &off, &adj) != RG_OK) die("read");
+  if (rg_read_graph(file, symmetric ? 1 : 0, P.getOption("-b") ? 1 : 0, &G.n, &G.m, &off, &adj) != RG_OK) {
+    die("read");
+  }
   rg_graph* g0 = nullptr;
-  if (rg_graph_create(G.n, G.m, off, adj, &g0) != RG_OK) die("upload");
+  const rg_status up = symmetric ? rg_graph_create(G.n, G.m, off, adj, &g0)
+                                 : rg_graph_create_directed(G.n, G.m, off, adj, &g0);
+  if (up != RG_OK) die("upload");
   rg_host_free(off);
   rg_host_free(adj);
-  if (pre == 0 || pre == 1) {  // symmetric: in- and out-degree coincide
+  if (pre == 0 || pre == 1) {  // 0: out-degree, 1: in-degree (the same when symmetric)
     Timer t;
     t.start();
-    if (rg_graph_degree_sort(g0, &G.g, nullptr) != RG_OK) die("degree sort");
+    if (rg_graph_degree_sort_by(g0, pre == 0 ? 1 : 0, &G.g, nullptr) != RG_OK) die("degree sort");
     rg_synchronize();
     printf("DegSort Time : %.6f\n", t.stop());
     rg_graph_free(g0);

@@ -110,6 +110,10 @@ struct EmOpts {
   bool dense_forward = true;
   int64_t threshold = -1;
   uint32_t hub_h = 0;  // 0 = budget
+  // run on the transposed graph (graph.h:78-86): pushes follow in-lists,
+  // pulls read out-lists, the next frontier's degrees are in-degrees (a
+  // no-op for symmetric graphs)
+  bool transpose = false;
 };
 
 // Frontiers below this many edges skip hub privatisation: the shared-memory
@@ -118,8 +122,8 @@ struct EmOpts {
 constexpr int64_t kHubMinEdges = 1 << 16;
 
 template <class Op, int kHub>
-rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo& hub, uint32_t* next_bits,
-                             cudaStream_t st) {
+rg_status launch_push(rg_graph* g, const DevGraph& pg, const FView& in, const Op& op, const HubInfo& hub,
+                      uint32_t* next_bits, cudaStream_t st) {
   constexpr int kT = kHub == kHubNone ? kPushThreads : kHubPushThreads;
   constexpr int kTile = kT * kPushItems;
   auto kern = push_lbs<Op, kHub, kT>;
@@ -150,7 +154,7 @@ rg_status launch_push(rg_graph* g, const FView& in, const Op& op, const HubInfo&
                                                                     ws.tiles.as<uint32_t>());
   g_timing.kernel_launches++;
   kt_begin(st);
-  kern<<<grid, kT, dyn, st>>>(g->view(), in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
+  kern<<<grid, kT, dyn, st>>>(pg, in.queue, in.qoff, ws.tiles.as<uint32_t>(), (uint32_t)in.degsum, op, hub,
                               next_bits);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
@@ -171,7 +175,7 @@ static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long*
   }
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);
-  mask_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+  mask_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(),
                                                                          (uint32_t)g->nchunks, visited, next, next_bits);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
@@ -195,11 +199,14 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
     // direction 1 pulls dense levels whatever the variant (no atomics; BFS's
     // pull also exits at the first frontier neighbour)
     const bool pull = dense && (!o.dense_forward || g_opts.direction == 1);
+    const bool tr = o.transpose && g->directed;
+    const DevGraph push_g = tr ? g->in_view() : g->view();
+    const DevGraph pull_g = tr ? g->view() : g->in_view();
     if (pull) {
       const int64_t groups_per_block = 256 / 8;
       int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
       kt_begin(st);
-      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(g->view(), in.bits, op, nb);
+      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(pull_g, in.bits, op, nb);
       kt_end(st);
       RG_CUDA(cudaGetLastError());
       g_timing.kernel_launches++;
@@ -210,21 +217,22 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
       if (hm == kHubPrefix) {
         hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
                         : hub_budget(sizeof(typename Op::HubT), g->n);
-        RG_TRY(launch_push<Op, kHubPrefix>(g, in, op, hub, nb, st));
+        RG_TRY(launch_push<Op, kHubPrefix>(g, push_g, in, op, hub, nb, st));
       } else if (hm == kHubMap) {
         uint32_t H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))
                              : hub_budget(sizeof(typename Op::HubT), g->n);
         RG_TRY(hub_map(g, H, hub));
-        RG_TRY(launch_push<Op, kHubMap>(g, in, op, hub, nb, st));
+        RG_TRY(launch_push<Op, kHubMap>(g, push_g, in, op, hub, nb, st));
       } else {
-        RG_TRY(launch_push<Op, kHubNone>(g, in, op, hub, nb, st));
+        RG_TRY(launch_push<Op, kHubNone>(g, push_g, in, op, hub, nb, st));
       }
     }
   }
   if (out) {
     Frontier tmp;  // non-owning shell for compact_bits
     tmp.bits.p = out->bits;
-    RG_TRY(compact_bits(g, tmp, st, true, depth, level, or_into, out->queue, out->qoff));
+    RG_TRY(compact_bits(g, tmp, st, true, depth, level, or_into, out->queue, out->qoff,
+                        (o.transpose && g->directed) ? g->in_off.as<uint32_t>() : nullptr));
     tmp.bits.p = nullptr;
     out->count = tmp.count;
     out->degsum = tmp.degsum;

@@ -272,8 +272,33 @@ __global__ void bc_final(double* deps, const double* __restrict__ inv, int64_t n
 }
 __global__ void set_f64(double* a, uint32_t i, double v) { a[i] = v; }
 
+// qoff = exclusive scan of the degrees (from deg_off) of a queue's vertices,
+// *degsum = their sum: a frontier's edge layout in another orientation.
+__global__ void queue_degrees(const uint32_t* __restrict__ q, int64_t k, const uint32_t* __restrict__ deg_off,
+                              uint32_t* __restrict__ deg) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) deg[j] = deg_off[q[j] + 1] - deg_off[q[j]];
+}
+
+static rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t count, const uint32_t* deg_off,
+                                 uint32_t* qoff, int64_t* degsum, DevBuf& tmp, cudaStream_t st) {
+  if (count == 0) {
+    *degsum = 0;
+    return RG_OK;
+  }
+  RG_TRY(tmp.reserve(4 * (size_t)count));
+  queue_degrees<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(queue, count, deg_off, tmp.as<uint32_t>());
+  RG_CUDA(cudaGetLastError());
+  RG_TRY(scan_u32(ctx().ws, tmp.as<uint32_t>(), qoff, count, st));
+  uint32_t total = 0;
+  RG_CUDA(cudaMemcpyAsync(&total, qoff + count, 4, cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  *degsum = total;
+  return RG_OK;
+}
+
 struct BcState {
-  DevBuf num_paths, deps, visited, levels_q, levels_qo, bits0, bits1, tmp;
+  DevBuf num_paths, deps, visited, levels_q, levels_qo, bits0, bits1, tmp, qdeg;
 };
 
 rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
@@ -313,8 +338,16 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
   int64_t total_levels = 0;
   std::vector<int64_t> lstart, lcount, ldeg;
   for (int it = 0; it < nsrc; it++) {
+    // the reference transposes the graph before every backward phase and
+    // never back (BC-manyiter-v2.C:334): on a directed graph source it's
+    // forward phase runs on the graph transposed `it` times, its backward
+    // phase on the opposite orientation (no-ops for symmetric graphs)
+    const bool fwd_t = g->directed && (it % 2 == 1);
+    EmOpts of = o, ob = o;
+    of.transpose = fwd_t;
+    ob.transpose = g->directed && !fwd_t;
     uint32_t start, start_deg;
-    RG_TRY(lookup_ids(g, &src_orig[it], 1, true, &start, &start_deg));
+    RG_TRY(lookup_ids(g, &src_orig[it], 1, true, &start, &start_deg, fwd_t));
     RG_CUDA(cudaMemsetAsync(np, 0, 8 * n, st));
     set_f64<<<1, 1, 0, st>>>(np, start, 1.0);
     RG_CUDA(cudaMemsetAsync(visited, 0, 4 * nwords, st));
@@ -338,7 +371,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     while (cur.count > 0) {
       round++;
       FView nxt{LQ + qpos, LQO + qpos + round, spare_bits, 0, 0};
-      RG_TRY(edge_map(g, cur, fop, &nxt, o, st, nullptr, 0, visited));
+      RG_TRY(edge_map(g, cur, fop, &nxt, of, st, nullptr, 0, visited));
       spare_bits = cur.bits;
       lstart.push_back(qpos);
       lcount.push_back(nxt.count);
@@ -364,6 +397,10 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     OpBcBwd bop{deps, visited};
     for (int64_t r = round - 2; r >= 0; r--) {
       FView lv = level_view(r + 1);
+      if (g->directed) {  // the level's degrees in the backward orientation
+        RG_TRY(requeue_degrees(g, lv.queue, lv.count, (ob.transpose ? g->in_off : g->off).as<uint32_t>(), lv.qoff,
+                               &lv.degsum, S.qdeg, st));
+      }
       // edge_map pulls a push-pull level above this size, and the pull reads
       // the level as a bitmap: build it with the same threshold
       const int64_t threshold = g->m / std::max<int64_t>(g_opts.dense_div, 1);
@@ -376,7 +413,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
         shell.queue.p = nullptr;
         shell.bits.p = nullptr;
       }
-      RG_TRY(edge_map(g, lv, bop, nullptr, o, st));
+      RG_TRY(edge_map(g, lv, bop, nullptr, ob, st));
       back_vertex(r);
     }
     bc_final<<<vblocks, 256, 0, st>>>(deps, np, n);
@@ -407,6 +444,9 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
 rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
   if (!g || k < 0 || (k > 0 && !out)) return fail(RG_EINVAL, "bad arguments");
   RG_TRY(host_arrays(g));
+  if (g->h_deg.size() != (size_t)g->n || (g->directed && g->h_in_deg.size() != (size_t)g->n) ||
+      (g->sorted && g->h_new_ids.size() != (size_t)g->n))
+    return fail(RG_EUNSUPPORTED, "host degree arrays missing");
   bool any = false;
   for (int64_t v = 0; v < g->n && !any; v++) any = g->h_deg[v] > 0;
   if (!any && k > 0) return fail(RG_EINVAL, "graph has no edges; no BC source can be drawn");
@@ -414,7 +454,10 @@ rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
   std::uniform_int_distribution<long> ud(0, g->n - 1);
   for (int i = 0; i < k; i++) {
     long s;
-    do { s = ud(rng); } while (g->h_deg[g->sorted ? g->h_new_ids[s] : (uint32_t)s] == 0);
+    // the reference checks the out-degree of the graph as it stands, and its
+    // BC transposes a directed graph once per source (BC-manyiter-v2.C:264-270)
+    const HostU32& deg = (g->directed && (i % 2)) ? g->h_in_deg : g->h_deg;
+    do { s = ud(rng); } while (deg[g->sorted ? g->h_new_ids[s] : (uint32_t)s] == 0);
     out[i] = (uint32_t)s;
   }
   return RG_OK;

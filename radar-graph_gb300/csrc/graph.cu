@@ -318,8 +318,10 @@ __global__ void comp_emit(const uint32_t* __restrict__ bits, int64_t nwords, con
 }
 
 rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool sync, int32_t* depth,
-                       int32_t level, uint32_t* or_into, uint32_t* queue_out, uint32_t* qoff_out) {
+                       int32_t level, uint32_t* or_into, uint32_t* queue_out, uint32_t* qoff_out,
+                       const uint32_t* deg_off) {
   Workspace& ws = ctx().ws;
+  const uint32_t* doff = deg_off ? deg_off : g->off.as<uint32_t>();
   const int64_t nwords = (g->n + 31) / 32;
   const int64_t nt = (nwords + kCompTile - 1) / kCompTile;
   RG_TRY(ws.scan_partials.reserve(sizeof(uint32_t) * 2 * (nt + 1)));
@@ -328,10 +330,10 @@ rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool syn
   uint32_t* q = queue_out ? queue_out : f.queue.as<uint32_t>();
   uint32_t* qo = qoff_out ? qoff_out : f.qoff.as<uint32_t>();
   uint64_t* info = ws.counters.as<uint64_t>();
-  comp_count<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, g->off.as<uint32_t>(), pc, pd);
+  comp_count<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, doff, pc, pd);
   comp_scan<<<1, kCompThreads, 0, st>>>(pc, pd, nt, info, qo);
-  comp_emit<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, g->off.as<uint32_t>(), pc,
-                                                   pd, q, qo, depth, level, or_into);
+  comp_emit<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, doff, pc, pd, q, qo, depth,
+                                                   level, or_into);
   RG_CUDA(cudaGetLastError());
   RG_CUDA(cudaMemcpyAsync(ws.h_info, info, 16, cudaMemcpyDeviceToHost, st));
   f.queue_valid = (queue_out == nullptr);
@@ -393,12 +395,19 @@ rg_status host_arrays(const rg_graph* g) {
     g->h_new_ids.resize(n);
     RG_CUDA(cudaMemcpy(g->h_new_ids.data(), g->new_ids.p, 4 * n, cudaMemcpyDeviceToHost));
   }
+  if (g->directed) {
+    RG_CUDA(cudaMemcpy(off.data(), g->in_off.p, 4 * (n + 1), cudaMemcpyDeviceToHost));
+    g->h_in_deg.resize(n);
+#pragma omp parallel for
+    for (int64_t v = 0; v < n; v++) g->h_in_deg[v] = off[v + 1] - off[v];
+  }
   g->host_ready = true;
   return RG_OK;
 }
 
 rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool orig, uint32_t* internal_out,
-                     uint32_t* deg_out) {
+                     uint32_t* deg_out, bool in_degree) {
+  in_degree = in_degree && g->directed;
   for (int64_t i = 0; i < k; i++) {
     if (ids[i] >= (uint64_t)g->n) return fail(RG_EINVAL, "vertex id %u >= n", ids[i]);
   }
@@ -410,10 +419,12 @@ rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool ori
   }
   if (ready || k > 4096) {
     RG_TRY(host_arrays(g));
+    if ((in_degree ? g->h_in_deg : g->h_deg).size() != (size_t)g->n || (map && g->h_new_ids.size() != (size_t)g->n))
+      return fail(RG_EUNSUPPORTED, "host degree arrays missing");
     for (int64_t i = 0; i < k; i++) {
       const uint32_t v = map ? g->h_new_ids[ids[i]] : ids[i];
       if (internal_out) internal_out[i] = v;
-      if (deg_out) deg_out[i] = g->h_deg[v];
+      if (deg_out) deg_out[i] = in_degree ? g->h_in_deg[v] : g->h_deg[v];
     }
     return RG_OK;
   }
@@ -426,7 +437,8 @@ rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool ori
   std::vector<uint32_t> back(2 * k);
   RG_CUDA(cudaMemcpyAsync(d, ids, 4 * k, cudaMemcpyHostToDevice, st));
   lookup_kernel<<<(unsigned)((k + 255) / 256), 256, 0, st>>>(map ? g->new_ids.as<uint32_t>() : nullptr,
-                                                             g->off.as<uint32_t>(), d, k, d + k, d + 2 * k);
+                                                             (in_degree ? g->in_off : g->off).as<uint32_t>(), d, k,
+                                                             d + k, d + 2 * k);
   RG_CUDA(cudaGetLastError());
   RG_CUDA(cudaMemcpyAsync(back.data(), d + k, 8 * k, cudaMemcpyDeviceToHost, st));
   RG_CUDA(cudaStreamSynchronize(st));
@@ -500,6 +512,12 @@ static rg_status finish_graph(rg_graph* g) {
     build_chunk_starts<<<(unsigned)((g->nchunks + 1 + 255) / 256), 256, 0, st>>>(
         g->off.as<uint32_t>(), (uint32_t)g->n, (uint32_t)g->m, g->nchunks, g->chunk_v.as<uint32_t>());
     RG_CUDA(cudaGetLastError());
+    if (g->directed) {
+      RG_TRY(g->in_chunk_v.reserve(sizeof(uint32_t) * (g->nchunks + 1)));
+      build_chunk_starts<<<(unsigned)((g->nchunks + 1 + 255) / 256), 256, 0, st>>>(
+          g->in_off.as<uint32_t>(), (uint32_t)g->n, (uint32_t)g->m, g->nchunks, g->in_chunk_v.as<uint32_t>());
+      RG_CUDA(cudaGetLastError());
+    }
   }
   RG_CUDA(cudaStreamSynchronize(st));
   return RG_OK;
@@ -750,9 +768,23 @@ __global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t*
 
 }  // namespace rg
 
-extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids) {
+// in-degree of each rank's vertex (a directed graph's new in-lists)
+__global__ void rank_in_deg(const uint32_t* __restrict__ sorted_ids, const uint32_t* __restrict__ in_off, uint32_t n,
+                            uint32_t* __restrict__ new_in_deg) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) {
+    const uint32_t v = sorted_ids[r];
+    new_in_deg[r] = in_off[v + 1] - in_off[v];
+  }
+}
+
+// Degree sort (IO.h:728-903): ranks by out-degree, or for a directed graph by
+// in-degree unless by_out (-preprocess 1 / 0, IO.h:739-750); both lists of a
+// directed graph are relabelled, their order kept.
+static rg_status degree_sort_impl(const rg_graph* g, bool by_out, rg_graph** out, uint32_t* h_new_ids) {
   if (!g || !out) return fail(RG_EINVAL, "rg_graph_degree_sort: null argument");
   const int64_t n = g->n, m = g->m;
+  const bool by_in = g->directed && !by_out;
   Ctx* c = nullptr;
   RG_TRY(get_ctx(&c));
   cudaStream_t st = c->stream;
@@ -763,11 +795,13 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
   RG_TRY(k0.reserve(4 * n)); RG_TRY(v0.reserve(4 * n));
   RG_TRY(k1.reserve(4 * n)); RG_TRY(v1.reserve(4 * n));
   RG_TRY(hist.reserve(4 * (256 * nblocks + 1)));
-  sort_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->off.as<uint32_t>(), (uint32_t)n, k0.as<uint32_t>(),
-                                                        v0.as<uint32_t>());
+  sort_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((by_in ? g->in_off : g->off).as<uint32_t>(), (uint32_t)n,
+                                                        k0.as<uint32_t>(), v0.as<uint32_t>());
   // ~deg differs from 0xFFFFFFFF only in the low bits that max_deg spans
+  // (in-degrees: all 32 bits, their maximum is not kept)
   int bits = 0;
   while (bits < 32 && (g->max_deg >> bits) != 0) bits++;
+  if (by_in) bits = 32;
   int passes = (bits + 7) / 8;
   uint32_t *ka = k0.as<uint32_t>(), *va = v0.as<uint32_t>(), *kb = k1.as<uint32_t>(), *vb = v1.as<uint32_t>();
   for (int p = 0; p < passes; p++) {
@@ -796,6 +830,19 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
     delete ng;
     return s;
   }
+  ng->directed = g->directed;
+  if (g->directed) {  // in-lists: offsets from the ranks' in-degrees (new_deg is free again after the scan)
+    if ((s = ng->in_off.reserve(4 * (n + 1))) != RG_OK || (s = ng->in_adj.reserve(4 * (m + 8))) != RG_OK) {
+      delete ng;
+      return s;
+    }
+    rank_in_deg<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(va, g->in_off.as<uint32_t>(), (uint32_t)n,
+                                                            new_deg.as<uint32_t>());
+    if ((s = scan_u32(ws, new_deg.as<uint32_t>(), ng->in_off.as<uint32_t>(), n, st)) != RG_OK) {
+      delete ng;
+      return s;
+    }
+  }
   if (m > 0) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device);
@@ -803,8 +850,14 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
     relabel_sweep<<<(unsigned)blocks, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
                                                     ng->new_ids.as<uint32_t>(), ng->off.as<uint32_t>(),
                                                     ng->adj.as<uint32_t>());
+    if (g->directed) {
+      relabel_sweep<<<(unsigned)blocks, 256, 0, st>>>(g->in_view(), g->in_chunks(), (uint32_t)g->nchunks,
+                                                      ng->new_ids.as<uint32_t>(), ng->in_off.as<uint32_t>(),
+                                                      ng->in_adj.as<uint32_t>());
+    }
   }
   cudaError_t e = cudaMemsetAsync(ng->adj.as<uint32_t>() + m, 0, 32, st);
+  if (e == cudaSuccess && g->directed) e = cudaMemsetAsync(ng->in_adj.as<uint32_t>() + m, 0, 32, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
@@ -820,6 +873,15 @@ extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uin
   if ((s = finish_graph(ng)) != RG_OK) { delete ng; return s; }
   *out = ng;
   return RG_OK;
+}
+
+extern "C" rg_status rg_graph_degree_sort(const rg_graph* g, rg_graph** out, uint32_t* h_new_ids) {
+  return degree_sort_impl(g, false, out, h_new_ids);
+}
+
+extern "C" rg_status rg_graph_degree_sort_by(const rg_graph* g, int by_out_degree, rg_graph** out,
+                                             uint32_t* h_new_ids) {
+  return degree_sort_impl(g, by_out_degree != 0, out, h_new_ids);
 }
 
 // ---------------------------------------------------------------------------
@@ -856,7 +918,7 @@ __global__ void csr_compact(const uint32_t* __restrict__ a, const uint32_t* __re
 __global__ void csr_offsets(const uint32_t* __restrict__ a, int64_t m, int64_t n, uint32_t* __restrict__ off) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= m; p += (int64_t)gridDim.x * blockDim.x) {
     const int64_t lo = p == 0 ? 0 : (int64_t)a[p - 1] + 1;
-    const int64_t hi = p == m ? n : (int64_t)a[p];
+    const int64_t hi = p == m ? n : min((int64_t)a[p], n);  // ids are < n; never write past off[n]
     for (int64_t v = lo; v <= hi; v++) off[v] = (uint32_t)p;
   }
 }
@@ -998,5 +1060,83 @@ extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, co
   g->max_deg = mx;  // host degree array: on first full use (host_arrays)
   if ((s = finish_graph(g)) != RG_OK) { delete g; return s; }
   *out = g;
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// directed graphs: the in-lists (the reference's CSC, IO.h:287-345) built on
+// the device.  The out-list entries are already ordered by source, so one
+// stable radix sort by target leaves every in-list's sources ascending.
+// ---------------------------------------------------------------------------
+namespace rg {
+
+__global__ void __launch_bounds__(256) expand_rows(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                   uint32_t nchunks, uint32_t* __restrict__ row) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+    for (int r = 0; r < kSweepChunk / 32; r++) {
+      const uint32_t e = c * kSweepChunk + r * 32 + lane;
+      if (e >= g.m) break;
+      row[e] = upper_index(g.off, vlo, vhi, e);
+    }
+  }
+}
+
+static rg_status build_in_lists(rg_graph* g, cudaStream_t st) {
+  const int64_t n = g->n, m = g->m;
+  RG_TRY(g->in_off.reserve(4 * (n + 1)));
+  RG_TRY(g->in_adj.reserve(4 * (m + 8)));
+  RG_CUDA(cudaMemsetAsync(g->in_adj.as<uint32_t>() + m, 0, 32, st));
+  int sms = 0;
+  RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device));
+  if (m == 0) {
+    RG_CUDA(cudaMemsetAsync(g->in_off.p, 0, 4 * (n + 1), st));
+    return RG_OK;
+  }
+  DevBuf key{true, st}, val{true, st}, key2{true, st}, val2{true, st}, hist{true, st};
+  RG_TRY(key.reserve(4 * (size_t)m));
+  RG_TRY(val.reserve(4 * (size_t)m));
+  RG_TRY(key2.reserve(4 * (size_t)m));
+  RG_TRY(val2.reserve(4 * (size_t)m));
+  RG_CUDA(cudaMemcpyAsync(key.p, g->adj.p, 4 * m, cudaMemcpyDeviceToDevice, st));
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((g->nchunks * 32 + 255) / 256, (int64_t)sms * 8));
+  expand_rows<<<(unsigned)blocks, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
+                                                val.as<uint32_t>());
+  RG_CUDA(cudaGetLastError());
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)(n - 1) >> bits) != 0) bits++;
+  RG_TRY(radix_pairs(ctx().ws, key, val, key2, val2, m, bits, hist, st));
+  RG_CUDA(cudaMemcpyAsync(g->in_adj.p, val.p, 4 * m, cudaMemcpyDeviceToDevice, st));
+  const int oblocks = (int)std::max<int64_t>(1, std::min<int64_t>((m + 1 + 255) / 256, (int64_t)sms * 32));
+  csr_offsets<<<oblocks, 256, 0, st>>>(key.as<uint32_t>(), m, n, g->in_off.as<uint32_t>());
+  RG_CUDA(cudaGetLastError());
+  RG_CUDA(cudaStreamSynchronize(st));
+  return RG_OK;
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_graph_create_directed(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                                              rg_graph** out) {
+  rg_graph* g = nullptr;
+  RG_TRY(rg_graph_create(n, m, h_off, h_adj, &g));
+  g->directed = true;
+  g->host_ready = false;  // host in-degrees come with the in-lists (host_arrays)
+  rg_status s = build_in_lists(g, ctx().stream);
+  if (s == RG_OK) s = finish_graph(g);  // partitions of both lists
+  if (s != RG_OK) {
+    rg_graph_free(g);
+    return s;
+  }
+  *out = g;
+  return RG_OK;
+}
+
+extern "C" rg_status rg_graph_is_directed(const rg_graph* g, int* directed) {
+  if (!g || !directed) return fail(RG_EINVAL, "null argument");
+  *directed = g->directed ? 1 : 0;
   return RG_OK;
 }

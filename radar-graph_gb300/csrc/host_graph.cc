@@ -222,9 +222,9 @@ rg_status read_graph(const char* path, int symmetric, int binary, int64_t* n_out
   if (!path || !n_out || !m_out || !off_out || !adj_out) {
     return fail(RG_EINVAL, "rg_read_graph: null argument");
   }
-  if (!symmetric) {
-    return fail(RG_EUNSUPPORTED, "rg_read_graph: directed graphs are not supported yet");
-  }
+  // a directed graph's out-lists get the same per-list clean-up as a
+  // symmetric one's (IO.h:287-474); its in-lists are built on the device
+  (void)symmetric;
   if (binary) {  // IO.h:477-626: .config holds n, .adj uint32 edges, .idx uint32 offsets
     std::string base(path);
     FILE* cf = fopen((base + ".config").c_str(), "r");

@@ -358,7 +358,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
       if (g->m > 0) {
         kt_begin(st);
         if (pull) {
-          pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+          pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->in_view(), g->in_chunks(),
                                                               (uint32_t)g->nchunks, C, (unsigned long long*)acc,
                                                               cacheH, prev);
         } else {

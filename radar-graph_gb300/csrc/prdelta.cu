@@ -188,7 +188,7 @@ rg_status pagerank_delta_run(rg_graph* g, int variant, int64_t max_iters, double
       const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
       g_timing.edges_traversed += cur.degsum;
       kt_begin(st);
-      prd_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
+      prd_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(),
                                                                              (uint32_t)g->nchunks, c, ngh);
       kt_end(st);
       RG_CUDA(cudaGetLastError());

@@ -141,9 +141,13 @@ struct rg_graph {
   int device = 0;
   uint64_t uid = 0;  // unique per graph in the process (device addresses can repeat)
   int64_t n = 0, m = 0;
-  rg::DevBuf off{true}, adj{true};  // CSR on the device
+  rg::DevBuf off{true}, adj{true};  // CSR on the device (out-lists)
   rg::DevBuf chunk_v{true};         // sweep partition: first vertex of every kSweepChunk edges
   int64_t nchunks = 0;
+  // directed graphs: in-lists (CSC, sources ascending) and their partition;
+  // a symmetric graph's in-lists are its out-lists
+  bool directed = false;
+  rg::DevBuf in_off{true}, in_adj{true}, in_chunk_v{true};
   bool sorted = false;
   rg::DevBuf new_ids{true};         // orig -> internal (when sorted)
   // Host copies of new_ids and of the degree by internal id.  An uploaded
@@ -152,6 +156,7 @@ struct rg_graph {
   // the sources), which lookup_ids reads from the device instead.
   mutable rg::HostU32 h_new_ids;
   mutable rg::HostU32 h_deg;
+  mutable rg::HostU32 h_in_deg;  // directed graphs: in-degree by internal id
   mutable bool host_ready = false;
   mutable std::mutex host_mu;
   uint32_t max_deg = 0;
@@ -160,6 +165,11 @@ struct rg_graph {
   rg::DevGraph view() const {
     return rg::DevGraph{(uint32_t)n, (uint32_t)m, off.as<uint32_t>(), adj.as<uint32_t>()};
   }
+  // the lists a pull reads (edges into each vertex) and their partition
+  rg::DevGraph in_view() const {
+    return directed ? rg::DevGraph{(uint32_t)n, (uint32_t)m, in_off.as<uint32_t>(), in_adj.as<uint32_t>()} : view();
+  }
+  const uint32_t* in_chunks() const { return directed ? in_chunk_v.as<uint32_t>() : chunk_v.as<uint32_t>(); }
   ~rg_graph();
 };
 
@@ -177,17 +187,21 @@ rg_status scan_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n, 
 // Builds frontier f (queue+qoff, ascending) from its bitmap.  Writes
 // (count, degsum) into ws.h_info[0..1] and syncs the stream if `sync`.
 // Optional epilogues: depth[v] = level for every member; or_into |= bits.
+// Degrees (for qoff/degsum) come from deg_off (n+1 offsets; default: the
+// out-lists).
 rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool sync,
                        int32_t* depth = nullptr, int32_t level = 0, uint32_t* or_into = nullptr,
-                       uint32_t* queue_out = nullptr, uint32_t* qoff_out = nullptr);
+                       uint32_t* queue_out = nullptr, uint32_t* qoff_out = nullptr,
+                       const uint32_t* deg_off = nullptr);
 
 // Fills g's host arrays (h_new_ids when sorted, h_deg) if not yet there.
 rg_status host_arrays(const rg_graph* g);
 // For k host ids (ORIGINAL ids when `orig`, else internal): the internal id
 // and/or the degree (either output may be null).  Few ids are gathered on
 // the device; many, or a graph whose host arrays exist, use the host arrays.
+// deg_out holds in-degrees when in_degree (directed graphs).
 rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool orig, uint32_t* internal_out,
-                     uint32_t* deg_out);
+                     uint32_t* deg_out, bool in_degree = false);
 
 // Sets a frontier from host ids (queue + qoff from their degrees + bitmap).
 rg_status frontier_from_host(const rg_graph* g, Frontier& f, const uint32_t* ids, int64_t k,

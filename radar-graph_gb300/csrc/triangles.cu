@@ -152,6 +152,7 @@ struct TcState {
 
 rg_status triangle_run(rg_graph* g, uint64_t* h_counts, uint64_t* total_out) {
   if (!g) return fail(RG_EINVAL, "null graph");
+  if (g->directed) return fail(RG_EUNSUPPORTED, "triangle counting needs an undirected graph (tc_local.cc:21-25)");
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;

@@ -116,6 +116,9 @@ _SIGS = {
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
     "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
+    "rg_graph_create_directed": [C.c_int64, C.c_int64, _u32p, _u32p, _P(C.c_void_p)],
+    "rg_graph_is_directed": [C.c_void_p, _P(C.c_int)],
+    "rg_graph_degree_sort_by": [C.c_void_p, C.c_int, _P(C.c_void_p), _u32p],
     "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
     "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
@@ -309,6 +312,28 @@ class Graph:
         _check(lib().rg_graph_create(len(off) - 1, len(adj), _ptr(off, C.c_uint32), _ptr(adj, C.c_uint32),
                                      C.byref(h)))
         return cls(h)
+
+    @classmethod
+    def from_csr_directed(cls, off, adj):
+        """A directed graph from its cleaned out-lists; in-lists built on the device."""
+        off = np.ascontiguousarray(off, np.uint32)
+        adj = np.ascontiguousarray(adj, np.uint32)
+        h = C.c_void_p()
+        _check(lib().rg_graph_create_directed(len(off) - 1, len(adj), _ptr(off, C.c_uint32),
+                                              _ptr(adj, C.c_uint32), C.byref(h)))
+        return cls(h)
+
+    @property
+    def directed(self):
+        d = C.c_int()
+        _check(lib().rg_graph_is_directed(self._h, C.byref(d)))
+        return bool(d.value)
+
+    def degree_sort_by(self, by_out_degree):
+        """Degree sort with the key chosen (out-degree, or in-degree for a directed graph)."""
+        h = C.c_void_p()
+        _check(lib().rg_graph_degree_sort_by(self._h, 1 if by_out_degree else 0, C.byref(h), None))
+        return Graph(h)
 
     @classmethod
     def from_edges(cls, n, src, dst):

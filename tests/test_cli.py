@@ -38,8 +38,8 @@ def _write_raw(golden, name, tmp_path):
 def test_usage_and_flags():
     r = _run("BFS")
     assert r.returncode == 2 and "usage" in r.stderr
-    r = _run("PageRank", "-maxiters", "3", "graph.adj")  # no -s
-    assert r.returncode == 2 and "symmetric" in r.stderr
+    r = _run("PageRank", "-maxiters", "3", "/nonexistent/graph.adj")  # no -s: read as a directed graph
+    assert r.returncode == 1 and "Unable to open" in r.stderr
     r = _run("BC", "-s", "-variant", "nosuch", "graph.adj")
     assert r.returncode == 2 and "variant" in r.stderr
     r = _run("Radii", "-s", "/nonexistent/graph.adj")
