@@ -14,7 +14,9 @@ app's result back.
 The same JSON line also carries the batched launch (512 uneven R-MAT graphs,
 64-source BFS + 10-iteration PageRank each, one persistent launch) and the
 served stream (3 resident graphs, Poisson arrivals of a BFS/BC/Radii mix),
-each against the plain one-query-per-launch GPU path.
+each against the plain one-query-per-launch GPU path, and the next rows:
+PageRankDelta, the device CSR build, triangle counting and the directed path
+(the same four apps on a directed R-MAT graph, in-degree sorted).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--scale S] [--impl reference]
 
@@ -206,6 +208,77 @@ def bench_triangles(rg, gs, with_cpu, small_scale=20):
         small["cpu_threads"] = os.cpu_count()
         small["identical"] = int(tc) == int(tg)
     out["s_small"] = small
+    return out
+
+
+def bench_directed(rg, scale, with_cpu, ef=16, seed=1, reps=3):
+    """The directed path: RMAT edges kept one way (src -> dst), built on the
+    device (out-lists cleaned, in-lists), in-degree sorted, then the four
+    RADAR apps (PageRank pulls over in-edges, BC transposes per source), with
+    the oracle port on the same sorted graph (PageRank 2 iterations, BFS, BC,
+    Radii) and the BFS depths and radii compared."""
+    src, dst = rg.generate_edges(scale, ef, seed, False)
+    n = 1 << scale
+    src_p, dst_p = rg.pinned_empty(len(src), np.uint32), rg.pinned_empty(len(dst), np.uint32)
+    src_p[:], dst_p[:] = src, dst
+    build_ms = []
+    for i in range(reps + 1):
+        rg.lib().rg_synchronize()
+        t0 = time.perf_counter()
+        g = rg.Graph.from_edges(n, src_p, dst_p, directed=True)
+        rg.lib().rg_synchronize()
+        if i:
+            build_ms.append((time.perf_counter() - t0) * 1e3)
+        if i < reps:
+            g.free()
+    off, _, _ = g.download()
+    root = pick_root(off)
+    gs = g.degree_sort()  # in-degree order (-preprocess 1)
+    g.free()
+    bc_src = gs.bc_pick_sources(1)
+    gs.autotune("radar")
+    stats = {}
+    for i in range(reps + 1):
+        run_step(rg, gs, root, bc_src, stats if i else {})
+    apps = {k: {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3), "ms": round(s["ms"] / reps, 3)}
+            for k, s in stats.items()}
+    tot_e = sum(s["edges"] for s in stats.values())
+    tot_ms = sum(s["ms"] for s in stats.values())
+    out = {"n": n, "m": int(gs.m), "edges_in": int(len(src)), "device_build_ms": round(min(build_ms), 2),
+           "gteps": round(tot_e / (tot_ms / 1e3) / 1e9, 3), "ms_per_step": round(tot_ms / reps, 3), "apps": apps,
+           "workload": f"RADAR PageRank(20 it)+BFS+BC(1 src)+Radii(64) on directed RMAT s{scale} ef{ef} seed {seed}, "
+                       "in-degree sorted, autotuned schedule"}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        cores = os.cpu_count() or 1
+        so, sa, ids = gs.download()
+        io, ia = orc.transpose(so, sa)
+        kw = {"in_off": io, "in_adj": ia}
+        _, depth, _, _ = gs.bfs("radar", root)
+        r_gpu, _ = gs.radii("radar")
+        seeds = orc.radii_seeds(n)
+        t, e, res = {}, {}, {}
+        runs = {
+            "pagerank": lambda: orc.pagerank(so, sa, "radar", 2, cores, **kw),
+            "bfs": lambda: orc.bfs(so, sa, int(ids[root]), "radar", cores, **kw),
+            "bc": lambda: orc.bc(so, sa, ids[bc_src], "radar", cores, **kw),
+            "radii": lambda: orc.radii(so, sa, ids[seeds], "radar", cores, **kw),
+        }
+        for k, fn in runs.items():
+            orc.take_edges()
+            t0 = time.time()
+            res[k] = fn()
+            t[k] = time.time() - t0
+            e[k] = orc.take_edges()
+        par = res["bfs"][0]
+        d_cpu = orc.depths_from_parents(par)[ids]
+        out["cpu_port"] = {"gteps": round(sum(e.values()) / sum(t.values()) / 1e9, 4), "cores": cores,
+                           "sample": "PageRank 2 iterations + BFS + BC 1 source + Radii 64 on the same sorted graph",
+                           "seconds": {k: round(v, 3) for k, v in t.items()},
+                           "identical_bfs_depths_and_radii": bool(np.array_equal(depth, d_cpu) and
+                                                                  np.array_equal(r_gpu, res["radii"][0][ids]))}
+    gs.free()
     return out
 
 
@@ -459,7 +532,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -577,6 +650,7 @@ def main():
     if rank == 0 and not args.no_extra:
         extra["graph_build"] = bench_input(rg, args.scale)
         extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
+        extra["directed"] = bench_directed(rg, args.scale, world == 1 and not args.no_cpu)
         extra["batched"] = bench_batched(rg)
         gsv = []
         for sc in (20, 22):

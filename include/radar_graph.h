@@ -128,6 +128,12 @@ rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_
  * Triangle counting and serving take undirected graphs only. */
 rg_status rg_graph_create_directed(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
                                    rg_graph** out);
+/* A DIRECTED graph built on the device from an edge list (src -> dst, ids
+ * < n; device arrays when on_device != 0): out-lists sorted, repeats and self
+ * loops dropped (the directed loader's per-list clean-up, IO.h:287-345), then
+ * the in-lists as in rg_graph_create_directed. */
+rg_status rg_graph_create_directed_from_edges(int64_t n, int64_t num_edges, const uint32_t* src,
+                                              const uint32_t* dst, int on_device, rg_graph** out);
 rg_status rg_graph_is_directed(const rg_graph* g, int* directed);
 /* Uploads from arrays already on the device (copied; caller keeps ownership). */
 rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,

@@ -968,21 +968,28 @@ static rg_status radix_pairs(Workspace& ws, DevBuf& key, DevBuf& val, DevBuf& ke
 
 }  // namespace rg
 
-extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_t* src, const uint32_t* dst,
-                                                int on_device, rg_graph** out) {
+namespace rg {
+rg_status build_in_lists(rg_graph* g, cudaStream_t st);
+}
+
+// Shared by the symmetric and directed builders.  Symmetric: entries
+// (a, b) = [src, dst] x [dst, src]; directed: (src, dst) only, and the
+// in-lists are built afterwards.
+static rg_status create_from_edges(const char* who, int64_t n, int64_t num_edges, const uint32_t* src,
+                                   const uint32_t* dst, int on_device, bool directed, rg_graph** out) {
   if (!out || n <= 0 || num_edges < 0 || (num_edges > 0 && (!src || !dst))) {
-    return fail(RG_EINVAL, "rg_graph_create_from_edges: bad arguments");
+    return fail(RG_EINVAL, "%s: bad arguments", who);
   }
-  if (n >= 0xFFFFFFFFll || 2 * num_edges >= 0xFFFFFFFFll) {
-    return fail(RG_EUNSUPPORTED, "rg_graph_create_from_edges: >= 2^32 vertices or directed entries");
+  const int64_t k = directed ? num_edges : 2 * num_edges;
+  if (n >= 0xFFFFFFFFll || k >= 0xFFFFFFFFll) {
+    return fail(RG_EUNSUPPORTED, "%s: >= 2^32 vertices or directed entries", who);
   }
   Ctx* c = nullptr;
   RG_TRY(get_ctx(&c));
   cudaStream_t st = c->stream;
   int sms = 0;
   RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-  const int64_t k = 2 * num_edges;
-  // entries (a, b): a = [src, dst], b = [dst, src]; temporaries from the pool
+  // temporaries from the pool
   DevBuf a{true, st}, b{true, st}, a2{true, st}, b2{true, st}, hist{true, st}, info{true, st};
   RG_TRY(a.reserve(4 * (size_t)k));
   RG_TRY(b.reserve(4 * (size_t)k));
@@ -992,9 +999,11 @@ extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, co
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (num_edges > 0) {
     RG_CUDA(cudaMemcpyAsync(a.as<uint32_t>(), src, 4 * num_edges, kind, st));
-    RG_CUDA(cudaMemcpyAsync(a.as<uint32_t>() + num_edges, dst, 4 * num_edges, kind, st));
     RG_CUDA(cudaMemcpyAsync(b.as<uint32_t>(), dst, 4 * num_edges, kind, st));
-    RG_CUDA(cudaMemcpyAsync(b.as<uint32_t>() + num_edges, src, 4 * num_edges, kind, st));
+    if (!directed) {
+      RG_CUDA(cudaMemcpyAsync(a.as<uint32_t>() + num_edges, dst, 4 * num_edges, kind, st));
+      RG_CUDA(cudaMemcpyAsync(b.as<uint32_t>() + num_edges, src, 4 * num_edges, kind, st));
+    }
   }
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((k + 255) / 256, (int64_t)sms * 32));
   if (k > 0) {  // every id must be < n: the offsets below are indexed by them
@@ -1059,8 +1068,27 @@ extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, co
   }
   g->max_deg = mx;  // host degree array: on first full use (host_arrays)
   if ((s = finish_graph(g)) != RG_OK) { delete g; return s; }
+  if (directed) {
+    g->directed = true;
+    s = build_in_lists(g, st);          // uses the out-list partition
+    if (s == RG_OK) s = finish_graph(g);  // partitions of both lists
+    if (s != RG_OK) {
+      rg_graph_free(g);
+      return s;
+    }
+  }
   *out = g;
   return RG_OK;
+}
+
+extern "C" rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                                int on_device, rg_graph** out) {
+  return create_from_edges("rg_graph_create_from_edges", n, num_edges, src, dst, on_device, false, out);
+}
+
+extern "C" rg_status rg_graph_create_directed_from_edges(int64_t n, int64_t num_edges, const uint32_t* src,
+                                                         const uint32_t* dst, int on_device, rg_graph** out) {
+  return create_from_edges("rg_graph_create_directed_from_edges", n, num_edges, src, dst, on_device, true, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1085,7 +1113,7 @@ __global__ void __launch_bounds__(256) expand_rows(DevGraph g, const uint32_t* _
   }
 }
 
-static rg_status build_in_lists(rg_graph* g, cudaStream_t st) {
+rg_status build_in_lists(rg_graph* g, cudaStream_t st) {
   const int64_t n = g->n, m = g->m;
   RG_TRY(g->in_off.reserve(4 * (n + 1)));
   RG_TRY(g->in_adj.reserve(4 * (m + 8)));

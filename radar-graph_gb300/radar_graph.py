@@ -122,6 +122,7 @@ _SIGS = {
     "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
     "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
+    "rg_graph_create_directed_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
     "rg_pinned_free": [C.c_void_p],
 }
@@ -336,16 +337,19 @@ class Graph:
         return Graph(h)
 
     @classmethod
-    def from_edges(cls, n, src, dst):
-        """Symmetric CSR built on the device from an edge list (the loader's
-        clean-up: both directions, sorted, no repeats or self loops)."""
+    def from_edges(cls, n, src, dst, directed=False):
+        """CSR built on the device from an edge list with the loader's
+        clean-up: symmetric (both directions, sorted, no repeats or self
+        loops), or directed (src -> dst out-lists cleaned the same way, plus
+        the in-lists)."""
         src = np.ascontiguousarray(src, np.uint32)
         dst = np.ascontiguousarray(dst, np.uint32)
         if len(src) != len(dst):
             raise ValueError("src and dst differ in length")
         h = C.c_void_p()
-        _check(lib().rg_graph_create_from_edges(n, len(src), src.ctypes.data if len(src) else None,
-                                                dst.ctypes.data if len(dst) else None, 0, C.byref(h)))
+        fn = lib().rg_graph_create_directed_from_edges if directed else lib().rg_graph_create_from_edges
+        _check(fn(n, len(src), src.ctypes.data if len(src) else None, dst.ctypes.data if len(dst) else None, 0,
+                  C.byref(h)))
         return cls(h)
 
     def degree_sort(self):

@@ -86,3 +86,31 @@ def test_device_build_equals_host_cleanup(case):
 def test_device_build_rejects_ids_out_of_range():
     with pytest.raises(rg.RgError, match="endpoint"):
         rg.Graph.from_edges(4, np.array([0, 1], np.uint32), np.array([2, 9], np.uint32))
+
+
+def _directed_cleanup(n, s, d):
+    """Directed per-list clean-up in numpy: out-lists sorted, repeats and
+    self loops dropped."""
+    s, d = np.asarray(s, np.uint64), np.asarray(d, np.uint64)
+    keys = np.unique(((s << np.uint64(32)) | d)[s != d])
+    src = (keys >> np.uint64(32)).astype(np.int64)
+    off = np.searchsorted(src, np.arange(n + 1), side="left").astype(np.uint32)
+    return off, (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
+def test_directed_device_build_equals_cleanup(case):
+    _, n, s, d = case
+    off, adj = _directed_cleanup(n, s, d)
+    with rg.Graph.from_edges(n, s, d, directed=True) as g:
+        assert g.directed and (g.n, g.m) == (n, len(adj))
+        o2, a2, _ = g.download()
+        assert np.array_equal(o2, off)
+        assert np.array_equal(a2, adj)
+        if len(adj):  # in-lists: pulls over them equal the uploaded graph's
+            with rg.Graph.from_csr_directed(off, adj) as g2:
+                for v in ("push", "push-pull"):
+                    r, it, _ = g.pagerank(v, 5)
+                    r2, it2, _ = g2.pagerank(v, 5)
+                    assert it == it2 and np.array_equal(r, r2)
