@@ -215,6 +215,17 @@ rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seed
 rg_status rg_bfs_multi(rg_graph* g, const uint32_t* h_sources, int k, int32_t* h_depths,
                        int64_t* rounds_out);
 
+/* k <= 64 independent single-source BC queries (ORIGINAL ids) in one
+ * traversal: the sources' levels from one 64-wide bitmask BFS, then path
+ * counts (exact 64-bit integers) and dependencies for all sources per level,
+ * one row of k values per vertex.  h_deps: k*n doubles, row q equal to
+ * rg_bc_sources(g, variant, &sources[q], 1, row) for every variant (the
+ * single-source pass of BC-manyiter-v2.C:180-232) up to summation order;
+ * NaN where sources[q] does not reach the vertex.  A graph whose path counts
+ * pass 2^64 is answered by one single-source pass per source. */
+rg_status rg_bc_multi(rg_graph* g, const uint32_t* h_sources, int k, double* h_deps,
+                      int64_t* levels_out);
+
 /* A set of graphs resident on the device, run by one persistent kernel. */
 typedef struct rg_batch rg_batch;
 /* Symmetric CSRs (h_offs[i]: ns[i]+1 entries, h_adjs[i]: ms[i]). */

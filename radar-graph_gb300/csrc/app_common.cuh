@@ -60,6 +60,14 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
 rg_status bc_pick(const rg_graph* g, int k, uint32_t* out);
 rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h_depths, int64_t* rounds_out,
                         int32_t* d_depths_out = nullptr);
+// k <= 64 independent single-source BCs in one traversal: h_out / d_out (either
+// may be null) receive k rows of n doubles in original-id order (bc_multi.cu).
+rg_status bc_multi_run(rg_graph* g, const uint32_t* src_orig, int k, double* h_out, double* d_out,
+                       int64_t* levels_out);
+// qoff = exclusive scan of the degrees (from deg_off) of a queue's vertices,
+// *degsum = their sum: a frontier's edge layout in another orientation.
+rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t count, const uint32_t* deg_off,
+                          uint32_t* qoff, int64_t* degsum, DevBuf& tmp, cudaStream_t st);
 
 // Hub slots that fit the push kernel's shared-memory budget (elem bytes each).
 uint32_t hub_budget(size_t elem, int64_t n);

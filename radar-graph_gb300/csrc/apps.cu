@@ -280,7 +280,7 @@ __global__ void queue_degrees(const uint32_t* __restrict__ q, int64_t k, const u
   if (j < k) deg[j] = deg_off[q[j] + 1] - deg_off[q[j]];
 }
 
-static rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t count, const uint32_t* deg_off,
+rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t count, const uint32_t* deg_off,
                                  uint32_t* qoff, int64_t* degsum, DevBuf& tmp, cudaStream_t st) {
   if (count == 0) {
     *degsum = 0;

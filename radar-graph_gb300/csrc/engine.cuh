@@ -226,6 +226,46 @@ struct OpBcBwd {
   }
 };
 
+// Multi-source BFS level (rg_bfs_multi, rg_bc_multi): bit q of F[s] says s is
+// in source q's frontier; the bits that reach d for the first time are ORed
+// into N[d] (Radii_F's mask propagation, one bit per source).
+struct OpMsBfs {
+  const unsigned long long* __restrict__ F;
+  const unsigned long long* __restrict__ seen;
+  unsigned long long* N;
+  using HubT = unsigned long long;
+  static constexpr int kPull = kPullOr;
+  static constexpr bool kOutput = true;
+  __device__ __forceinline__ bool cond(uint32_t) const { return true; }
+  __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
+    const unsigned long long w = F[s] & ~seen[d];
+    if (!w) return false;
+    atomicOr(N + d, w);
+    return true;
+  }
+  __device__ static HubT hub_identity() { return 0ull; }
+  __device__ __forceinline__ void hub_push(HubT* hs, uint32_t slot, uint32_t s, uint32_t d) const {
+    const unsigned long long w = F[s] & ~seen[d];
+    if (w) atomicOr(hs + slot, w);
+  }
+  __device__ __forceinline__ bool hub_changes(uint32_t s, uint32_t d) const { return (F[s] & ~seen[d]) != 0; }
+  __device__ __forceinline__ bool hub_merge(uint32_t v, HubT x) const {
+    if (!x) return false;
+    atomicOr(N + v, x);
+    return true;
+  }
+  using PullT = unsigned long long;
+  __device__ static PullT pull_identity() { return 0ull; }
+  __device__ __forceinline__ PullT pull_val(uint32_t u) const { return F[u]; }
+  __device__ static PullT combine(PullT a, PullT b) { return a | b; }
+  __device__ __forceinline__ bool pull_apply(uint32_t v, PullT x) const {
+    const unsigned long long w = x & ~seen[v];
+    if (!w) return false;
+    N[v] |= w;
+    return true;
+  }
+};
+
 // Radii_F (Radii.C:37-106): OR the source's mask into next_visited[d] when it
 // adds bits; d joins the next frontier.  radii[d] = round is written for
 // every member of the next frontier by the compaction that follows (the same

@@ -31,43 +31,6 @@ namespace rg {
 // ---------------------------------------------------------------------------
 namespace {
 
-struct OpMsBfs {
-  const unsigned long long* __restrict__ F;
-  const unsigned long long* __restrict__ seen;
-  unsigned long long* N;
-  using HubT = unsigned long long;
-  static constexpr int kPull = kPullOr;
-  static constexpr bool kOutput = true;
-  __device__ __forceinline__ bool cond(uint32_t) const { return true; }
-  __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
-    const unsigned long long w = F[s] & ~seen[d];
-    if (!w) return false;
-    atomicOr(N + d, w);
-    return true;
-  }
-  __device__ static HubT hub_identity() { return 0ull; }
-  __device__ __forceinline__ void hub_push(HubT* hs, uint32_t slot, uint32_t s, uint32_t d) const {
-    const unsigned long long w = F[s] & ~seen[d];
-    if (w) atomicOr(hs + slot, w);
-  }
-  __device__ __forceinline__ bool hub_changes(uint32_t s, uint32_t d) const { return (F[s] & ~seen[d]) != 0; }
-  __device__ __forceinline__ bool hub_merge(uint32_t v, HubT x) const {
-    if (!x) return false;
-    atomicOr(N + v, x);
-    return true;
-  }
-  using PullT = unsigned long long;
-  __device__ static PullT pull_identity() { return 0ull; }
-  __device__ __forceinline__ PullT pull_val(uint32_t u) const { return F[u]; }
-  __device__ static PullT combine(PullT a, PullT b) { return a | b; }
-  __device__ __forceinline__ bool pull_apply(uint32_t v, PullT x) const {
-    const unsigned long long w = x & ~seen[v];
-    if (!w) return false;
-    N[v] |= w;
-    return true;
-  }
-};
-
 __global__ void ms_clear_frontier(const uint32_t* __restrict__ q, int64_t k, unsigned long long* F) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j < k) F[q[j]] = 0ull;

@@ -101,6 +101,7 @@ _SIGS = {
     "rg_set_option": [C.c_int, C.c_int64],
     "rg_get_option": [C.c_int, _i64p],
     "rg_bfs_multi": [C.c_void_p, _u32p, C.c_int, _i32p, _i64p],
+    "rg_bc_multi": [C.c_void_p, _u32p, C.c_int, _f64p, _i64p],
     "rg_batch_create": [C.c_int, _i64p, _i64p, _P(_u32p), _P(_u32p), C.c_void_p],
     "rg_batch_run": [C.c_void_p, _u32p, C.c_int, C.c_int64, _i32p, _f64p, _i32p, _f64p],
     "rg_batch_free": [C.c_void_p],
@@ -447,6 +448,15 @@ class Graph:
         lv = C.c_int64()
         _check(lib().rg_bc_sources(self._h, _variant(variant), _ptr(s, C.c_uint32), len(s),
                                    _ptr(deps, C.c_double), C.byref(lv)))
+        return deps, lv.value
+
+    def bc_multi(self, sources):
+        """k <= 64 independent single-source BCs in one traversal: (k, n)
+        array, row q = bc_sources([sources[q]]), and the level count."""
+        s = np.ascontiguousarray(sources, np.uint32)
+        deps = np.empty((len(s), self.n), np.float64)
+        lv = C.c_int64()
+        _check(lib().rg_bc_multi(self._h, _ptr(s, C.c_uint32), len(s), _ptr(deps, C.c_double), C.byref(lv)))
         return deps, lv.value
 
     def bc_pick_sources(self, k):
