@@ -376,7 +376,7 @@ def bench_batched(rg, ngraphs=512, k=64, pr_iters=10, plain_graphs=24, seed=7):
 # served stream: 3 resident graphs, Poisson arrivals, BFS 60% / BC 25% / Radii 15%
 # ---------------------------------------------------------------------------
 
-def bench_serving(rg, graphs, rates=(200, 800, 3200), per_rate=300, seed=5, workers=4):
+def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=5, workers=4):
     rng = np.random.default_rng(seed)
 
     def draw(nq):

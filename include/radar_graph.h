@@ -226,6 +226,14 @@ rg_status rg_bfs_multi(rg_graph* g, const uint32_t* h_sources, int k, int32_t* h
 rg_status rg_bc_multi(rg_graph* g, const uint32_t* h_sources, int k, double* h_deps,
                       int64_t* levels_out);
 
+/* nq <= 16 Radii queries in one traversal: query q samples
+ * h_seeds[q*k .. q*k+k) (ORIGINAL ids, k <= 64) and owns word q of a
+ * multi-word mask per vertex, so every gather fetches all queries' masks of
+ * a neighbour.  h_radii: nq*n int32, row q equal to rg_radii_seeds(g, v,
+ * &h_seeds[q*k], k, row) for every variant (Radii.C:140-218 per word). */
+rg_status rg_radii_multi(rg_graph* g, const uint32_t* h_seeds, int k, int nq, int32_t* h_radii,
+                         int64_t* rounds_out);
+
 /* A set of graphs resident on the device, run by one persistent kernel. */
 typedef struct rg_batch rg_batch;
 /* Symmetric CSRs (h_offs[i]: ns[i]+1 entries, h_adjs[i]: ms[i]). */
@@ -244,10 +252,13 @@ rg_status rg_batch_free(rg_batch* b);
 /* ------------------------------------------------------------------------
  * Serving: a request loop over resident graphs (no counterpart in the
  * reference).  Worker threads, each with its own stream, run queries as they
- * arrive; BFS queries waiting for the same graph are coalesced (up to
- * max_batch <= 64) into one multi-source traversal; a batch is admitted when
- * its estimated device memory fits hbm_fraction of the HBM free at start.
- * Results equal the single-query entry points:
+ * arrive; BFS queries, and BC queries, waiting for the same graph are
+ * coalesced (up to max_batch <= 64) into one multi-source traversal
+ * (rg_bfs_multi / rg_bc_multi) when the batch reaches the size at which that
+ * beats one traversal per query (measured per graph at creation); a batch is
+ * admitted when its estimated device memory fits hbm_fraction of the HBM free
+ * at start.  Results equal the single-query entry points (BC within 1e-9
+ * relative):
  *   RG_QUERY_BFS   source = root (ORIGINAL id) -> int32[n] depths (rg_bfs)
  *   RG_QUERY_BC    source = BC source           -> double[n] (rg_bc_sources
  *                  with that one source)

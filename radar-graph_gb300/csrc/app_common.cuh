@@ -64,6 +64,11 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
 // may be null) receive k rows of n doubles in original-id order (bc_multi.cu).
 rg_status bc_multi_run(rg_graph* g, const uint32_t* src_orig, int k, double* h_out, double* d_out,
                        int64_t* levels_out);
+// nq <= 16 Radii queries of k seeds each (seeds[q*k + i], ORIGINAL ids) in one
+// traversal; h_radii / d_radii_out (either may be null): nq rows of n int32 in
+// original-id order (radii_multi.cu).
+rg_status radii_multi_run(rg_graph* g, const uint32_t* seeds_orig, int k, int nq, int32_t* h_radii,
+                          int32_t* d_radii_out, int64_t* rounds_out);
 // qoff = exclusive scan of the degrees (from deg_off) of a queue's vertices,
 // *degsum = their sum: a frontier's edge layout in another orientation.
 rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t count, const uint32_t* deg_off,

@@ -1,0 +1,354 @@
+// Many Radii queries in one traversal: query q (its own <= 64 sample
+// vertices) owns word q of a W-word mask per vertex, W = the query count
+// rounded up to a power of two (<= 16).  A round propagates all words at
+// once -- sparse rounds push over the union frontier with the engine's
+// edge-balanced push, dense rounds pull every vertex's neighbour masks with
+// an edge-balanced sweep, so one gather fetches all W words of a neighbour
+// -- and radii[q][v] = round wherever word q of v changed (Radii.C:37-106,
+// 140-218, applied per word).
+//
+// Each query's result equals its own single-query run: a vertex is in the
+// union frontier when any word changed, and pushing a word that did not
+// change adds nothing, because that word was pushed to every neighbour in the
+// round it last changed.  The same argument lets the dense rounds skip the
+// frontier test (as the single-query dense rounds do).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "app_common.cuh"
+
+namespace rg {
+namespace {
+
+// Radii_F on W words: every word of s that adds bits to d is ORed into
+// next[d]; d joins the next frontier when any word grew.
+struct OpRadiiW {
+  const unsigned long long* __restrict__ vis;
+  unsigned long long* nvis;
+  int W;
+  using HubT = unsigned long long;  // no hub copies: the push runs without them
+  static constexpr bool kOutput = true;
+  __device__ __forceinline__ bool cond(uint32_t) const { return true; }
+  __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
+    bool grew = false;
+    for (int w = 0; w < W; w++) {
+      const unsigned long long x = vis[(size_t)s * W + w] & ~vis[(size_t)d * W + w];
+      if (x) {
+        atomicOr(nvis + (size_t)d * W + w, x);
+        grew = true;
+      }
+    }
+    return grew;
+  }
+  __device__ static HubT hub_identity() { return 0ull; }
+  __device__ __forceinline__ void hub_push(HubT*, uint32_t, uint32_t, uint32_t) const {}
+  __device__ __forceinline__ bool hub_merge(uint32_t, HubT) const { return false; }
+};
+
+__global__ void rq_seed(const uint32_t* __restrict__ v, const unsigned long long* __restrict__ mask,
+                        const int* __restrict__ word, int k, int W, int64_t n, unsigned long long* nvis,
+                        int32_t* radii) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) {
+    nvis[(size_t)v[j] * W + word[j]] = mask[j];
+    radii[(int64_t)word[j] * n + v[j]] = 0;
+  }
+}
+
+// Start of a round: the frontier's masks become current (vertexMap
+// Radii_Vertex_F, Radii.C:78-86).
+__global__ void rq_sync(const uint32_t* __restrict__ q, int64_t count, int W, unsigned long long* vis,
+                        const unsigned long long* __restrict__ nvis) {
+  const int64_t total = count * W;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i / W;
+    const size_t e = (size_t)q[j] * W + (i - j * W);
+    vis[e] = nvis[e];
+  }
+}
+
+// radii[w][v] = round for every word that grew at a new frontier vertex.
+__global__ void rq_mark(const uint32_t* __restrict__ q, int64_t count, int W, int nq, int64_t n,
+                        const unsigned long long* __restrict__ vis, const unsigned long long* __restrict__ nvis,
+                        int32_t* radii, int32_t round) {
+  const int64_t total = count * W;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i / W;
+    const int w = (int)(i - j * W);
+    if (w >= nq) continue;
+    const uint32_t v = q[j];
+    const size_t e = (size_t)v * W + w;
+    if (nvis[e] != vis[e]) radii[(int64_t)w * n + v] = round;
+  }
+}
+
+// One vertex's W mask words with as few requests as possible: gathers are
+// bound by the L1TEX request rate, not by bytes, so a 32-byte row costs one
+// 256-bit load rather than four 64-bit ones.  Rows are W*8-byte aligned.
+template <int W>
+__device__ __forceinline__ void load_row(const unsigned long long* p, unsigned long long (&x)[W]) {
+  if constexpr (W == 1) {
+    x[0] = __ldg(p);
+  } else if constexpr (W == 2) {
+    const ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p));
+    x[0] = t.x;
+    x[1] = t.y;
+  } else {
+#pragma unroll
+    for (int b = 0; b < W; b += 4) {
+      uint32_t r[8];
+      asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+          : "l"(p + b));
+#pragma unroll
+      for (int h = 0; h < 4; h++) x[b + h] = ((unsigned long long)r[2 * h + 1] << 32) | r[2 * h];
+    }
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void rq_flush(const unsigned long long* __restrict__ vis, unsigned long long* nvis,
+                                         uint32_t* next_bits, uint32_t row, const unsigned long long (&part)[W]) {
+  bool grew = false;
+#pragma unroll
+  for (int w = 0; w < W; w++) {
+    if (!part[w]) continue;
+    const unsigned long long x = part[w] & ~__ldg(vis + (size_t)row * W + w);
+    if (x) {
+      atomicOr(nvis + (size_t)row * W + w, x);
+      grew = true;
+    }
+  }
+  if (grew) bit_set(next_bits, row);
+}
+
+// Dense round, W words: next[v] |= (OR of vis[u] over every neighbour u) &
+// ~vis[v] per word.  Edge-balanced like mask_pull_sweep: a warp takes a
+// 512-edge chunk, kItems edges per lane, row pieces combined by a segmented
+// OR scan, one flush per row piece.
+template <int W, int kItems>
+__global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
+                                                     uint32_t nchunks, const unsigned long long* __restrict__ vis,
+                                                     unsigned long long* nvis, uint32_t* next_bits) {
+  constexpr int kStep = 32 * kItems;
+  static_assert(kSweepChunk % kStep == 0, "chunk must hold whole steps");
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = warp; c < nchunks; c += nwarps) {
+    const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
+    for (int r = 0; r < kSweepChunk / kStep; r++) {
+      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
+      uint32_t row = kNone;
+      unsigned long long part[W];
+#pragma unroll
+      for (int w = 0; w < W; w++) part[w] = 0ull;
+      if (e < g.m) {
+        uint32_t v = upper_index(g.off, vlo, vhi, e);
+        uint32_t nxt = g.off[v + 1];
+        uint32_t u[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) u[i] = (e + i < g.m) ? g.adj[e + i] : 0u;
+        unsigned long long x[kItems][W];
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+          if (e + i < g.m) {
+            load_row<W>(vis + (size_t)u[i] * W, x[i]);
+          } else {
+#pragma unroll
+            for (int w = 0; w < W; w++) x[i][w] = 0ull;
+          }
+        }
+        row = v;
+#pragma unroll
+        for (int i = 0; i < kItems; i++) {
+          const uint32_t ee = e + i;
+          if (ee >= g.m) break;
+          if (ee >= nxt) {  // a row piece that ends in this lane
+            rq_flush<W>(vis, nvis, next_bits, row, part);
+#pragma unroll
+            for (int w = 0; w < W; w++) part[w] = 0ull;
+            do {
+              v++;
+              nxt = g.off[v + 1];
+            } while (ee >= nxt);
+            row = v;
+          }
+#pragma unroll
+          for (int w = 0; w < W; w++) part[w] |= x[i][w];
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          const unsigned long long t = __shfl_up_sync(0xffffffffu, part[w], o);
+          if (lane >= o && tr == row) part[w] |= t;
+        }
+      }
+      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
+      if (row != kNone && (lane == 31 || next_row != row)) rq_flush<W>(vis, nvis, next_bits, row, part);
+    }
+  }
+}
+
+template <int W>
+rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned long long* nvis, uint32_t* bits,
+                          cudaStream_t st) {
+  constexpr int kItems = W <= 2 ? 8 : 16 / W;  // about 16 mask words in flight per lane
+  auto kern = rq_pull_sweep<W, kItems>;
+  static int per_sm = 0;
+  if (!per_sm) {
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    per_sm = std::max(per_sm, 1);
+  }
+  const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
+  kt_begin(st);
+  kern<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(), (uint32_t)g->nchunks, vis,
+                                                             nvis, bits);
+  kt_end(st);
+  RG_CUDA(cudaGetLastError());
+  g_timing.kernel_launches++;
+  g_timing.edge_launches++;
+  return RG_OK;
+}
+
+rg_status rq_sweep(int W, rg_graph* g, const unsigned long long* vis, unsigned long long* nvis, uint32_t* bits,
+                   cudaStream_t st) {
+  switch (W) {
+    case 1: return launch_rq_sweep<1>(g, vis, nvis, bits, st);
+    case 2: return launch_rq_sweep<2>(g, vis, nvis, bits, st);
+    case 4: return launch_rq_sweep<4>(g, vis, nvis, bits, st);
+    case 8: return launch_rq_sweep<8>(g, vis, nvis, bits, st);
+    default: return launch_rq_sweep<16>(g, vis, nvis, bits, st);
+  }
+}
+
+inline unsigned grid_for(int64_t items) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((items + 255) / 256, (int64_t)device_sms() * 32));
+}
+
+}  // namespace
+
+rg_status radii_multi_run(rg_graph* g, const uint32_t* seeds_orig, int k, int nq, int32_t* h_radii,
+                          int32_t* d_radii_out, int64_t* rounds_out) {
+  if (!g) return fail(RG_EINVAL, "null graph");
+  if (nq < 1 || nq > 16) return fail(RG_EINVAL, "need 1..16 queries");
+  if (k < 0 || k > 64 || (k > 0 && !seeds_orig)) return fail(RG_EINVAL, "need 0..64 seeds per query");
+  OptScope opt_scope(g, kAppRadii);
+  Ctx* cx = nullptr;
+  RG_TRY(get_ctx(&cx));
+  cudaStream_t st = cx->stream;
+  const int64_t n = g->n;
+  int W = 1;
+  while (W < nq) W *= 2;
+  // per query: seeding loop (Radii.C:162-169), NextVisited[v] = 1<<i is a
+  // plain store, so on a collision the largest i wins
+  std::vector<uint32_t> all(k * (size_t)nq), sv, frontier;
+  std::vector<unsigned long long> sm;
+  std::vector<int> sw;
+  RG_TRY(lookup_ids(g, seeds_orig, (int64_t)k * nq, true, all.data(), nullptr));
+  for (int q = 0; q < nq; q++) {
+    const size_t first = sv.size();
+    for (int i = 0; i < k; i++) {
+      const uint32_t v = all[(size_t)q * k + i];
+      auto it = std::find(sv.begin() + first, sv.end(), v);
+      if (it == sv.end()) {
+        sv.push_back(v);
+        sm.push_back(1ull << i);
+        sw.push_back(q);
+      } else {
+        sm[it - sv.begin()] = 1ull << i;
+      }
+    }
+  }
+  frontier = sv;
+  std::sort(frontier.begin(), frontier.end());
+  frontier.erase(std::unique(frontier.begin(), frontier.end()), frontier.end());
+  DevBuf vis(true, st), nvis(true, st), radii(true, st), seedv(true, st), seedm(true, st), seedw(true, st),
+      out(true, st);
+  Frontier f[2];
+  RG_TRY(vis.reserve(8 * (size_t)n * W));
+  RG_TRY(nvis.reserve(8 * (size_t)n * W));
+  RG_TRY(radii.reserve(4 * (size_t)n * nq));
+  RG_TRY(frontier_alloc(g, f[0]));
+  RG_TRY(frontier_alloc(g, f[1]));
+  CallTimer timer(g);
+  unsigned long long* pv = vis.as<unsigned long long>();
+  unsigned long long* pn = nvis.as<unsigned long long>();
+  int32_t* pr = radii.as<int32_t>();
+  RG_CUDA(cudaMemsetAsync(pv, 0, 8 * (size_t)n * W, st));
+  RG_CUDA(cudaMemsetAsync(pn, 0, 8 * (size_t)n * W, st));
+  RG_CUDA(cudaMemsetAsync(pr, 0xFF, 4 * (size_t)n * nq, st));
+  if (!sv.empty()) {
+    RG_TRY(seedv.reserve(4 * sv.size()));
+    RG_TRY(seedm.reserve(8 * sm.size()));
+    RG_TRY(seedw.reserve(4 * sw.size()));
+    RG_CUDA(cudaMemcpyAsync(seedv.p, sv.data(), 4 * sv.size(), cudaMemcpyHostToDevice, st));
+    RG_CUDA(cudaMemcpyAsync(seedm.p, sm.data(), 8 * sm.size(), cudaMemcpyHostToDevice, st));
+    RG_CUDA(cudaMemcpyAsync(seedw.p, sw.data(), 4 * sw.size(), cudaMemcpyHostToDevice, st));
+    rq_seed<<<(unsigned)((sv.size() + 255) / 256), 256, 0, st>>>(seedv.as<uint32_t>(), seedm.as<unsigned long long>(),
+                                                               seedw.as<int>(), (int)sv.size(), W, n, pn, pr);
+    g_timing.kernel_launches++;
+  }
+  RG_TRY(frontier_from_host(g, f[0], frontier.data(), (int64_t)frontier.size(), st));
+  FView cur = view_of(f[0]), nxt = view_of(f[1]);
+  const int64_t nwords = (n + 31) / 32;
+  const int64_t threshold = g->m / std::max<int64_t>(g_opts.dense_div, 1);
+  int32_t round = 0;
+  while (cur.count > 0) {
+    round++;
+    rq_sync<<<grid_for(cur.count * W), 256, 0, st>>>(cur.queue, cur.count, W, pv, pn);
+    g_timing.kernel_launches++;
+    RG_CUDA(cudaMemsetAsync(nxt.bits, 0, 4 * nwords, st));
+    if (cur.degsum > 0) {
+      g_timing.edges_traversed += cur.degsum;
+      if (cur.count + cur.degsum > threshold) {
+        RG_TRY(rq_sweep(W, g, pv, pn, nxt.bits, st));
+      } else {
+        RG_TRY(launch_push<OpRadiiW, kHubNone>(g, g->view(), cur, OpRadiiW{pv, pn, W}, HubInfo{}, nxt.bits, st));
+      }
+    }
+    Frontier shell;  // non-owning view of nxt for the compaction
+    shell.bits.p = nxt.bits;
+    RG_TRY(compact_bits(g, shell, st, true, nullptr, 0, nullptr, nxt.queue, nxt.qoff));
+    shell.bits.p = nullptr;
+    nxt.count = shell.count;
+    nxt.degsum = shell.degsum;
+    g_timing.kernel_launches += 3;
+    if (nxt.count > 0) {
+      rq_mark<<<grid_for(nxt.count * W), 256, 0, st>>>(nxt.queue, nxt.count, W, nq, n, pv, pn, pr, round);
+      g_timing.kernel_launches++;
+    }
+    RG_CUDA(cudaGetLastError());
+    std::swap(cur, nxt);
+  }
+  RG_TRY(timer.stop());
+  const int32_t* res = pr;
+  if (g->sorted) {  // rows in original-id order
+    RG_TRY(out.reserve(4 * (size_t)n * nq));
+    for (int q = 0; q < nq; q++) {
+      gather_kernel<int32_t><<<grid_for(n), 256, 0, st>>>(pr + (size_t)q * n, g->new_ids.as<uint32_t>(), n,
+                                                          out.as<int32_t>() + (size_t)q * n);
+    }
+    RG_CUDA(cudaGetLastError());
+    res = out.as<int32_t>();
+  }
+  if (d_radii_out) RG_CUDA(cudaMemcpyAsync(d_radii_out, res, 4 * (size_t)n * nq, cudaMemcpyDeviceToDevice, st));
+  if (h_radii) RG_CUDA(cudaMemcpyAsync(h_radii, res, 4 * (size_t)n * nq, cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  g_timing.algorithmic_bytes = (4 + 8 * W) * g_timing.edges_traversed + (int64_t)(16 * W + 4 * nq) * n;
+  if (rounds_out) *rounds_out = round;
+  return RG_OK;
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_radii_multi(rg_graph* g, const uint32_t* h_seeds, int k, int nq, int32_t* h_radii,
+                                    int64_t* rounds_out) {
+  return rg::radii_multi_run(g, h_seeds, k, nq, h_radii, nullptr, rounds_out);
+}

@@ -12,8 +12,14 @@
 //    runs as single-source traversals instead, so light load costs no more
 //    than one query per launch;
 //  * a Radii query (64 seeded sample vertices) is one 64-bit mask traversal
-//    (Radii.C), the same run as rg_radii_seeds;
-//  * a BC query (one source) runs BC-manyiter-v2's forward/backward phases.
+//    (Radii.C), the same run as rg_radii_seeds; up to 8 waiting on the same
+//    graph run as one traversal with one mask word per query
+//    (rg_radii_multi);
+//  * BC queries waiting for the same graph are coalesced the same way into one
+//    multi-source BC (rg_bc_multi: levels from one bitmask BFS, path counts
+//    and dependencies for every source per level); below the graph's BC
+//    break-even size (measured at start-up from two batch sizes against one
+//    single-source BC) each runs BC-manyiter-v2's single-source pass.
 // Results stay in device memory (stream-ordered allocations) until the client
 // fetches them with rg_server_wait, which copies one query's array straight
 // into the client's buffer.  A batch is admitted only when its working set
@@ -42,6 +48,10 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// Radii queries per shared traversal: beyond 8 mask words per vertex the
+// masks of a large graph no longer stay in L2 and the per-query cost rises.
+constexpr int kRadiiBatch = 8;
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(Clock::now().time_since_epoch()).count();
@@ -76,6 +86,7 @@ struct Result {
 struct rg_server {
   std::vector<rg_graph*> graphs;
   std::vector<int> bfs_breakeven;  // per graph: smallest batch worth a multi-source traversal
+  std::vector<int> bc_breakeven;   // the same for BC
   int device = 0;
   int max_batch = 64;
   size_t hbm_budget = 0, hbm_in_use = 0;
@@ -108,7 +119,7 @@ int radii_seeds(uint64_t seed, int64_t n, uint32_t* out) {
 
 size_t result_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
-  return kind == RG_QUERY_BFS ? 4 * n * k : kind == RG_QUERY_BC ? 8 * n : 4 * n;
+  return kind == RG_QUERY_BC ? 8 * n * k : 4 * n * k;
 }
 
 // Break-even batch size for one graph: time one single-source BFS and one
@@ -136,10 +147,44 @@ rg_status calibrate_bfs(rg_graph* g, int* breakeven) {
   return RG_OK;
 }
 
+// BC break-even: one single-source pass against multi-source passes of 2 and
+// 16 sources (cost ~ a + b k); the smallest k with a + b k < k * single.
+rg_status calibrate_bc(rg_graph* g, int* breakeven) {
+  using namespace rg;
+  const int64_t n = g->n;
+  std::vector<uint32_t> src(16);
+  RG_TRY(bc_pick(g, 16, src.data()));
+  DevBuf out;
+  RG_TRY(out.reserve(8 * (size_t)n * 16));
+  const int variant = g->sorted ? RG_DEGSORT : RG_PUSH;
+  double t1 = 0, t2 = 0, t16 = 0;
+  for (int rep = 0; rep < 2; rep++) {
+    auto a = Clock::now();
+    RG_TRY(bc_run(g, variant, src.data(), 1, nullptr, nullptr, 0, out.as<double>()));
+    RG_CUDA(cudaStreamSynchronize(ctx().stream));
+    auto b = Clock::now();
+    RG_TRY(bc_multi_run(g, src.data(), 2, nullptr, out.as<double>(), nullptr));
+    auto c = Clock::now();
+    RG_TRY(bc_multi_run(g, src.data(), 16, nullptr, out.as<double>(), nullptr));
+    auto d = Clock::now();
+    t1 = std::chrono::duration<double>(b - a).count();
+    t2 = std::chrono::duration<double>(c - b).count();
+    t16 = std::chrono::duration<double>(d - c).count();
+  }
+  const double per = std::max(0.0, (t16 - t2) / 14.0), fixed = std::max(0.0, t2 - 2 * per);
+  *breakeven = t1 > per ? (int)std::min(65.0, std::max(2.0, std::floor(fixed / (t1 - per)) + 1)) : 65;
+  return RG_OK;
+}
+
 size_t working_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
-  if (kind == RG_QUERY_BC) return 64 * n;
-  if (kind == RG_QUERY_RADII) return 40 * n;  // two masks, radii, two frontiers
+  // multi-source BC: two rows of ceil4(k) columns, the level store, masks and frontiers
+  if (kind == RG_QUERY_BC) return k > 1 ? (size_t)(16 * ((k + 3) & ~3) + 112) * n : 64 * n;
+  if (kind == RG_QUERY_RADII) {  // two mask rows of W words, radii rows and their copy, two frontiers
+    int W = 1;
+    while (W < k) W *= 2;
+    return (size_t)(16 * W + 8 * k + 40) * n;
+  }
   return (size_t)(8 * k + 40) * n;  // masks, depth rows and their original-order copy, two frontiers
 }
 
@@ -158,9 +203,10 @@ void worker_main(rg_server* S) {
       const Query q0 = S->pending.front();
       S->pending.pop_front();
       batch.push_back(q0);
-      if (q0.kind == RG_QUERY_BFS) {  // coalesce waiting BFS queries on the same graph
-        for (auto it = S->pending.begin(); it != S->pending.end() && (int)batch.size() < S->max_batch;) {
-          if (it->kind == RG_QUERY_BFS && it->graph == q0.graph) {
+      {  // coalesce waiting queries of the same kind on the same graph
+        const int cap = q0.kind == RG_QUERY_RADII ? std::min(S->max_batch, kRadiiBatch) : S->max_batch;
+        for (auto it = S->pending.begin(); it != S->pending.end() && (int)batch.size() < cap;) {
+          if (it->kind == q0.kind && it->graph == q0.graph) {
             batch.push_back(*it);
             it = S->pending.erase(it);
           } else {
@@ -169,7 +215,7 @@ void worker_main(rg_server* S) {
         }
       }
       const rg_graph* g = S->graphs[q0.graph];
-      const int k = q0.kind == RG_QUERY_BFS ? (int)batch.size() : 64;
+      const int k = (int)batch.size();
       work = working_bytes(g, q0.kind, k);
       res = result_bytes(g, q0.kind, k);
       // admission by free HBM: wait while running batches and unfetched
@@ -185,8 +231,10 @@ void worker_main(rg_server* S) {
     auto block = std::make_shared<Block>();
     block->bytes = res;
     rg_status status = cx ? RG_OK : RG_ENODEV;
-    // BFS batches below the graph's break-even size run query by query
-    const bool multi = kind == RG_QUERY_BFS && (int)batch.size() >= S->bfs_breakeven[batch[0].graph];
+    // BFS and BC batches below the graph's break-even size run query by query
+    const bool multi = (kind == RG_QUERY_BFS && (int)batch.size() >= S->bfs_breakeven[batch[0].graph]) ||
+                       (kind == RG_QUERY_BC && (int)batch.size() >= S->bc_breakeven[batch[0].graph]) ||
+                       (kind == RG_QUERY_RADII && batch.size() >= 2);
     if (status == RG_OK && cudaMallocAsync(&block->p, res, st) != cudaSuccess) {
       cudaGetLastError();
       status = fail(RG_ENOMEM, "server: result allocation of %zu bytes failed", res);
@@ -205,14 +253,28 @@ void worker_main(rg_server* S) {
           status = rg::bfs_multi_run(g, src.data(), k, nullptr, nullptr, static_cast<int32_t*>(block->p));
         }
       } else if (kind == RG_QUERY_RADII) {
-        src.resize(64);
-        const int k = radii_seeds(batch[0].source, n, src.data());
-        status = rg::radii_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, src.data(), k, nullptr, nullptr, 0,
-                               static_cast<int32_t*>(block->p));
+        const int nq = (int)batch.size();
+        const int k = (int)std::min<int64_t>(n, 64);  // samples per query
+        src.resize((size_t)k * nq);
+        for (int i = 0; i < nq; i++) radii_seeds(batch[i].source, n, src.data() + (size_t)i * k);
+        if (multi) {
+          status = rg::radii_multi_run(g, src.data(), k, nq, nullptr, static_cast<int32_t*>(block->p), nullptr);
+        } else {
+          status = rg::radii_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, src.data(), k, nullptr, nullptr, 0,
+                                 static_cast<int32_t*>(block->p));
+        }
       } else {
-        const uint32_t s = batch[0].source;
-        status = rg::bc_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, &s, 1, nullptr, nullptr, 0,
-                            static_cast<double*>(block->p));
+        const int k = (int)batch.size();
+        src.resize(k);
+        for (int i = 0; i < k; i++) src[i] = batch[i].source;
+        if (multi) {
+          status = rg::bc_multi_run(g, src.data(), k, nullptr, static_cast<double*>(block->p), nullptr);
+        } else {
+          for (int i = 0; i < k && status == RG_OK; i++) {
+            status = rg::bc_run(g, g->sorted ? RG_DEGSORT : RG_PUSH, &src[i], 1, nullptr, nullptr, 0,
+                                static_cast<double*>(block->p) + (size_t)i * (size_t)n);
+          }
+        }
       }
       // the result is complete before any client (on another stream) copies it
       if (status == RG_OK) {
@@ -226,7 +288,7 @@ void worker_main(rg_server* S) {
       S->hbm_in_use -= work;
       if (status != RG_OK) S->hbm_in_use -= res;
       S->running--;
-      if (kind == RG_QUERY_BFS && !multi) {
+      if (!multi) {
         S->launches += (int64_t)batch.size();
       } else {
         S->launches++;
@@ -281,8 +343,10 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
   RG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   S->hbm_budget = (size_t)(hbm_fraction * (double)free_b);
   S->bfs_breakeven.assign(ngraphs, 1);
+  S->bc_breakeven.assign(ngraphs, 2);
   for (int i = 0; i < ngraphs; i++) {
-    const rg_status cs = calibrate_bfs(S->graphs[i], &S->bfs_breakeven[i]);
+    rg_status cs = calibrate_bfs(S->graphs[i], &S->bfs_breakeven[i]);
+    if (cs == RG_OK && S->graphs[i]->m > 0) cs = calibrate_bc(S->graphs[i], &S->bc_breakeven[i]);
     if (cs != RG_OK) {
       delete S;
       return cs;

@@ -102,6 +102,7 @@ _SIGS = {
     "rg_get_option": [C.c_int, _i64p],
     "rg_bfs_multi": [C.c_void_p, _u32p, C.c_int, _i32p, _i64p],
     "rg_bc_multi": [C.c_void_p, _u32p, C.c_int, _f64p, _i64p],
+    "rg_radii_multi": [C.c_void_p, _u32p, C.c_int, C.c_int, _i32p, _i64p],
     "rg_batch_create": [C.c_int, _i64p, _i64p, _P(_u32p), _P(_u32p), C.c_void_p],
     "rg_batch_run": [C.c_void_p, _u32p, C.c_int, C.c_int64, _i32p, _f64p, _i32p, _f64p],
     "rg_batch_free": [C.c_void_p],
@@ -458,6 +459,19 @@ class Graph:
         lv = C.c_int64()
         _check(lib().rg_bc_multi(self._h, _ptr(s, C.c_uint32), len(s), _ptr(deps, C.c_double), C.byref(lv)))
         return deps, lv.value
+
+    def radii_multi(self, seeds):
+        """nq <= 16 Radii queries in one traversal; seeds: (nq, k) array of
+        sample vertices.  Returns (nq, n) radii (row q = radii_seeds(seeds[q]))
+        and the round count."""
+        s = np.ascontiguousarray(seeds, np.uint32)
+        if s.ndim != 2:
+            raise ValueError("seeds must be (queries, samples)")
+        r = np.empty((s.shape[0], self.n), np.int32)
+        rounds = C.c_int64()
+        _check(lib().rg_radii_multi(self._h, _ptr(s, C.c_uint32), s.shape[1], s.shape[0], _ptr(r, C.c_int32),
+                                    C.byref(rounds)))
+        return r, rounds.value
 
     def bc_pick_sources(self, k):
         out = np.empty(k, np.uint32)

@@ -89,3 +89,27 @@ def test_bad_queries_are_errors(graphs):
             S.submit(5, "bfs", 0)
         with pytest.raises(rg.RgError):
             S.submit(0, "bfs", 10**9)
+
+
+def test_bc_queries_are_coalesced(graphs):
+    G = graphs[1]
+    srcs = list(range(3, 3 + 40 * 97, 97))
+    with rg.Server([G], workers=1, max_batch=64) as S:
+        tickets = [S.submit(0, "bc", s) for s in srcs]
+        outs = [S.wait(t, 0, "bc")[0] for t in tickets]
+        st = S.stats()
+    assert st["launches"] < len(tickets) and st["batched"] > 0
+    for s, got in zip(srcs, outs):
+        assert_close(got, _alone(G, "bc", s), what=f"bc s{s}")
+
+
+def test_radii_queries_are_coalesced(graphs):
+    G = graphs[0]
+    seeds = list(range(40))
+    with rg.Server([G], workers=1, max_batch=64) as S:
+        tickets = [S.submit(0, "radii", s) for s in seeds]
+        outs = [S.wait(t, 0, "radii")[0] for t in tickets]
+        st = S.stats()
+    assert st["launches"] < len(tickets) and st["batched"] > 0
+    for s, got in zip(seeds, outs):
+        assert np.array_equal(got, _alone(G, "radii", s)), s
