@@ -282,6 +282,44 @@ def bench_directed(rg, scale, with_cpu, ef=16, seed=1, reps=3):
     return out
 
 
+def bench_batched_sources(rg, gs, reps=2, plain_sample=8):
+    """Many sources on one resident graph per traversal (rg_bfs_multi,
+    rg_bc_multi, rg_radii_multi) against one query per launch: queries/s of
+    each, the plain side timed on `plain_sample` queries, results compared."""
+    n = gs.n
+    out = {}
+    cases = {
+        "bfs": (64, lambda s: gs.bfs_multi(s), lambda s: gs.bfs("radar", int(s))[1]),
+        "bc": (64, lambda s: gs.bc_multi(s), lambda s: gs.bc_sources(np.array([s], np.uint32), "radar")[0]),
+        "radii": (8, lambda s: gs.radii_multi(s), lambda s: gs.radii_seeds(s, "radar")[0]),
+    }
+    for kind, (k, multi, single) in cases.items():
+        if kind == "radii":
+            src = np.stack([rg.radii_query_seeds(q, n) for q in range(k)])
+        else:
+            src = gs.bc_pick_sources(k)
+        multi(src)
+        ms = []
+        for _ in range(reps):
+            rows = multi(src)[0]
+            ms.append(rg.last_timing()["total_ms"])
+        single(src[0])
+        t_plain, ok = 0.0, True
+        for q in range(plain_sample):
+            want = single(src[q])
+            t_plain += rg.last_timing()["total_ms"]
+            if kind == "bc":
+                ok &= bool(np.array_equal(np.isnan(rows[q]), np.isnan(want)) and np.allclose(
+                    rows[q][~np.isnan(want)], want[~np.isnan(want)], rtol=1e-9, atol=0))
+            else:
+                ok &= bool(np.array_equal(rows[q], want))
+        qps, plain_qps = k / (min(ms) / 1e3), plain_sample / (t_plain / 1e3)
+        out[kind] = {"per_traversal": k, "ms": round(min(ms), 2), "queries_per_s": round(qps, 1),
+                     "plain_queries_per_s": round(plain_qps, 1), "speedup_vs_plain": round(qps / plain_qps, 2),
+                     "identical_results": ok}
+    return out
+
+
 def make_graph(rg, scale, ef, seed, uniform=False):
     src, dst = rg.generate_edges(scale, ef, seed, uniform)
     return rg.csr_from_edges(1 << scale, src, dst)
@@ -652,6 +690,7 @@ def main():
         extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
         extra["directed"] = bench_directed(rg, args.scale, world == 1 and not args.no_cpu)
         extra["batched"] = bench_batched(rg)
+        extra["batched_sources"] = bench_batched_sources(rg, gs)
         gsv = []
         for sc in (20, 22):
             o2, a2 = make_graph(rg, sc, 16, 1)
