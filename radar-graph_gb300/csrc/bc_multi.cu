@@ -135,8 +135,8 @@ constexpr unsigned kFull = 0xffffffffu;
 // 128 at a time: lane l stages queue entry jc + l (start offset, vertex,
 // mask, adjacency base), every lane finds the entries owning its four edges
 // by a shuffle search over those starts and loads the four neighbours and
-// their masks; then each lane walks its four edges' sources together, one
-// source of each per step, so four row loads are in flight per lane.
+// their masks; then each lane walks its four edges' sources together, two
+// sources of each per step, so eight row loads are in flight per lane.
 // Forward: the largest value pushed goes to *vmax (the overflow bound).
 template <class T>
 __global__ void __launch_bounds__(256) rows_push(DevGraph g, const uint32_t* __restrict__ queue,
@@ -188,21 +188,22 @@ __global__ void __launch_bounds__(256) rows_push(DevGraph g, const uint32_t* __r
         if (b[i]) b[i] &= lmask[x[i]];
       }
       while (b[0] | b[1] | b[2] | b[3]) {
-        int q[kStage];
-        T val[kStage];
+        int q[2 * kStage];
+        T val[2 * kStage];
 #pragma unroll
-        for (int i = 0; i < kStage; i++) {
+        for (int i = 0; i < 2 * kStage; i++) {
+          unsigned long long& bi = b[i % kStage];
           q[i] = -1;
-          if (b[i]) {
-            q[i] = __ffsll((long long)b[i]) - 1;
-            b[i] &= b[i] - 1;
-            val[i] = rows[(size_t)u[i] * kk + q[i]];
+          if (bi) {
+            q[i] = __ffsll((long long)bi) - 1;
+            bi &= bi - 1;
+            val[i] = rows[(size_t)u[i % kStage] * kk + q[i]];
           }
         }
 #pragma unroll
-        for (int i = 0; i < kStage; i++) {
+        for (int i = 0; i < 2 * kStage; i++) {
           if (q[i] >= 0) {
-            atomicAdd(rows + (size_t)x[i] * kk + q[i], val[i]);
+            atomicAdd(rows + (size_t)x[i % kStage] * kk + q[i], val[i]);
             if constexpr (std::is_same<T, unsigned long long>::value) mx = max(mx, val[i]);
           }
         }
