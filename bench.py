@@ -44,6 +44,7 @@ sys.path.insert(0, os.path.join(ROOT, "radar-graph_gb300"))
 
 METRIC = "GTEPS + % HBM roofline per app (RMAT s24); batched queries/s, p50/p99 vs plain"
 APPS = ("pagerank", "bfs", "bc", "radii")
+EXTRA_LEGS = ("graph_build", "triangles", "directed", "batched", "batched_sources", "serving")
 
 
 def peaks():
@@ -95,9 +96,11 @@ class Clocks:
 
 
 def cuda_profiler(on):
-    """Marks the timed region for a profiler started with --profile-from-start
-    off (cudaProfilerStart/Stop of the CUDA runtime the library loaded); a
-    no-op when no profiler is attached."""
+    """Marks the profiled ranges -- the timed step, and the extra legs -- for
+    a profiler started with --profile-from-start off (cudaProfilerStart/Stop
+    of the CUDA runtime the library loaded); a profiler started from the
+    start stops at the end of the timed step unless the extra legs reopen
+    it.  A no-op when no profiler is attached."""
     for name in ("libcudart.so.13", "libcudart.so"):
         try:
             rt = ctypes.CDLL(name)
@@ -576,6 +579,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--only", default="", help="comma list of extra legs to run (default all): " + ",".join(EXTRA_LEGS))
     ap.add_argument("--cpu-pr-iters", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -685,21 +689,30 @@ def main():
                                "rounds": prd_rounds,
                                "hbm_frac_of_measured": round(prd["bytes"] / (prd_ms / 1e3) / 1e9 / hbm, 4),
                                "variant": "radar", "max_iters": 100}
+    legs = set(args.only.split(",")) if args.only else set(EXTRA_LEGS)
     if rank == 0 and not args.no_extra:
-        extra["graph_build"] = bench_input(rg, args.scale)
-        extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
-        extra["directed"] = bench_directed(rg, args.scale, world == 1 and not args.no_cpu)
-        extra["batched"] = bench_batched(rg)
-        extra["batched_sources"] = bench_batched_sources(rg, gs)
-        gsv = []
-        for sc in (20, 22):
-            o2, a2 = make_graph(rg, sc, 16, 1)
-            with rg.Graph.from_csr(o2, a2) as gg:
-                gsv.append(gg.degree_sort())
-        gsv.append(gs)
-        extra["serving"] = bench_serving(rg, gsv)
-        for G in gsv[:2]:
-            G.free()
+        cuda_profiler(True)
+        if "graph_build" in legs:
+            extra["graph_build"] = bench_input(rg, args.scale)
+        if "triangles" in legs:
+            extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
+        if "directed" in legs:
+            extra["directed"] = bench_directed(rg, args.scale, world == 1 and not args.no_cpu)
+        if "batched" in legs:
+            extra["batched"] = bench_batched(rg)
+        if "batched_sources" in legs:
+            extra["batched_sources"] = bench_batched_sources(rg, gs)
+        if "serving" in legs:
+            gsv = []
+            for sc in (20, 22):
+                o2, a2 = make_graph(rg, sc, 16, 1)
+                with rg.Graph.from_csr(o2, a2) as gg:
+                    gsv.append(gg.degree_sort())
+            gsv.append(gs)
+            extra["serving"] = bench_serving(rg, gsv)
+            for G in gsv[:2]:
+                G.free()
+        cuda_profiler(False)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
