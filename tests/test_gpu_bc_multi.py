@@ -90,3 +90,48 @@ def test_errors():
             G.bc_multi(np.zeros(65, np.uint32))
         with pytest.raises(rg.RgError):
             G.bc_multi(np.array([G.n], np.uint32))
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_rows_equal_the_oracle(golden, name):
+    """Independent of the GPU single-source path: each row against the CPU
+    oracle's single-source BC (oracle/oracle.cc, BC-manyiter-v2.C)."""
+    import oracle as orc
+    g = golden[name]
+    with rg.Graph.from_csr(g["off"], g["adj"]) as G:
+        src = G.bc_pick_sources(4)
+        rows, _ = G.bc_multi(src)
+    for q, s in enumerate(src):
+        want, _ = orc.bc(g["off"], g["adj"], np.array([s], np.uint32), "push", 0)
+        assert_close(rows[q], want, what=f"{name} oracle source {s}")
+
+
+def _layered(width, layers):
+    """Vertex 0, then `layers` layers of `width` vertices, complete bipartite
+    between consecutive layers: vertex 0 reaches layer k by width^(k-1) paths."""
+    src, dst = [], []
+    prev = [0]
+    nxt_id = 1
+    for _ in range(layers):
+        cur = list(range(nxt_id, nxt_id + width))
+        nxt_id += width
+        for a in prev:
+            for b in cur:
+                src.append(a)
+                dst.append(b)
+        prev = cur
+    return rg.csr_from_edges(nxt_id, np.array(src, np.uint32), np.array(dst, np.uint32))
+
+
+def test_path_counts_past_64_bits_fall_back():
+    """16^17 = 2^68 shortest paths reach the last layer: the 64-bit counts
+    would wrap, so the call must answer through single-source passes."""
+    off, adj = _layered(16, 18)
+    with rg.Graph.from_csr(off, adj) as G:
+        _check_rows(G, np.array([0, 3, 200], np.uint32), "layered 16x18")
+
+
+def test_path_counts_below_64_bits():
+    off, adj = _layered(8, 12)  # 8^11 = 2^33 paths: exact in 64 bits
+    with rg.Graph.from_csr(off, adj) as G:
+        _check_rows(G, np.array([0, 1, 50, 96], np.uint32), "layered 8x12")
