@@ -92,9 +92,11 @@ rg_status rg_csr_from_edges(int64_t n, int64_t num_edges, const uint32_t* h_src,
 rg_status rg_write_adjacency(const char* path, int64_t n, int64_t m, const uint32_t* h_off,
                              const uint32_t* h_adj);
 /* Reads a Ligra text graph (binary=0) or the binary .config/.adj/.idx triple
- * (binary=1, IO.h:477-626) and applies the same clean-up as the reference
- * loader for symmetric graphs (text only; the binary reader does no clean-up
- * in the reference either).  Result arrays as in rg_csr_from_edges. */
+ * (binary=1, IO.h:477-626) and applies the reference loader's per-list
+ * clean-up (sort, unique, drop self loops): IO.h:429-474 for symmetric = 1,
+ * the out-lists of a directed graph for symmetric = 0 (IO.h:287-345; pass them
+ * to rg_graph_create_directed).  Text only: the binary reader does no clean-up
+ * in the reference either.  Result arrays as in rg_csr_from_edges. */
 rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_out,
                         int64_t* m_out, uint32_t** h_off_out, uint32_t** h_adj_out);
 /* Reads a GAP serialized graph (.sg, GAP/src/reader.h:251-304): bool
@@ -425,7 +427,7 @@ rg_status rg_graph_clear_tuning(rg_graph* g);
 typedef struct rg_timing {
   double total_ms;          /* whole app call on the device */
   double edge_ms;           /* time inside edge kernels */
-  int64_t edges_traversed;  /* GTEPS numerator (SURVEY-style edge count) */
+  int64_t edges_traversed;  /* GTEPS numerator: edges examined by the edge maps */
   int64_t algorithmic_bytes;/* compulsory bytes of the app's byte model */
   int64_t edge_launches;    /* launches of the dominant edge kernel */
   int64_t kernel_launches;  /* all kernel launches of the call */

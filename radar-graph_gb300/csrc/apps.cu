@@ -241,7 +241,7 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
   RG_CUDA(cudaStreamSynchronize(st));
   RG_TRY(download_orig<int32_t>(g, depth, h_depth, S.tmp, st));
   RG_CUDA(cudaStreamSynchronize(st));
-  // edges examined: the out-edges of every reached vertex (SURVEY byte model)
+  // edges examined: the out-edges of every reached vertex
   g_timing.algorithmic_bytes = 4 * g_timing.edges_traversed + 4 * (n + 1) + 4 * n + 2 * ((n + 7) / 8) * rounds;
   if (rounds_out) *rounds_out = rounds;
   if (reached_out) *reached_out = reached;
