@@ -135,10 +135,14 @@ constexpr unsigned kFull = 0xffffffffu;
 // 128 at a time: lane l stages queue entry jc + l (start offset, vertex,
 // mask, adjacency base), every lane finds the entries owning its four edges
 // by a shuffle search over those starts and loads the four neighbours and
-// their masks; then each lane walks its four edges' sources together, two
-// sources of each per step, so eight row loads are in flight per lane.
+// their masks.  Narrow rows (kCols false): each lane then walks its four
+// edges' sources together, two of each per step, so eight row loads are in
+// flight per lane.  Wide rows (kCols true): the edges with work are taken
+// four at a time by the whole warp, lane l moving columns l and l + 32, so
+// one reduction instruction covers consecutive entries of a row, which L1
+// merges into sector-sized requests to L2.
 // Forward: the largest value pushed goes to *vmax (the overflow bound).
-template <class T>
+template <class T, bool kCols>
 __global__ void __launch_bounds__(256) rows_push(DevGraph g, const uint32_t* __restrict__ queue,
                                                  const uint32_t* __restrict__ qoff,
                                                  const unsigned long long* __restrict__ qmask, uint32_t count,
@@ -186,6 +190,41 @@ __global__ void __launch_bounds__(256) rows_push(DevGraph g, const uint32_t* __r
 #pragma unroll
       for (int i = 0; i < kStage; i++) {
         if (b[i]) b[i] &= lmask[x[i]];
+      }
+      if constexpr (kCols) {
+#pragma unroll
+        for (int i = 0; i < kStage; i++) {
+          unsigned act = __ballot_sync(kFull, b[i] != 0ull);
+          while (act) {
+            uint32_t xs[4], us[4];
+            unsigned long long bs[4];
+#pragma unroll
+            for (int w = 0; w < 4; w++) {
+              const bool ok = act != 0u;
+              const int sl = ok ? __ffs(act) - 1 : 0;
+              act &= act - 1u;
+              xs[w] = __shfl_sync(kFull, x[i], sl);
+              us[w] = __shfl_sync(kFull, u[i], sl);
+              const unsigned long long bb = __shfl_sync(kFull, b[i], sl);
+              bs[w] = ok ? bb : 0ull;
+            }
+            T v0[4], v1[4];
+#pragma unroll
+            for (int w = 0; w < 4; w++) {
+              const T* row = rows + (size_t)us[w] * kk;
+              v0[w] = ((bs[w] >> lane) & 1) ? row[lane] : T(0);
+              v1[w] = ((bs[w] >> (lane + 32)) & 1) ? row[lane + 32] : T(0);
+            }
+#pragma unroll
+            for (int w = 0; w < 4; w++) {
+              T* row = rows + (size_t)xs[w] * kk;
+              if ((bs[w] >> lane) & 1) atomicAdd(row + lane, v0[w]);
+              if ((bs[w] >> (lane + 32)) & 1) atomicAdd(row + lane + 32, v1[w]);
+              if constexpr (std::is_same<T, unsigned long long>::value) mx = max(mx, max(v0[w], v1[w]));
+            }
+          }
+        }
+        b[0] = b[1] = b[2] = b[3] = 0ull;
       }
       while (b[0] | b[1] | b[2] | b[3]) {
         int q[2 * kStage];
@@ -255,8 +294,8 @@ inline unsigned blocks_for(int64_t items, int per_block = 256) {
   return (unsigned)std::max<int64_t>(1, (items + per_block - 1) / per_block);
 }
 
-template <class T>
-rg_status launch_push(const DevGraph& dg, const uint32_t* queue, const uint32_t* qoff,
+template <class T, bool kCols>
+rg_status launch_push_as(const DevGraph& dg, const uint32_t* queue, const uint32_t* qoff,
                       const unsigned long long* qmask, int64_t count, int64_t degsum,
                       const unsigned long long* lmask, T* rows, int kk, unsigned long long* vmax, DevBuf& ts,
                       cudaStream_t st) {
@@ -267,7 +306,7 @@ rg_status launch_push(const DevGraph& dg, const uint32_t* queue, const uint32_t*
                                                                     kPushTile, (uint32_t)tiles, ts.as<uint32_t>());
   const int64_t blocks = std::min<int64_t>((tiles + 7) / 8, (int64_t)device_sms() * 8);
   kt_begin(st);
-  rows_push<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
+  rows_push<T, kCols><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
       dg, queue, qoff, qmask, (uint32_t)count, (uint32_t)degsum, ts.as<uint32_t>(), lmask, rows, kk, vmax);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
@@ -275,6 +314,17 @@ rg_status launch_push(const DevGraph& dg, const uint32_t* queue, const uint32_t*
   g_timing.edge_launches++;
   g_timing.edges_traversed += degsum;
   return RG_OK;
+}
+
+// Rows of 16 or more columns move a row per warp (kCols); narrower rows, a
+// source per lane.
+template <class T>
+rg_status launch_push(const DevGraph& dg, const uint32_t* queue, const uint32_t* qoff,
+                      const unsigned long long* qmask, int64_t count, int64_t degsum,
+                      const unsigned long long* lmask, T* rows, int kk, unsigned long long* vmax, DevBuf& ts,
+                      cudaStream_t st) {
+  if (kk >= 16) return launch_push_as<T, true>(dg, queue, qoff, qmask, count, degsum, lmask, rows, kk, vmax, ts, st);
+  return launch_push_as<T, false>(dg, queue, qoff, qmask, count, degsum, lmask, rows, kk, vmax, ts, st);
 }
 
 // Level storage (queues, degree scans, masks of every level), grown by copy.
