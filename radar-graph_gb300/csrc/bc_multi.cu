@@ -265,19 +265,35 @@ __global__ void __launch_bounds__(256) rows_push(DevGraph g, const uint32_t* __r
 
 // out[q*n + o] for original id o: (D - 1/sigma) / (1/sigma) (as
 // (D - 1/sigma) * sigma: exactly 0 for a vertex with no successors), NaN
-// where sigma = 0 (the source never reached the vertex).
-__global__ void mb_final(const unsigned long long* __restrict__ sig, const double* __restrict__ D, int kk, int k,
-                         int64_t n, const uint32_t* __restrict__ new_ids, double* __restrict__ out) {
-  const int64_t total = n * k;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = i / k;
-    const int q = (int)(i - o * k);
-    const uint32_t v = new_ids ? new_ids[o] : (uint32_t)o;
-    const size_t e = (size_t)v * kk + q;
-    const unsigned long long s = sig[e];
-    double r = __longlong_as_double(0x7ff8000000000000ll);
-    if (s) r = (D[e] - inv_count(s)) * (double)s;
-    out[(int64_t)q * n + o] = r;
+// where sigma = 0 (the source never reached the vertex).  A block takes 32
+// consecutive original ids: their rows are read whole into shared memory,
+// then each source's 32 results are written as one contiguous segment.
+constexpr int kFinalIds = 32;
+__global__ void __launch_bounds__(256) mb_final(const unsigned long long* __restrict__ sig,
+                                                const double* __restrict__ D, int kk, int k, int64_t n,
+                                                const uint32_t* __restrict__ new_ids, double* __restrict__ out) {
+  __shared__ double res[kFinalIds][64 + 1];
+  const int64_t ntiles = (n + kFinalIds - 1) / kFinalIds;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t o0 = t * kFinalIds;
+    for (int i = threadIdx.x; i < kFinalIds * kk; i += blockDim.x) {
+      const int j = i / kk, q = i - j * kk;
+      const int64_t o = o0 + j;
+      if (o >= n || q >= k) continue;
+      const uint32_t v = new_ids ? new_ids[o] : (uint32_t)o;
+      const size_t e = (size_t)v * kk + q;
+      const unsigned long long s = sig[e];
+      double r = __longlong_as_double(0x7ff8000000000000ll);
+      if (s) r = (D[e] - inv_count(s)) * (double)s;
+      res[j][q] = r;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kFinalIds * k; i += blockDim.x) {
+      const int q = i / kFinalIds, j = i - q * kFinalIds;
+      const int64_t o = o0 + j;
+      if (o < n) out[(int64_t)q * n + o] = res[j][q];
+    }
+    __syncthreads();
   }
 }
 
@@ -515,7 +531,7 @@ rg_status bc_multi_run(rg_graph* g, const uint32_t* src_orig, int k, double* h_o
     result = res.as<double>();
   }
   if (!overflow) {
-    const int64_t blocks = std::min<int64_t>((n * k + 255) / 256, (int64_t)device_sms() * 32);
+    const int64_t blocks = std::min<int64_t>((n + kFinalIds - 1) / kFinalIds, (int64_t)device_sms() * 8);
     mb_final<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
         pSig, pD, kk, k, n, g->sorted ? g->new_ids.as<uint32_t>() : nullptr, result);
     RG_CUDA(cudaGetLastError());
