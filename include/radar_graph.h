@@ -127,7 +127,7 @@ rg_status rg_graph_create_from_edges(int64_t n, int64_t num_edges, const uint32_
  * from rg_read_graph with symmetric = 0); the in-lists (the reference's CSC,
  * IO.h:287-345) are built on the device.  Pushes follow out-edges, pulls read
  * in-edges, and BC transposes per source as BC-manyiter-v2.C:334 does.
- * Triangle counting and serving take undirected graphs only. */
+ * Triangle counting takes undirected graphs only. */
 rg_status rg_graph_create_directed(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
                                    rg_graph** out);
 /* A DIRECTED graph built on the device from an edge list (src -> dst, ids

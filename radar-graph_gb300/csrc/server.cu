@@ -332,7 +332,6 @@ rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, i
   }
   for (int i = 0; i < ngraphs; i++) {
     if (!graphs[i]) return fail(RG_EINVAL, "rg_server_create: null graph %d", i);
-    if (graphs[i]->directed) return fail(RG_EUNSUPPORTED, "rg_server_create: graph %d is directed", i);
   }
   rg_server* S = new (std::nothrow) rg_server();
   if (!S) return fail(RG_ENOMEM, "host allocation failed");

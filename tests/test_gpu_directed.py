@@ -112,8 +112,29 @@ def test_directed_refusals(golden_directed):
     with rg.Graph.from_csr_directed(g["off"], g["adj"]) as G:
         with pytest.raises(rg.RgError, match="undirected"):
             G.triangles()
-        with pytest.raises(rg.RgError, match="directed"):
-            rg.Server([G], workers=1)
+
+
+def test_served_directed_queries(golden_directed):
+    """Directed graphs served with coalescing: every result equals the query
+    run alone (BC within 1e-9 relative)."""
+    g = golden_directed["drmat13"]
+    with rg.Graph.from_csr_directed(g["off"], g["adj"]) as G0, G0.degree_sort() as G:
+        n = G.n
+        deg = np.diff(g["off"].astype(np.int64))
+        srcs = [int(v) for v in np.nonzero(deg)[0][::97][:30]]
+        qs = [("bfs", s) for s in srcs] + [("bc", s) for s in srcs[:20]] + [("radii", i) for i in range(12)]
+        with rg.Server([G], workers=1, max_batch=64) as S:
+            ts = [S.submit(0, kind, s) for kind, s in qs]
+            outs = [S.wait(t, 0, kind)[0] for t, (kind, _) in zip(ts, qs)]
+            st = S.stats()
+        assert st["batched"] > 0
+        for (kind, s), got in zip(qs, outs):
+            if kind == "bfs":
+                assert np.array_equal(got, G.bfs("push", s)[1]), (kind, s)
+            elif kind == "bc":
+                assert_close(got, G.bc_sources(np.array([s], np.uint32), "push")[0], what=f"bc {s}")
+            else:
+                assert np.array_equal(got, G.radii_seeds(rg.radii_query_seeds(s, n), "push")[0]), (kind, s)
 
 
 def test_cli_directed(golden_directed, tmp_path):
