@@ -135,3 +135,15 @@ def test_path_counts_below_64_bits():
     off, adj = _layered(8, 12)  # 8^11 = 2^33 paths: exact in 64 bits
     with rg.Graph.from_csr(off, adj) as G:
         _check_rows(G, np.array([0, 1, 50, 96], np.uint32), "layered 8x12")
+
+
+@pytest.mark.parametrize("n", [1, 6])
+def test_no_edges(n):
+    off = np.zeros(n + 1, np.uint32)
+    with rg.Graph.from_csr(off, np.zeros(0, np.uint32)) as G:
+        src = np.arange(min(n, 3), dtype=np.uint32)
+        rows, levels = G.bc_multi(src)
+        for q, s in enumerate(src):
+            want = np.full(n, np.nan)
+            want[s] = 0.0
+            assert_close(rows[q], want, what=f"isolated source {s}")

@@ -72,3 +72,11 @@ def test_errors():
             G.radii_multi(np.zeros((2, 65), np.uint32))
         with pytest.raises(rg.RgError):
             G.radii_multi(np.full((2, 4), G.n, np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 6])
+def test_no_edges(n):
+    off = np.zeros(n + 1, np.uint32)
+    with rg.Graph.from_csr(off, np.zeros(0, np.uint32)) as G:
+        seeds = np.stack([rg.radii_query_seeds(q, n) for q in range(3)])
+        _check(G, seeds, f"no edges n={n}")
