@@ -467,7 +467,7 @@ def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=
         out["identical_results"] = identical
         best = 0.0
         for rate in rates:
-            qs = draw(per_rate)
+            qs = draw(max(per_rate, int(rate * 0.5)))  # at least half a second of arrivals
             S.reset_stats()
             inbox = queue.Queue()
 

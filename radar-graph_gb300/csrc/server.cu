@@ -49,9 +49,17 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// Radii queries per shared traversal: beyond 8 mask words per vertex the
-// masks of a large graph no longer stay in L2 and the per-query cost rises.
+// Radii queries per shared traversal: one 8-byte mask word per query and
+// vertex.  Once the masks outgrow a few times L2, every dense round streams
+// them from DRAM and the cost per query rises (measured on RMAT s24: 4.4 ms
+// per query in batches of 4, 4.9 in batches of 8), so the batch is the
+// largest power of two <= 8 whose masks fit 600 MB.
 constexpr int kRadiiBatch = 8;
+int radii_batch(const rg_graph* g) {
+  int w = kRadiiBatch;
+  while (w > 1 && (size_t)8 * w * (size_t)g->n > (size_t)600 << 20) w /= 2;
+  return w;
+}
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(Clock::now().time_since_epoch()).count();
@@ -204,7 +212,8 @@ void worker_main(rg_server* S) {
       S->pending.pop_front();
       batch.push_back(q0);
       {  // coalesce waiting queries of the same kind on the same graph
-        const int cap = q0.kind == RG_QUERY_RADII ? std::min(S->max_batch, kRadiiBatch) : S->max_batch;
+        const int cap = q0.kind == RG_QUERY_RADII ? std::min(S->max_batch, radii_batch(S->graphs[q0.graph]))
+                                                  : S->max_batch;
         for (auto it = S->pending.begin(); it != S->pending.end() && (int)batch.size() < cap;) {
           if (it->kind == q0.kind && it->graph == q0.graph) {
             batch.push_back(*it);
