@@ -106,6 +106,17 @@ rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_
  * in rg_csr_from_edges. */
 rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** h_off_out,
                      uint32_t** h_adj_out);
+/* Reads a GAP text edge list, the format chosen by the suffix as GAP's
+ * Reader::ReadFile does (GAP/src/reader.h:50-248): .el "u v"; .wel "u v w";
+ * .gr DIMACS "a u v w" lines; .graph METIS (1-based lists, fmt 0/1/100);
+ * .mtx MatrixMarket coordinate (1-based; symmetric adds both directions).
+ * Weights are skipped.  n = largest id + 1 (builder.h:74-83).  The edges
+ * come back as read -- repeats, self loops and one direction only -- for
+ * rg_csr_from_edges / rg_graph_create_from_edges (symmetric, GAP's -s) or
+ * rg_graph_create_directed_from_edges to clean up.  *h_src_out and
+ * *h_dst_out are released with rg_host_free. */
+rg_status rg_read_edges(const char* path, int64_t* n_out, int64_t* num_edges_out, uint32_t** h_src_out,
+                        uint32_t** h_dst_out);
 void rg_host_free(void* p);
 
 /* ------------------------------------------------------------------------

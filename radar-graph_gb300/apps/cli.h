@@ -69,6 +69,16 @@ inline void die(const char* what) {
   exit(1);
 }
 
+// GAP's text edge-list suffixes (GAP/src/reader.h:219-248)
+inline bool gap_edge_list(const char* path) {
+  const char* dot = strrchr(path, '.');
+  if (!dot) return false;
+  for (const char* sfx : {".el", ".wel", ".gr", ".graph", ".mtx"}) {
+    if (strcmp(dot, sfx) == 0) return true;
+  }
+  return false;
+}
+
 inline rg_variant parse_variant(const char* s) {
   if (!strcmp(s, "push") || !strcmp(s, "push-new-orig")) return RG_PUSH;
   if (!strcmp(s, "push-pull")) return RG_PUSH_PULL;
@@ -137,16 +147,32 @@ inline int run(int argc, char** argv, ComputeFn compute) {
   // degree-sorting and RADAR sort by default (-preprocess 1); the others do not
   const bool sorts_by_default = G.variant == RG_DEGSORT || G.variant == RG_RADAR;
   const long pre = P.getOptionLongValue("-preprocess", sorts_by_default ? 1 : -1);
-  uint32_t *off = nullptr, *adj = nullptr;
-  if (rg_read_graph(file, symmetric ? 1 : 0, P.getOption("-b") ? 1 : 0, &G.n, &G.m, &off, &adj) != RG_OK) {
-    die("read");
-  }
   rg_graph* g0 = nullptr;
-  const rg_status up = symmetric ? rg_graph_create(G.n, G.m, off, adj, &g0)
-                                 : rg_graph_create_directed(G.n, G.m, off, adj, &g0);
-  if (up != RG_OK) die("upload");
-  rg_host_free(off);
-  rg_host_free(adj);
+  if (gap_edge_list(file)) {
+    // GAP text edge lists (.el .wel .gr .graph .mtx): read as written, then
+    // cleaned up on the device (both directions with -s, as GAP's -s does)
+    int64_t ne = 0;
+    uint32_t *src = nullptr, *dst = nullptr;
+    if (rg_read_edges(file, &G.n, &ne, &src, &dst) != RG_OK) die("read");
+    const rg_status up = symmetric ? rg_graph_create_from_edges(G.n, ne, src, dst, 0, &g0)
+                                   : rg_graph_create_directed_from_edges(G.n, ne, src, dst, 0, &g0);
+    if (up != RG_OK) die("build");
+    rg_host_free(src);
+    rg_host_free(dst);
+    int64_t m = 0;
+    if (rg_graph_info(g0, nullptr, &m, nullptr) != RG_OK) die("info");
+    G.m = m;
+  } else {
+    uint32_t *off = nullptr, *adj = nullptr;
+    if (rg_read_graph(file, symmetric ? 1 : 0, P.getOption("-b") ? 1 : 0, &G.n, &G.m, &off, &adj) != RG_OK) {
+      die("read");
+    }
+    const rg_status up = symmetric ? rg_graph_create(G.n, G.m, off, adj, &g0)
+                                   : rg_graph_create_directed(G.n, G.m, off, adj, &g0);
+    if (up != RG_OK) die("upload");
+    rg_host_free(off);
+    rg_host_free(adj);
+  }
   if (pre == 0 || pre == 1) {  // 0: out-degree, 1: in-degree (the same when symmetric)
     Timer t;
     t.start();

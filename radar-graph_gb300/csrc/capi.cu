@@ -57,6 +57,11 @@ rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t*
   return read_sg(path, n_out, m_out, h_off_out, h_adj_out);
 }
 
+rg_status rg_read_edges(const char* path, int64_t* n_out, int64_t* num_edges_out, uint32_t** h_src_out,
+                        uint32_t** h_dst_out) {
+  return read_edges(path, n_out, num_edges_out, h_src_out, h_dst_out);
+}
+
 void rg_host_free(void* p) { free(p); }
 
 rg_status rg_device_alloc(size_t bytes, void** d_ptr) {

@@ -352,4 +352,205 @@ rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** o
   return RG_OK;
 }
 
+// GAP text edge lists (GAP/src/reader.h:50-248), chosen by the file suffix:
+//   .el     "u v" pairs, ids as written                       (ReadInEL)
+//   .wel    "u v w", weight ignored                             (ReadInWEL)
+//   .gr     DIMACS: lines "a u v w" only, ids as written        (ReadInGR)
+//   .graph  METIS: '%' comments, header "n m [fmt]" (fmt 1: weighted
+//           lists, 0 or 100: plain), then line u (from 0) lists its
+//           neighbours 1-based, weights after each when fmt is 1 (ReadInMetis)
+//   .mtx    MatrixMarket "matrix coordinate pattern|real|double|integer
+//           symmetric|general|skew-symmetric", '%' comments, "rows cols nnz"
+//           (square), entries "i j [w]" 1-based; symmetric adds (j, i) too
+//           (ReadInMTX)
+// The vertex count is the largest id + 1, as GAP's builder takes it
+// (builder.h:74-83); the edges are returned as read, for rg_csr_from_edges
+// or the device builders to clean up (builder.h:188-244's squish).
+namespace {
+
+struct TextScan {
+  const char* p;
+  const char* end;
+  void skip_blank() {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) p++;
+  }
+  void skip_space() {
+    while (p < end && is_space(*p)) p++;
+  }
+  bool at_eol() const { return p >= end || *p == '\n'; }
+  void next_line() {
+    while (p < end && *p != '\n') p++;
+    if (p < end) p++;
+  }
+  // an integer token (optional sign); a real token's integer part is read
+  // and the rest of the token skipped (weights are not used)
+  bool integer(int64_t& v) {
+    bool neg = false;
+    if (p < end && (*p == '-' || *p == '+')) neg = *p++ == '-';
+    if (p >= end || *p < '0' || *p > '9') return false;
+    int64_t x = 0;
+    while (p < end && *p >= '0' && *p <= '9') {
+      x = x * 10 + (*p - '0');
+      if (x > (int64_t)1 << 40) return false;
+      p++;
+    }
+    while (p < end && !is_space(*p)) p++;
+    v = neg ? -x : x;
+    return true;
+  }
+  bool skip_token() {  // a weight: any non-blank token
+    if (p >= end || is_space(*p)) return false;
+    while (p < end && !is_space(*p)) p++;
+    return true;
+  }
+  std::string word() {
+    skip_space();
+    const char* b = p;
+    while (p < end && !is_space(*p)) p++;
+    return std::string(b, p - b);
+  }
+};
+
+}  // namespace
+
+rg_status read_edges(const char* path, int64_t* n_out, int64_t* ne_out, uint32_t** src_out, uint32_t** dst_out) {
+  if (!path || !n_out || !ne_out || !src_out || !dst_out) return fail(RG_EINVAL, "rg_read_edges: null argument");
+  const std::string name(path);
+  const size_t dot = name.rfind('.');
+  const std::string suffix = dot == std::string::npos ? "" : name.substr(dot);
+  if (suffix != ".el" && suffix != ".wel" && suffix != ".gr" && suffix != ".graph" && suffix != ".mtx") {
+    return fail(RG_EINVAL, "rg_read_edges: unrecognized suffix '%s' (.el .wel .gr .graph .mtx)", suffix.c_str());
+  }
+  std::vector<char> buf;
+  if (!read_file(path, buf)) return fail(RG_EIO, "rg_read_edges: cannot open %s", path);
+  TextScan t{buf.data(), buf.data() + buf.size()};
+  std::vector<uint32_t> src, dst;
+  int64_t max_id = -1;
+  auto add = [&](int64_t u, int64_t v) -> bool {
+    if (u < 0 || v < 0 || u >= 0xFFFFFFFFll || v >= 0xFFFFFFFFll) return false;
+    src.push_back((uint32_t)u);
+    dst.push_back((uint32_t)v);
+    max_id = std::max(max_id, std::max(u, v));
+    return true;
+  };
+  auto bad = [&](const char* what) { return fail(RG_EFORMAT, "rg_read_edges: %s in %s", what, path); };
+  if (suffix == ".el" || suffix == ".wel") {
+    const int per = suffix == ".el" ? 2 : 3;
+    for (;;) {
+      t.skip_space();
+      if (t.p >= t.end) break;
+      int64_t x[2];
+      for (int k = 0; k < 2; k++) {
+        t.skip_space();
+        if (!t.integer(x[k])) return bad("malformed edge");
+      }
+      if (per == 3) {
+        t.skip_space();
+        if (!t.skip_token()) return bad("malformed weight");
+      }
+      if (!add(x[0], x[1])) return bad("vertex id out of range");
+    }
+  } else if (suffix == ".gr") {
+    while (t.p < t.end) {
+      if (*t.p == 'a') {
+        t.p++;
+        int64_t u, v;
+        t.skip_blank();
+        if (!t.integer(u)) return bad("malformed arc");
+        t.skip_blank();
+        if (!t.integer(v)) return bad("malformed arc");
+        t.skip_blank();
+        if (!t.skip_token()) return bad("malformed arc weight");
+        if (!add(u, v)) return bad("vertex id out of range");
+      }
+      t.next_line();
+    }
+  } else if (suffix == ".graph") {
+    while (t.p < t.end && *t.p == '%') t.next_line();
+    int64_t nn, mm, fmt = 0;
+    t.skip_blank();
+    if (!t.integer(nn)) return bad("malformed METIS header");
+    t.skip_blank();
+    if (!t.integer(mm)) return bad("malformed METIS header");
+    t.skip_blank();
+    if (!t.at_eol() && !t.integer(fmt)) return bad("malformed METIS header");
+    if (fmt != 0 && fmt != 1 && fmt != 100) return fail(RG_EUNSUPPORTED, "rg_read_edges: METIS fmt %lld", (long long)fmt);
+    t.next_line();
+    for (int64_t u = 0; u < nn && t.p < t.end;) {
+      if (*t.p == '%') {
+        t.next_line();
+        continue;
+      }
+      for (;;) {
+        t.skip_blank();
+        if (t.at_eol()) break;
+        int64_t v;
+        if (!t.integer(v)) return bad("malformed METIS list");
+        if (fmt == 1) {
+          t.skip_blank();
+          if (!t.skip_token()) return bad("malformed METIS weight");
+        }
+        if (!add(u, v - 1)) return bad("vertex id out of range");
+      }
+      t.next_line();
+      u++;
+    }
+  } else {  // .mtx
+    if (t.word() != "%%MatrixMarket") return bad(".mtx file did not start with %%MatrixMarket");
+    const std::string object = t.word(), format = t.word(), field = t.word(), symmetry = t.word();
+    if (object != "matrix" || format != "coordinate") return bad("only matrix coordinate format for .mtx");
+    bool weights;
+    if (field == "pattern") weights = false;
+    else if (field == "real" || field == "double" || field == "integer") weights = true;
+    else return bad("unsupported .mtx field type");
+    bool undirected;
+    if (symmetry == "symmetric") undirected = true;
+    else if (symmetry == "general" || symmetry == "skew-symmetric") undirected = false;
+    else return bad("unsupported .mtx symmetry type");
+    t.next_line();
+    while (t.p < t.end && *t.p == '%') t.next_line();
+    int64_t rows, cols, nnz;
+    t.skip_space();
+    if (!t.integer(rows)) return bad("malformed .mtx size line");
+    t.skip_blank();
+    if (!t.integer(cols)) return bad("malformed .mtx size line");
+    t.skip_blank();
+    if (!t.integer(nnz)) return bad("malformed .mtx size line");
+    if (rows != cols) return bad("matrix must be square for .mtx");
+    t.next_line();
+    while (t.p < t.end) {
+      t.skip_blank();
+      if (t.at_eol()) {
+        t.next_line();
+        continue;
+      }
+      int64_t i, j;
+      if (!t.integer(i)) return bad("malformed .mtx entry");
+      t.skip_blank();
+      if (!t.integer(j)) return bad("malformed .mtx entry");
+      if (weights) {
+        t.skip_blank();
+        if (!t.skip_token()) return bad("malformed .mtx weight");
+      }
+      if (!add(i - 1, j - 1)) return bad("vertex id out of range");
+      if (undirected && !add(j - 1, i - 1)) return bad("vertex id out of range");
+      t.next_line();
+    }
+  }
+  const int64_t ne = (int64_t)src.size();
+  if (max_id + 1 >= 0xFFFFFFFFll) return fail(RG_EUNSUPPORTED, "rg_read_edges: >= 2^32 vertices");
+  uint32_t* s_out = (uint32_t*)malloc(4 * (size_t)std::max<int64_t>(ne, 1));
+  uint32_t* d_out = (uint32_t*)malloc(4 * (size_t)std::max<int64_t>(ne, 1));
+  if (!s_out || !d_out) { free(s_out); free(d_out); return fail(RG_ENOMEM, "host malloc failed"); }
+  if (ne) {
+    memcpy(s_out, src.data(), 4 * (size_t)ne);
+    memcpy(d_out, dst.data(), 4 * (size_t)ne);
+  }
+  *n_out = max_id + 1;
+  *ne_out = ne;
+  *src_out = s_out;
+  *dst_out = d_out;
+  return RG_OK;
+}
+
 }  // namespace rg

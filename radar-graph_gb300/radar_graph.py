@@ -123,6 +123,7 @@ _SIGS = {
     "rg_graph_degree_sort_by": [C.c_void_p, C.c_int, _P(C.c_void_p), _u32p],
     "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
     "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
+    "rg_read_edges": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_graph_create_directed_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
@@ -276,6 +277,18 @@ def read_sg(path):
     n, m, po, pa = C.c_int64(), C.c_int64(), _u32p(), _u32p()
     _check(lib().rg_read_sg(str(path).encode(), C.byref(n), C.byref(m), C.byref(po), C.byref(pa)))
     return _take_host_csr(n.value, m.value, po, pa)
+
+
+def read_edges(path):
+    """GAP text edge list (.el .wel .gr .graph .mtx) -> (n, src, dst), edges as read."""
+    n, ne, ps, pd = C.c_int64(), C.c_int64(), _u32p(), _u32p()
+    _check(lib().rg_read_edges(str(path).encode(), C.byref(n), C.byref(ne), C.byref(ps), C.byref(pd)))
+    k = ne.value
+    src = np.ctypeslib.as_array(ps, shape=(max(k, 1),))[:k].copy()
+    dst = np.ctypeslib.as_array(pd, shape=(max(k, 1),))[:k].copy()
+    lib().rg_host_free(ps)
+    lib().rg_host_free(pd)
+    return n.value, src, dst
 
 
 def read_graph(path, symmetric=True, binary=False):

@@ -77,3 +77,19 @@ def test_cli_triangle_count(golden, tmp_path):
     assert f"{int(g['tc_total'][0])} triangles" in r.stdout
     want, _ = orc.triangles(g["off"], g["adj"], 0)
     assert np.array_equal(np.loadtxt(out, dtype=np.uint64), want)
+
+
+@pytest.mark.parametrize("fmt", ["el", "wel", "gr", "graph", "mtx", "sym.mtx"])
+def test_cli_reads_gap_edge_lists(tmp_path, fmt):
+    """TriangleCount -s on each GAP text format counts what GAP's tc_local
+    counted on the same file (golden)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_gap_formats as mg
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "gap_formats.npz"))
+    want = dict(zip(gold["formats"].tolist(), gold["totals"].tolist()))[fmt]
+    path = mg.write_formats(gold["src"], gold["dst"], str(tmp_path / "g"))[fmt]
+    exe = os.path.join(ROOT, "radar-graph_gb300", "bin", "TriangleCount")
+    r = subprocess.run([exe, "-s", "-rounds", "0", path], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert f"{want} triangles" in r.stdout

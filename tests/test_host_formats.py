@@ -140,3 +140,69 @@ def test_no_cuda_device_is_a_clean_error():
     with pytest.raises(rg.RgError) as e:
         rg.Graph.from_csr(off, adj)
     assert e.value.status in (3, 8)
+
+
+# ---- GAP text edge lists (rg_read_edges) -----------------------------------
+
+def _gap_golden():
+    import os
+    from conftest import GOLDEN
+    return np.load(os.path.join(GOLDEN, "gap_formats.npz"))
+
+
+def test_gap_formats_match_the_reference_triangle_totals(tmp_path):
+    """The same edges in every GAP format: read, symmetric clean-up, and the
+    triangle total equals GAP tc_local's on that file (golden)."""
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_gap_formats as mg
+    import oracle as orc
+    gold = _gap_golden()
+    paths = mg.write_formats(gold["src"], gold["dst"], str(tmp_path / "g"))
+    want = dict(zip(gold["formats"].tolist(), gold["totals"].tolist()))
+    assert set(want) == set(mg.FORMATS)
+    ref_off, ref_adj = rg.csr_from_edges(int(max(gold["src"].max(), gold["dst"].max())) + 1, gold["src"], gold["dst"])
+    for fmt, path in paths.items():
+        n, s, d = rg.read_edges(path)
+        off, adj = rg.csr_from_edges(n, s, d)
+        assert np.array_equal(off, ref_off) and np.array_equal(adj, ref_adj), fmt
+        _, total = orc.triangles(off, adj, 0)
+        assert total == want[fmt], fmt
+
+
+def test_gap_formats_parse_details(tmp_path):
+    p = tmp_path / "a.el"
+    p.write_text("0 1\n1 2\n\n2 2\n5 3\n")
+    n, s, d = rg.read_edges(p)
+    assert n == 6 and s.tolist() == [0, 1, 2, 5] and d.tolist() == [1, 2, 2, 3]
+    p = tmp_path / "a.gr"  # only 'a' lines; ids as written
+    p.write_text("c comment\np sp 4 2\na 1 2 7\na 3 1 2.5\n")
+    n, s, d = rg.read_edges(p)
+    assert n == 4 and s.tolist() == [1, 3] and d.tolist() == [2, 1]
+    p = tmp_path / "a.graph"  # weighted METIS (fmt 1), an empty list, comments
+    p.write_text("% c\n3 2 1\n2 5 3 1\n% between lists\n\n1 9\n")
+    n, s, d = rg.read_edges(p)
+    assert n == 3 and s.tolist() == [0, 0, 2] and d.tolist() == [1, 2, 0]
+    p = tmp_path / "a.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate integer symmetric\n%x\n3 3 2\n2 1 4\n3 3 1\n")
+    n, s, d = rg.read_edges(p)
+    assert n == 3 and s.tolist() == [1, 0, 2, 2] and d.tolist() == [0, 1, 2, 2]
+
+
+@pytest.mark.parametrize("name,text,match", [
+    ("a.txt", "0 1\n", "suffix"),
+    ("b.el", "0 x\n", "malformed"),
+    ("c.el", "0 -1\n", "range"),
+    ("d.mtx", "%%MatrixMarket matrix array real general\n2 2\n1\n", "coordinate"),
+    ("e.mtx", "%%MatrixMarket matrix coordinate complex general\n2 2 1\n1 1 1 1\n", "field"),
+    ("f.mtx", "%%MatrixMarket matrix coordinate pattern general\n2 3 1\n1 1\n", "square"),
+    ("g.graph", "3 2 11\n2\n", "fmt"),
+    ("h.mtx", "hello\n", "MatrixMarket"),
+])
+def test_gap_format_errors(tmp_path, name, text, match):
+    p = tmp_path / name
+    p.write_text(text)
+    with pytest.raises(rg.RgError, match=match):
+        rg.read_edges(p)
+    with pytest.raises(rg.RgError):
+        rg.read_edges(tmp_path / "missing.el")
