@@ -101,11 +101,14 @@ rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_
                         int64_t* m_out, uint32_t** h_off_out, uint32_t** h_adj_out);
 /* Reads a GAP serialized graph (.sg, GAP/src/reader.h:251-304): bool
  * directed, int64 directed-entry count, int64 n, int64 offsets[n+1], int32
- * neighbours.  GAP's builder already cleaned it, so it is returned as is
- * (bounds-checked); directed graphs give RG_EUNSUPPORTED.  Result arrays as
- * in rg_csr_from_edges. */
+ * neighbours (a directed graph may follow with its in-lists).  GAP's builder
+ * already cleaned it, so the out-lists are returned as is (bounds-checked).
+ * *directed_out tells which graph it is (pass the lists to
+ * rg_graph_create_directed for a directed one); with directed_out NULL a
+ * directed file gives RG_EUNSUPPORTED.  Result arrays as in
+ * rg_csr_from_edges. */
 rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** h_off_out,
-                     uint32_t** h_adj_out);
+                     uint32_t** h_adj_out, int* directed_out);
 /* Reads a GAP text edge list, the format chosen by the suffix as GAP's
  * Reader::ReadFile does (GAP/src/reader.h:50-248): .el "u v"; .wel "u v w";
  * .gr DIMACS "a u v w" lines; .graph METIS (1-based lists, fmt 0/1/100);

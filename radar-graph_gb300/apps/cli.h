@@ -148,7 +148,18 @@ inline int run(int argc, char** argv, ComputeFn compute) {
   const bool sorts_by_default = G.variant == RG_DEGSORT || G.variant == RG_RADAR;
   const long pre = P.getOptionLongValue("-preprocess", sorts_by_default ? 1 : -1);
   rg_graph* g0 = nullptr;
-  if (gap_edge_list(file)) {
+  const char* dot = strrchr(file, '.');
+  if (dot && strcmp(dot, ".sg") == 0) {
+    // GAP serialized graph: cleaned lists; the file says whether it is directed
+    uint32_t *off = nullptr, *adj = nullptr;
+    int directed = 0;
+    if (rg_read_sg(file, &G.n, &G.m, &off, &adj, &directed) != RG_OK) die("read");
+    const rg_status up = directed ? rg_graph_create_directed(G.n, G.m, off, adj, &g0)
+                                  : rg_graph_create(G.n, G.m, off, adj, &g0);
+    if (up != RG_OK) die("upload");
+    rg_host_free(off);
+    rg_host_free(adj);
+  } else if (gap_edge_list(file)) {
     // GAP text edge lists (.el .wel .gr .graph .mtx): read as written, then
     // cleaned up on the device (both directions with -s, as GAP's -s does)
     int64_t ne = 0;

@@ -53,8 +53,8 @@ rg_status rg_read_graph(const char* path, int symmetric, int binary, int64_t* n_
 }
 
 rg_status rg_read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** h_off_out,
-                     uint32_t** h_adj_out) {
-  return read_sg(path, n_out, m_out, h_off_out, h_adj_out);
+                     uint32_t** h_adj_out, int* directed_out) {
+  return read_sg(path, directed_out, n_out, m_out, h_off_out, h_adj_out);
 }
 
 rg_status rg_read_edges(const char* path, int64_t* n_out, int64_t* num_edges_out, uint32_t** h_src_out,

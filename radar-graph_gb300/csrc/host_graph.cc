@@ -310,10 +310,14 @@ rg_status read_graph(const char* path, int symmetric, int binary, int64_t* n_out
 
 // GAP serialized graph (.sg, GAP/src/reader.h:251-304, written by
 // writer.h): bool directed; int64 num_edges (directed entries); int64
-// num_nodes; int64 offsets[num_nodes+1]; int32 neighbours[num_edges].  GAP's
-// builder has already sorted and deduplicated it (builder.h:188-244), so it
-// is taken as is after bounds checks.  Directed graphs are refused.
-rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** off_out, uint32_t** adj_out) {
+// num_nodes; int64 offsets[num_nodes+1]; int32 neighbours[num_edges]; a
+// directed graph may follow with its in-lists in the same layout (reader.h:
+// 290-295).  GAP's builder has already sorted and deduplicated the lists
+// (builder.h:188-244), so the out-lists are taken as is after bounds checks;
+// in-lists are rebuilt on the device (rg_graph_create_directed).  Directed
+// files are refused when the caller passes no directed_out.
+rg_status read_sg(const char* path, int* directed_out, int64_t* n_out, int64_t* m_out, uint32_t** off_out,
+                  uint32_t** adj_out) {
   if (!path || !n_out || !m_out || !off_out || !adj_out) return fail(RG_EINVAL, "rg_read_sg: null argument");
   std::vector<char> f;
   if (!read_file(path, f)) return fail(RG_EIO, "rg_read_sg: cannot open %s", path);
@@ -323,11 +327,14 @@ rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** o
   int64_t m = 0, n = 0;
   memcpy(&m, f.data() + 1, 8);
   memcpy(&n, f.data() + 9, 8);
-  if (directed) return fail(RG_EUNSUPPORTED, "rg_read_sg: directed graphs are not supported");
+  if (directed && !directed_out) return fail(RG_EUNSUPPORTED, "rg_read_sg: directed graph (pass directed_out)");
   if (n <= 0 || m < 0) return fail(RG_EFORMAT, "rg_read_sg: bad node or edge count");
   if (n >= 0xFFFFFFFFll || m >= 0xFFFFFFFFll) return fail(RG_EUNSUPPORTED, "rg_read_sg: >= 2^32 nodes or edges");
   const size_t need = head + 8 * (size_t)(n + 1) + 4 * (size_t)m;
-  if (f.size() != need) return fail(RG_EFORMAT, "rg_read_sg: file size %zu, expected %zu", f.size(), need);
+  const bool with_inverse = directed && f.size() == head + 2 * (need - head);
+  if (f.size() != need && !with_inverse) {
+    return fail(RG_EFORMAT, "rg_read_sg: file size %zu, expected %zu", f.size(), need);
+  }
   uint32_t* o = (uint32_t*)malloc(4 * (n + 1));
   uint32_t* a = (uint32_t*)malloc(4 * (m + 4));
   if (!o || !a) { free(o); free(a); return fail(RG_ENOMEM, "host malloc failed"); }
@@ -348,6 +355,7 @@ rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** o
   }
   if (bad) { free(o); free(a); return fail(RG_EFORMAT, "rg_read_sg: offsets or neighbour ids out of range"); }
   memset(a + m, 0, 16);
+  if (directed_out) *directed_out = directed ? 1 : 0;
   *n_out = n; *m_out = m; *off_out = o; *adj_out = a;
   return RG_OK;
 }

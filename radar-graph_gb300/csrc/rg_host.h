@@ -17,7 +17,8 @@ rg_status csr_from_edges(int64_t n, int64_t ne, const uint32_t* src, const uint3
                          uint32_t** off_out, uint32_t** adj_out, int64_t* m_out);
 rg_status write_adjacency(const char* path, int64_t n, int64_t m, const uint32_t* off,
                           const uint32_t* adj);
-rg_status read_sg(const char* path, int64_t* n_out, int64_t* m_out, uint32_t** off_out, uint32_t** adj_out);
+rg_status read_sg(const char* path, int* directed_out, int64_t* n_out, int64_t* m_out, uint32_t** off_out,
+                  uint32_t** adj_out);
 rg_status read_edges(const char* path, int64_t* n_out, int64_t* ne_out, uint32_t** src_out, uint32_t** dst_out);
 rg_status read_graph(const char* path, int symmetric, int binary, int64_t* n_out, int64_t* m_out,
                      uint32_t** off_out, uint32_t** adj_out);

@@ -122,7 +122,7 @@ _SIGS = {
     "rg_graph_is_directed": [C.c_void_p, _P(C.c_int)],
     "rg_graph_degree_sort_by": [C.c_void_p, C.c_int, _P(C.c_void_p), _u32p],
     "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
-    "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
+    "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p), _P(C.c_int)],
     "rg_read_edges": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_graph_create_directed_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
@@ -272,11 +272,14 @@ def write_adjacency(path, off, adj):
                                     _ptr(adj, C.c_uint32)))
 
 
-def read_sg(path):
-    """GAP serialized undirected graph (.sg) -> CSR (off, adj)."""
-    n, m, po, pa = C.c_int64(), C.c_int64(), _u32p(), _u32p()
-    _check(lib().rg_read_sg(str(path).encode(), C.byref(n), C.byref(m), C.byref(po), C.byref(pa)))
-    return _take_host_csr(n.value, m.value, po, pa)
+def read_sg(path, allow_directed=False):
+    """GAP serialized graph (.sg) -> CSR (off, adj); with allow_directed,
+    (off, adj, directed) and a directed file gives its out-lists."""
+    n, m, po, pa, dr = C.c_int64(), C.c_int64(), _u32p(), _u32p(), C.c_int()
+    _check(lib().rg_read_sg(str(path).encode(), C.byref(n), C.byref(m), C.byref(po), C.byref(pa),
+                            C.byref(dr) if allow_directed else None))
+    off, adj = _take_host_csr(n.value, m.value, po, pa)
+    return (off, adj, bool(dr.value)) if allow_directed else (off, adj)
 
 
 def read_edges(path):

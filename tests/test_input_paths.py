@@ -10,14 +10,34 @@ import pytest
 import radar_graph as rg
 
 
-def _write_sg(path, off, adj, directed=False, bad_size=False):
+def _write_sg(path, off, adj, directed=False, bad_size=False, inverse=None):
     """GAP's layout (writer.h): bool directed, int64 edges, int64 nodes,
-    int64 offsets[n+1], int32 neighbours[m]."""
+    int64 offsets[n+1], int32 neighbours[m]; a directed graph may follow
+    with its in-lists (inverse = (in_off, in_adj))."""
     n, m = len(off) - 1, len(adj)
     with open(path, "wb") as f:
         f.write(struct.pack("<?qq", directed, m, n))
         f.write(np.asarray(off, np.int64).tobytes())
         f.write(np.asarray(adj, np.int32).tobytes()[: (4 * m - 4) if bad_size else None])
+        if inverse is not None:
+            f.write(np.asarray(inverse[0], np.int64).tobytes())
+            f.write(np.asarray(inverse[1], np.int32).tobytes())
+
+
+@pytest.mark.parametrize("with_inverse", [False, True])
+def test_sg_directed(tmp_path, with_inverse):
+    import oracle as orc
+    off = np.array([0, 2, 3, 3, 4], np.uint32)
+    adj = np.array([1, 3, 2, 0], np.uint32)
+    inv = orc.transpose(off, adj) if with_inverse else None
+    p = tmp_path / "d.sg"
+    _write_sg(p, off, adj, directed=True, inverse=inv)
+    o2, a2, directed = rg.read_sg(p, allow_directed=True)
+    assert directed and np.array_equal(o2, off) and np.array_equal(a2, adj)
+    with pytest.raises(rg.RgError, match="directed"):
+        rg.read_sg(p)
+    _write_sg(p, off, adj)
+    assert rg.read_sg(p, allow_directed=True)[2] is False
 
 
 def test_sg_round_trip(tmp_path):
