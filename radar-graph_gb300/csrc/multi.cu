@@ -76,8 +76,11 @@ __global__ void ms_gather(const int32_t* __restrict__ in, const uint32_t* __rest
   }
 }
 
+// Per-thread state sized by n; the k rows of depths (up to 64 n int32) are
+// taken from the stream-ordered pool per call, so a serving worker does not
+// keep them between batches.
 struct MsState {
-  DevBuf F, N, seen, depth, src, out;
+  DevBuf F, N, seen, src;
   Frontier f[2];
 };
 
@@ -99,7 +102,8 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
   RG_TRY(S.F.reserve(8 * n));
   RG_TRY(S.N.reserve(8 * n));
   RG_TRY(S.seen.reserve(8 * n));
-  RG_TRY(S.depth.reserve(4 * n * k));
+  DevBuf depth_rows(true, st), out_rows(true, st);
+  RG_TRY(depth_rows.reserve(4 * n * k));
   RG_TRY(S.src.reserve(4 * 64));
   RG_TRY(frontier_alloc(g, S.f[0]));
   RG_TRY(frontier_alloc(g, S.f[1]));
@@ -112,7 +116,7 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
   unsigned long long* F = S.F.as<unsigned long long>();
   unsigned long long* N = S.N.as<unsigned long long>();
   unsigned long long* seen = S.seen.as<unsigned long long>();
-  int32_t* depth = S.depth.as<int32_t>();
+  int32_t* depth = depth_rows.as<int32_t>();
   RG_CUDA(cudaMemsetAsync(F, 0, 8 * n, st));
   RG_CUDA(cudaMemsetAsync(N, 0, 8 * n, st));
   RG_CUDA(cudaMemsetAsync(seen, 0, 8 * n, st));
@@ -160,11 +164,11 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
   RG_TRY(timer.stop());
   const int32_t* res = depth;
   if (g->sorted && (h_depths || d_depths_out)) {
-    RG_TRY(S.out.reserve(4 * n * k));
+    RG_TRY(out_rows.reserve(4 * n * k));
     const int64_t blocks = std::min<int64_t>((n * k + 255) / 256, (int64_t)device_sms() * 32);
-    ms_gather<<<(unsigned)blocks, 256, 0, st>>>(depth, g->new_ids.as<uint32_t>(), n, k, S.out.as<int32_t>());
+    ms_gather<<<(unsigned)blocks, 256, 0, st>>>(depth, g->new_ids.as<uint32_t>(), n, k, out_rows.as<int32_t>());
     RG_CUDA(cudaGetLastError());
-    res = S.out.as<int32_t>();
+    res = out_rows.as<int32_t>();
   }
   if (d_depths_out) RG_CUDA(cudaMemcpyAsync(d_depths_out, res, 4 * n * k, cudaMemcpyDeviceToDevice, st));
   if (h_depths) RG_CUDA(cudaMemcpyAsync(h_depths, res, 4 * n * k, cudaMemcpyDeviceToHost, st));
