@@ -644,10 +644,11 @@ def main():
                    "hbm_frac_of_measured": round(s["bytes"] / (s["ms"] / 1e3) / 1e9 / hbm, 4),
                    "tuned": tuning[k][1]}
 
-    # e2e through the C ABI: every step copies the CSR from pinned host
-    # memory, degree-sorts it on the device, runs the four apps and copies
-    # every result back into host buffers (pinned, allocated once and reused
-    # as a serving loop would)
+    # e2e through the C ABI: every step moves the CSR from pinned host memory
+    # and degree-sorts it (rg_graph_create_sorted: offsets uploaded, the
+    # neighbour array read over the host link by the relabel), runs the four
+    # apps and copies every result back into host buffers (pinned, allocated
+    # once and reused as a serving loop would)
     h2d = 4 * (n + 1) + 4 * m
     d2h = 8 * n + 4 * n + 4 * n + 8 * n + 4 * n
     off_p, adj_p = rg.pinned_empty(n + 1, np.uint32), rg.pinned_empty(m, np.uint32)
@@ -657,7 +658,7 @@ def main():
     e2e_ms, e2e_edges = 0.0, 0
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        with rg.Graph.from_csr(off_p, adj_p) as g1, g1.degree_sort() as g2:
+        with rg.Graph.from_csr_sorted(off_p, adj_p) as g2:
             g2.set_tuning(tuning)
             g2.pagerank("radar", 20, out=ranks_p)
             e = rg.last_timing()["edges_traversed"]

@@ -151,6 +151,15 @@ rg_status rg_graph_create_directed(int64_t n, int64_t m, const uint32_t* h_off, 
 rg_status rg_graph_create_directed_from_edges(int64_t n, int64_t num_edges, const uint32_t* src,
                                               const uint32_t* dst, int on_device, rg_graph** out);
 rg_status rg_graph_is_directed(const rg_graph* g, int* directed);
+/* rg_graph_create + rg_graph_degree_sort in one call (symmetric graphs),
+ * the same graph and permutation: only the offsets are uploaded, and the
+ * relabel reads h_adj straight from host memory when the device can (memory
+ * from rg_pinned_alloc / cudaHostAlloc, 16-byte aligned), so the unsorted
+ * neighbour array never lands in HBM; otherwise it is copied first.  Offsets
+ * are checked (monotone, ending at m) and neighbour ids must be < n
+ * (RG_EINVAL otherwise). */
+rg_status rg_graph_create_sorted(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                                 rg_graph** out, uint32_t* h_new_ids);
 /* Uploads from arrays already on the device (copied; caller keeps ownership). */
 rg_status rg_graph_create_device(int64_t n, int64_t m, const uint32_t* d_off,
                                  const uint32_t* d_adj, rg_graph** out);

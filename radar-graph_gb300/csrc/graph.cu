@@ -734,10 +734,13 @@ __global__ void rank_to_ids(const uint32_t* __restrict__ sorted_ids, const uint3
 // Edge-balanced relabel: every warp owns kSweepChunk consecutive edges of the
 // original CSR (16-byte loads), finds each edge's source from the chunk
 // partition, and writes new_ids[neighbour] at the source's new position.
+// The neighbour array may be pinned host memory read over the host link
+// (rg_graph_create_sorted); it then has no padding, so the last partial
+// group of four is read entry by entry.
 __global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                      uint32_t nchunks, const uint32_t* __restrict__ new_ids,
                                                      const uint32_t* __restrict__ new_off,
-                                                     uint32_t* __restrict__ new_adj) {
+                                                     uint32_t* __restrict__ new_adj, unsigned int* bad_id) {
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -747,11 +750,20 @@ __global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t*
     for (int r = 0; r < kSweepChunk / 128; r++) {
       const uint32_t e = c * kSweepChunk + r * 128 + lane * 4;
       if (e >= g.m) continue;
-      const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+      uint32_t dd[4];
+      if (e + 4 <= g.m) {
+        const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
+        dd[0] = d4.x;
+        dd[1] = d4.y;
+        dd[2] = d4.z;
+        dd[3] = d4.w;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; i++) dd[i] = e + i < g.m ? __ldg(g.adj + e + i) : 0u;
+      }
       uint32_t s = upper_index(g.off, vlo, vhi, e);
       uint32_t nxt = g.off[s + 1];
       uint32_t base = new_off[new_ids[s]] - g.off[s];  // modulo 2^32; base + e is the new slot
-      const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
       for (int i = 0; i < 4; i++) {
         const uint32_t ee = e + i;
@@ -760,7 +772,12 @@ __global__ void __launch_bounds__(256) relabel_sweep(DevGraph g, const uint32_t*
           do { s++; nxt = g.off[s + 1]; } while (ee >= nxt);
           base = new_off[new_ids[s]] - g.off[s];
         }
-        new_adj[base + ee] = new_ids[dd[i]];
+        if (dd[i] < g.n) {
+          new_adj[base + ee] = new_ids[dd[i]];
+        } else {  // a neighbour id out of range: reported, never used as an index
+          new_adj[base + ee] = 0u;
+          atomicOr(bad_id, 1u);
+        }
       }
     }
   }
@@ -790,7 +807,9 @@ static rg_status degree_sort_impl(const rg_graph* g, bool by_out, rg_graph** out
   cudaStream_t st = c->stream;
   Workspace& ws = c->ws;
   // temporaries from the stream-ordered pool, released in order on `st`
-  DevBuf k0{true, st}, v0{true, st}, k1{true, st}, v1{true, st}, hist{true, st}, new_deg{true, st};
+  DevBuf k0{true, st}, v0{true, st}, k1{true, st}, v1{true, st}, hist{true, st}, new_deg{true, st}, bad{true, st};
+  RG_TRY(bad.reserve(16));
+  RG_CUDA(cudaMemsetAsync(bad.p, 0, 4, st));
   const int64_t nblocks = (n + kSortTile - 1) / kSortTile;
   RG_TRY(k0.reserve(4 * n)); RG_TRY(v0.reserve(4 * n));
   RG_TRY(k1.reserve(4 * n)); RG_TRY(v1.reserve(4 * n));
@@ -849,20 +868,26 @@ static rg_status degree_sort_impl(const rg_graph* g, bool by_out, rg_graph** out
     const int64_t blocks = std::min<int64_t>((g->nchunks * 32 + 255) / 256, (int64_t)std::max(sms, 1) * 8);
     relabel_sweep<<<(unsigned)blocks, 256, 0, st>>>(g->view(), g->chunk_v.as<uint32_t>(), (uint32_t)g->nchunks,
                                                     ng->new_ids.as<uint32_t>(), ng->off.as<uint32_t>(),
-                                                    ng->adj.as<uint32_t>());
+                                                    ng->adj.as<uint32_t>(), bad.as<unsigned int>());
     if (g->directed) {
       relabel_sweep<<<(unsigned)blocks, 256, 0, st>>>(g->in_view(), g->in_chunks(), (uint32_t)g->nchunks,
                                                       ng->new_ids.as<uint32_t>(), ng->in_off.as<uint32_t>(),
-                                                      ng->in_adj.as<uint32_t>());
+                                                      ng->in_adj.as<uint32_t>(), bad.as<unsigned int>());
     }
   }
   cudaError_t e = cudaMemsetAsync(ng->adj.as<uint32_t>() + m, 0, 32, st);
   if (e == cudaSuccess && g->directed) e = cudaMemsetAsync(ng->in_adj.as<uint32_t>() + m, 0, 32, st);
+  unsigned int h_bad = 0;
   if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h_bad, bad.p, 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     delete ng;
     return cuda_fail(e, "degree sort", __FILE__, __LINE__);
+  }
+  if (h_bad) {
+    delete ng;
+    return fail(RG_EINVAL, "rg_graph_degree_sort: a neighbour id is >= n");
   }
   ng->sorted = true;
   ng->max_deg = g->max_deg;  // host arrays: on first full use (host_arrays)
@@ -1167,4 +1192,83 @@ extern "C" rg_status rg_graph_is_directed(const rg_graph* g, int* directed) {
   if (!g || !directed) return fail(RG_EINVAL, "null argument");
   *directed = g->directed ? 1 : 0;
   return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// readGraph + preprocessGraph in one call (symmetric graphs): only the
+// offsets are uploaded; the ranking runs on them while nothing else waits,
+// and the relabel reads the neighbour array straight from page-locked host
+// memory over the host link, writing the relabelled array into HBM.  The
+// unsorted neighbour array never lands on the device, which saves one full
+// pass over it.  Host memory the device cannot read in place (pageable, or
+// not 16-byte aligned) takes the copy-then-sort path.
+// ---------------------------------------------------------------------------
+namespace rg {
+
+__global__ void check_offsets(const uint32_t* __restrict__ off, int64_t n, uint32_t m, unsigned int* bad) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += (int64_t)gridDim.x * blockDim.x) {
+    const bool ok = (v == 0 ? off[0] == 0u : off[v - 1] <= off[v]) && (v < n || off[n] == m);
+    if (!ok) atomicOr(bad, 1u);
+  }
+}
+
+}  // namespace rg
+
+extern "C" rg_status rg_graph_create_sorted(int64_t n, int64_t m, const uint32_t* h_off, const uint32_t* h_adj,
+                                            rg_graph** out, uint32_t* h_new_ids) {
+  if (!out || n <= 0 || m < 0 || !h_off || (m > 0 && !h_adj)) return fail(RG_EINVAL, "rg_graph_create_sorted: bad arguments");
+  if (n >= 0xFFFFFFFFll || m >= 0xFFFFFFFFll) return fail(RG_EUNSUPPORTED, ">= 2^32 vertices or edges");
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
+  cudaStream_t st = c->stream;
+  const uint32_t* d_adj = nullptr;
+  if (m > 0) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, h_adj) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        ((uintptr_t)pa.devicePointer & 15u) == 0) {
+      d_adj = static_cast<const uint32_t*>(pa.devicePointer);
+    }
+    cudaGetLastError();  // an unregistered pointer is not an error here
+  }
+  if (m > 0 && !d_adj) {  // copy, then sort
+    rg_graph* g0 = nullptr;
+    RG_TRY(rg_graph_create(n, m, h_off, h_adj, &g0));
+    const rg_status s = rg_graph_degree_sort(g0, out, h_new_ids);
+    rg_graph_free(g0);
+    return s;
+  }
+  rg_graph* g0 = nullptr;
+  RG_TRY(new_graph(&g0));
+  g0->n = n;
+  g0->m = m;
+  DevBuf info(true, st);
+  rg_status s = g0->off.reserve(4 * (n + 1));
+  if (s == RG_OK) s = info.reserve(16);
+  unsigned int h_info[2] = {0, 0};
+  if (s == RG_OK) {
+    cudaError_t e = cudaMemcpyAsync(g0->off.p, h_off, 4 * (n + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(info.p, 0, 8, st);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int64_t blocks = std::min<int64_t>((n + 256) / 256, (int64_t)std::max(sms, 1) * 16);
+    if (e == cudaSuccess) {
+      check_offsets<<<(unsigned)blocks, 256, 0, st>>>(g0->off.as<uint32_t>(), n, (uint32_t)m, info.as<unsigned int>());
+      max_degree<<<(unsigned)blocks, 256, 0, st>>>(g0->off.as<uint32_t>(), n, info.as<unsigned int>() + 1);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_info, info.p, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_fail(e, "graph offsets", __FILE__, __LINE__);
+  }
+  if (s == RG_OK && h_info[0]) s = fail(RG_EINVAL, "rg_graph_create_sorted: offsets not monotone or not ending at m");
+  if (s == RG_OK) {
+    g0->max_deg = h_info[1];
+    g0->adj.p = const_cast<uint32_t*>(d_adj);  // borrowed: released below without freeing
+    s = finish_graph(g0);                       // the chunk partition of the old CSR
+    if (s == RG_OK) s = degree_sort_impl(g0, false, out, h_new_ids);
+  }
+  g0->adj.p = nullptr;
+  g0->adj.bytes = 0;
+  delete g0;
+  return s;
 }

@@ -124,6 +124,7 @@ _SIGS = {
     "rg_triangle_count": [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)],
     "rg_read_sg": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p), _P(C.c_int)],
     "rg_read_edges": [C.c_char_p, _i64p, _i64p, _P(_u32p), _P(_u32p)],
+    "rg_graph_create_sorted": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, _P(C.c_void_p), C.c_void_p],
     "rg_graph_create_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_graph_create_directed_from_edges": [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int, _P(C.c_void_p)],
     "rg_pagerank_delta": [C.c_void_p, C.c_int, C.c_int64, _P(C.c_double), _i64p, _P(C.c_double)],
@@ -368,6 +369,18 @@ class Graph:
         fn = lib().rg_graph_create_directed_from_edges if directed else lib().rg_graph_create_from_edges
         _check(fn(n, len(src), src.ctypes.data if len(src) else None, dst.ctypes.data if len(dst) else None, 0,
                   C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_csr_sorted(cls, off, adj):
+        """Upload and degree-sort a symmetric CSR in one call (the same graph as
+        from_csr(off, adj).degree_sort()); page-locked adj (pinned_empty) is
+        read in place by the relabel."""
+        off = np.ascontiguousarray(off, np.uint32)
+        adj = np.ascontiguousarray(adj, np.uint32)
+        h = C.c_void_p()
+        _check(lib().rg_graph_create_sorted(len(off) - 1, len(adj), off.ctypes.data,
+                                            adj.ctypes.data if len(adj) else None, C.byref(h), None))
         return cls(h)
 
     def degree_sort(self):

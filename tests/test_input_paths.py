@@ -134,3 +134,43 @@ def test_directed_device_build_equals_cleanup(case):
                     r, it, _ = g.pagerank(v, 5)
                     r2, it2, _ = g2.pagerank(v, 5)
                     assert it == it2 and np.array_equal(r, r2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+@pytest.mark.parametrize("case", [(10, 8, 1), (14, 16, 2), (16, 16, 3)], ids=["s10", "s14", "s16"])
+def test_create_sorted_equals_upload_then_sort(case, pinned):
+    scale, ef, seed = case
+    off, adj = rg.rmat_csr(scale, ef, seed=seed)
+    if len(adj) % 4 == 0:  # exercise the relabel's exact tail: drop the last vertex's last edge
+        last = int(np.nonzero(np.diff(off.astype(np.int64)))[0][-1])
+        keep = np.ones(len(adj), bool)
+        keep[int(off[last + 1]) - 1] = False
+        adj = adj[keep]
+        off = off.copy()
+        off[last + 1:] -= 1
+    a = rg.pinned_empty(len(adj), np.uint32) if pinned else np.array(adj, copy=True)
+    a[:] = adj
+    with rg.Graph.from_csr(off, adj) as g0, g0.degree_sort() as want, rg.Graph.from_csr_sorted(off, a) as got:
+        wo, wa, wi = want.download()
+        go, ga, gi = got.download()
+        assert np.array_equal(wo, go) and np.array_equal(wa, ga) and np.array_equal(wi, gi)
+        r1, _, _ = want.pagerank("radar", 10)
+        r2, _, _ = got.pagerank("radar", 10)
+        assert np.array_equal(r1, r2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+def test_create_sorted_rejects_bad_input(pinned):
+    off = np.array([0, 2, 3, 4], np.uint32)
+    adj = np.array([1, 2, 0, 0], np.uint32)
+    a = rg.pinned_empty(4, np.uint32) if pinned else np.array(adj, copy=True)
+    a[:] = adj
+    a[3] = 7  # neighbour id >= n
+    with pytest.raises(rg.RgError):
+        rg.Graph.from_csr_sorted(off, a)
+    a[3] = 0
+    bad_off = np.array([0, 3, 2, 4], np.uint32)  # not monotone
+    with pytest.raises(rg.RgError):
+        rg.Graph.from_csr_sorted(bad_off, a)
