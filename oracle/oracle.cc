@@ -26,6 +26,7 @@
 
 #include <omp.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 #include <math.h>
 #include <algorithm>
@@ -96,11 +97,43 @@ inline double add_f64_old(double* p, double v) {
     if (__atomic_compare_exchange_n(q, &old, nb, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return o;
   }
 }
+// Sets a shared flag byte, writing only when it is still clear (the
+// reference's `if (doMerge[d] == false) CAS(...)`, BC-manyiter-v2.C:62-63):
+// once set, the byte's cache line stays shared instead of bouncing between
+// the threads that touch the same hub.
+inline void set_flag(uint8_t* p) {
+  if (!__atomic_load_n(p, __ATOMIC_RELAXED)) __atomic_store_n(p, (uint8_t)1, __ATOMIC_RELAXED);
+}
 inline void or_i64(int64_t* p, int64_t b) {
   int64_t old = __atomic_load_n(p, __ATOMIC_RELAXED);
   while ((old | b) != old &&
          !__atomic_compare_exchange_n(p, &old, old | b, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
   }
+}
+
+// Arrays the app drivers allocate per call, filled in parallel as the
+// reference's parallel_for initialisations do (a serial fill of the hub
+// copies alone is tens of MB on one core).
+template <class V> void par_fill(V* p, int64_t n, V v) {
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; i++) p[i] = v;
+}
+template <class V> struct Arr {
+  V* p;
+  int64_t n;
+  Arr(int64_t n_, V v) : p(static_cast<V*>(malloc(sizeof(V) * (n_ > 0 ? n_ : 1)))), n(n_) { par_fill(p, n, v); }
+  Arr(const Arr&) = delete;
+  Arr& operator=(const Arr&) = delete;
+  ~Arr() { free(p); }
+  V& operator[](int64_t i) { return p[i]; }
+  V* data() { return p; }
+};
+// Per-thread hub copies, each allocated and filled by its own thread.
+template <class V> std::vector<std::vector<V>> make_dup(int threads, int64_t count, V init) {
+  std::vector<std::vector<V>> d(count ? threads : 0);
+#pragma omp parallel for schedule(static, 1)
+  for (int t = 0; t < (int)d.size(); t++) d[t].assign(count, init);
+  return d;
 }
 
 // Parallel pack of the indices of set bytes, in increasing order (the
@@ -352,7 +385,7 @@ struct PrDeltaF {
     int32_t h = hubs->slot(d);
     if (h >= 0) {
       (*dup)[tid][h] += delta[s] / g->deg(s);
-      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+      set_flag(&(*do_merge)[h]);
     } else {
       add_f64(&ngh[d], delta[s] / g->deg(s));
     }
@@ -386,7 +419,7 @@ struct BfsF {
     if (h >= 0) {
       if ((*dup)[tid][h] == kNone) {
         (*dup)[tid][h] = s;
-        __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+        set_flag(&(*do_merge)[h]);
       }
     } else if (parents[d] == kNone) {
       if (cas_u32(&parents[d], kNone, s)) next[d] = 1;
@@ -424,7 +457,7 @@ struct BcF {
     int32_t h = hubs->slot(d);
     if (h >= 0) {
       (*dup)[tid][h] += num_paths[s];
-      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+      set_flag(&(*do_merge)[h]);
     } else {
       double o = add_f64_old(&num_paths[d], num_paths[s]);
       if (o == 0.0) next[d] = 1;
@@ -457,7 +490,7 @@ struct BcBackF {
     int32_t h = hubs->slot(d);
     if (h >= 0) {
       (*dup)[tid][h] += deps[s];
-      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+      set_flag(&(*do_merge)[h]);
     } else {
       add_f64(&deps[d], deps[s]);
     }
@@ -495,7 +528,7 @@ struct RadiiF {
     int32_t h = hubs->slot(d);
     if (h >= 0) {
       (*dup)[tid][h] |= w;
-      __atomic_store_n(&(*do_merge)[h], (uint8_t)1, __ATOMIC_RELAXED);
+      set_flag(&(*do_merge)[h]);
     } else {
       or_i64(&next_visited[d], w);
     }
@@ -595,12 +628,12 @@ int orc_pagerank(int64_t n, const uint32_t* off, const uint32_t* adj, int varian
   ThreadScope ts(nthreads);
   Csr g = make_csr(n, off, adj);
   const double damping = 0.85, eps = 0.0000001;
-  std::vector<double> a(n, 1.0 / (double)n), b(n, 0.0);
+  Arr<double> a(n, 1.0 / (double)n), b(n, 0.0);
   double* p_curr = a.data();
   double* p_next = b.data();
   int T = omp_get_max_threads();
   Hubs hubs = make_hubs(g, variant, T, sizeof(double), variant == kHubDup ? 5 : 0);
-  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  std::vector<std::vector<double>> dup = make_dup(T, hubs.count, 0.0);
   Frontier fr = Frontier::all(n);
   const double added = (1 - damping) * (1 / (double)n);
   int64_t iter = 0;
@@ -640,10 +673,10 @@ int orc_pagerank_delta(int64_t n, const uint32_t* off, const uint32_t* adj, int 
   const double damping = 0.85, eps = 0.0000001, eps2 = 0.01;
   const double one_over_n = 1 / (double)n;
   const double added = (1 - damping) * one_over_n;
-  std::vector<double> p(n, 0.0), delta(n, one_over_n), ngh(n, 0.0);
+  Arr<double> p(n, 0.0), delta(n, one_over_n), ngh(n, 0.0);
   int T = omp_get_max_threads();
   Hubs hubs = make_hubs(g, variant, T, sizeof(double), variant == kHubDup ? 6 : 1);
-  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  std::vector<std::vector<double>> dup = make_dup(T, hubs.count, 0.0);
   std::vector<uint8_t> do_merge(hubs.count, 0);
   std::vector<uint8_t> active(n);
   Frontier fr = Frontier::all(n);
@@ -688,17 +721,16 @@ int orc_bfs(int64_t n, const uint32_t* off, const uint32_t* adj, int variant, ui
             int nthreads, uint32_t* parents, int64_t* rounds_out) {
   ThreadScope ts(nthreads);
   Csr g = make_csr(n, off, adj);
-  for (int64_t i = 0; i < n; i++) parents[i] = kNone;
+  par_fill(parents, n, kNone);
   parents[root] = root;
   int T = omp_get_max_threads();
   Hubs hubs = make_hubs(g, variant, T, sizeof(uint32_t), 1 + (variant == kHubDup ? 5 : 0));
-  std::vector<std::vector<uint32_t>> dup(hubs.count ? T : 0,
-                                         std::vector<uint32_t>(hubs.count, kNone));
+  std::vector<std::vector<uint32_t>> dup = make_dup(T, hubs.count, kNone);
   // RADAR seeds the private copies from Parents (BFS.C:154-156); with hub
   // slot == vertex id that marks the root's slot as already set, which is
   // harmless because the root already has its parent.
   std::vector<uint8_t> do_merge(hubs.count, 0);
-  std::vector<uint8_t> next(n, 0);
+  Arr<uint8_t> next(n, 0);
   Frontier fr = Frontier::single(n, root);
   int64_t rounds = 0;
   while (fr.count > 0) {
@@ -720,11 +752,11 @@ int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
   const Csr g0 = make_csr(n, off, adj);
   int T = omp_get_max_threads();
   Hubs hubs = make_hubs(g0, variant, T, sizeof(double), 1 + (variant == kHubDup ? 5 : 0));
-  std::vector<std::vector<double>> dup(hubs.count ? T : 0, std::vector<double>(hubs.count, 0.0));
+  std::vector<std::vector<double>> dup = make_dup(T, hubs.count, 0.0);
   std::vector<uint8_t> do_merge(hubs.count, 0);
-  std::vector<double> num_paths(n);
-  std::vector<uint8_t> visited(n), next(n);
-  for (int64_t i = 0; i < n; i++) deps[i] = 0.0;
+  Arr<double> num_paths(n, 0.0);
+  Arr<uint8_t> visited(n, 0), next(n, 0);
+  par_fill(deps, n, 0.0);
   int64_t total_levels = 0;
   for (int it = 0; it < nsrc; it++) {
     // the reference transposes the graph before every backward phase and
@@ -734,9 +766,9 @@ int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
     const Csr& g = gf;
     const Csr gb = gf.transposed();
     uint32_t start = sources[it];
-    std::fill(num_paths.begin(), num_paths.end(), 0.0);
+    par_fill(num_paths.data(), n, 0.0);
     num_paths[start] = 1.0;
-    std::fill(visited.begin(), visited.end(), 0);
+    par_fill(visited.data(), n, (uint8_t)0);
     visited[start] = 1;
     std::vector<Frontier> levels;
     Frontier fr = Frontier::single(n, start);
@@ -751,10 +783,10 @@ int orc_bc(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
       fr = out;
     }
     total_levels += round;
-    std::vector<double>& inv = num_paths;  // inverted in place (BC-manyiter-v2.C:324-325)
+    double* inv = num_paths.data();  // inverted in place (BC-manyiter-v2.C:324-325)
 #pragma omp parallel for
     for (int64_t i = 0; i < n; i++) inv[i] = 1 / inv[i];
-    std::fill(visited.begin(), visited.end(), 0);
+    par_fill(visited.data(), n, (uint8_t)0);
     auto back_vertex = [&](uint32_t i) { visited[i] = 1; deps[i] += inv[i]; };
     Frontier cur = levels[round - 1];
     cur.for_each(back_vertex);
@@ -780,8 +812,8 @@ int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
               int64_t* rounds_out) {
   ThreadScope ts(nthreads);
   Csr g = make_csr(n, off, adj);
-  std::vector<int64_t> visited(n, 0), next_visited(n, 0);
-  for (int64_t i = 0; i < n; i++) radii[i] = -1;
+  Arr<int64_t> visited(n, 0), next_visited(n, 0);
+  par_fill(radii, n, -1);
   std::vector<uint32_t> starts(nseeds);
   for (int i = 0; i < nseeds; i++) {
     uint32_t v = seeds[i];
@@ -791,9 +823,9 @@ int orc_radii(int64_t n, const uint32_t* off, const uint32_t* adj, int variant,
   }
   int T = omp_get_max_threads();
   Hubs hubs = make_hubs(g, variant, T, sizeof(int64_t), 1 + (variant == kHubDup ? 5 : 0));
-  std::vector<std::vector<int64_t>> dup(hubs.count ? T : 0, std::vector<int64_t>(hubs.count, 0));
+  std::vector<std::vector<int64_t>> dup = make_dup(T, hubs.count, (int64_t)0);
   std::vector<uint8_t> do_merge(hubs.count, 0);
-  std::vector<uint8_t> next(n, 0);
+  Arr<uint8_t> next(n, 0);
   Frontier fr = Frontier::from_ids(n, starts);
   int32_t round = 0;
   while (fr.count > 0) {
