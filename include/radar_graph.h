@@ -435,7 +435,8 @@ rg_status rg_get_option(rg_option opt, int64_t* value);
  * (one source) and Radii on g for `variant` -- direction, dense threshold,
  * hub copies and their shared-memory budget -- and keeps the fastest per app
  * in g; later calls on g use it (instead of the thread's options).
- * best_ms[4] (may be NULL) receives the winners' times. */
+ * best_ms[4] (may be NULL) receives the winners' times.  It and the two
+ * setters below change g: no other thread may use g while they run. */
 rg_status rg_autotune(rg_graph* g, rg_variant variant, double* best_ms);
 /* The tuned value of `opt` for app 0 PageRank, 1 BFS, 2 BC, 3 Radii (-1 if
  * the app is not tuned); rg_graph_clear_tuning forgets every choice. */
