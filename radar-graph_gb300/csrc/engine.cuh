@@ -421,19 +421,41 @@ __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t*
       reinterpret_cast<uint4*>(s_owner)[threadIdx.x] = w4;
       __syncthreads();
     }
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += kThreads) {
-      uint32_t s, pos;
-      if (staged) {
-        const uint32_t li = s_owner[e - e0];
-        s = s_q[li];
-        pos = s_base[li] + (e - s_qo[li]);
-      } else {
-        const uint32_t gi = upper_index(qoff, i0, i1, e);
-        s = queue[gi];
-        pos = g.off[s] + (e - qoff[gi]);
+    // A thread's kPushItems edges go through each stage together -- their
+    // neighbour ids, then their cond tests, then the updates -- so the
+    // scattered loads of one stage overlap instead of forming one chain per
+    // edge.  cond is only a filter (the update itself decides, as with
+    // Ligra's concurrent threads), so testing it before this thread's
+    // earlier updates changes no result.
+    uint32_t sv[kPushItems], dv[kPushItems];
+    bool live[kPushItems];
+#pragma unroll
+    for (int i = 0; i < kPushItems; i++) {
+      const uint32_t e = e0 + threadIdx.x + (uint32_t)i * kThreads;
+      live[i] = e < e1;
+      sv[i] = 0;
+      dv[i] = 0;
+      if (live[i]) {
+        uint32_t s, pos;
+        if (staged) {
+          const uint32_t li = s_owner[e - e0];
+          s = s_q[li];
+          pos = s_base[li] + (e - s_qo[li]);
+        } else {
+          const uint32_t gi = upper_index(qoff, i0, i1, e);
+          s = queue[gi];
+          pos = g.off[s] + (e - qoff[gi]);
+        }
+        sv[i] = s;
+        dv[i] = g.adj[pos];
       }
-      const uint32_t d = g.adj[pos];
-      if (!op.cond(d)) continue;
+    }
+#pragma unroll
+    for (int i = 0; i < kPushItems; i++) live[i] = live[i] && op.cond(dv[i]);
+#pragma unroll
+    for (int i = 0; i < kPushItems; i++) {
+      if (!live[i]) continue;
+      const uint32_t s = sv[i], d = dv[i];
       uint32_t slot;
       if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) {
         if constexpr (IsRadii<Op>::value) {
