@@ -89,7 +89,7 @@ def test_pagerank_delta_schedules(graph, div, direction, kb, variant):
 
 
 @pytest.mark.parametrize("div", [5, 20, 80])
-@pytest.mark.parametrize("kb", [0, 16, 48])
+@pytest.mark.parametrize("kb", [0, 4, 16, 48])
 @pytest.mark.parametrize("variant", ["radar", "hubdup", "push-pull"])
 def test_bc_schedules(graph, div, kb, variant):
     G_ = graph.gs if variant == "radar" else graph.g
