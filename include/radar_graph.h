@@ -426,7 +426,12 @@ typedef enum rg_option {
   /* shape of the full-graph PageRank pull sweep: 10 * (edges per lane, 4 or 8)
    * + cache mode (0 plain loads; 1 streamed edge array; 2 streamed edge array
    * and gathers kept in L1/L2).  Default 81.  Never changes a result. */
-  RG_OPT_SWEEP_SHAPE = 4
+  RG_OPT_SWEEP_SHAPE = 4,
+  /* BC's forward (path counting) pushes use hub copies too: 1 (default) or
+   * 0 (only the backward pushes do).  The backward phase pushes into the
+   * levels that hold the hubs, where the reductions pile up; the forward
+   * reaches the hubs in its first levels.  Never changes a result. */
+  RG_OPT_BC_FWD_HUBS = 5
 } rg_option;
 rg_status rg_set_option(rg_option opt, int64_t value);
 rg_status rg_get_option(rg_option opt, int64_t* value);

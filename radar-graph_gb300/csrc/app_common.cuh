@@ -123,6 +123,7 @@ struct EmOpts {
   bool dense_forward = true;
   int64_t threshold = -1;
   uint32_t hub_h = 0;  // 0 = budget
+  bool hubs = true;    // false: this push runs without hub copies
   // run on the transposed graph (graph.h:78-86): pushes follow in-lists,
   // pulls read out-lists, the next frontier's degrees are in-degrees (a
   // no-op for symmetric graphs)
@@ -225,7 +226,7 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
       g_timing.kernel_launches++;
       g_timing.edge_launches++;
     } else {
-      int hm = (in.degsum >= kHubMinEdges && g_opts.hub_smem_kb > 0) ? hub_mode_of(o.variant) : kHubNone;
+      int hm = (o.hubs && in.degsum >= kHubMinEdges && g_opts.hub_smem_kb > 0) ? hub_mode_of(o.variant) : kHubNone;
       HubInfo hub;
       if (hm == kHubPrefix) {
         hub.H = o.hub_h ? std::min<uint32_t>(o.hub_h, hub_budget(sizeof(typename Op::HubT), g->n))

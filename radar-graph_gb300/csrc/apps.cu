@@ -344,6 +344,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     // phase on the opposite orientation (no-ops for symmetric graphs)
     const bool fwd_t = g->directed && (it % 2 == 1);
     EmOpts of = o, ob = o;
+    of.hubs = g_opts.bc_fwd_hubs != 0;
     of.transpose = fwd_t;
     ob.transpose = g->directed && !fwd_t;
     uint32_t start, start_deg;
@@ -640,6 +641,10 @@ rg_status rg_set_option(rg_option opt, int64_t value) {
       }
       g_opts.sweep_shape = value;
       return RG_OK;
+    case RG_OPT_BC_FWD_HUBS:
+      if (value != 0 && value != 1) return fail(RG_EINVAL, "bc_fwd_hubs must be 0 or 1");
+      g_opts.bc_fwd_hubs = value;
+      return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -652,6 +657,7 @@ rg_status rg_get_option(rg_option opt, int64_t* value) {
     case RG_OPT_HUB_SMEM_KB: *value = g_opts.hub_smem_kb; return RG_OK;
     case RG_OPT_DENSE_DIV: *value = g_opts.dense_div; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: *value = g_opts.sweep_shape; return RG_OK;
+    case RG_OPT_BC_FWD_HUBS: *value = g_opts.bc_fwd_hubs; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }

@@ -16,11 +16,12 @@ namespace {
 
 std::vector<Options> candidates(int app, bool hubs, const Options& base) {
   std::vector<Options> out;
-  auto add = [&](int64_t dir, int64_t div, int64_t kb) {
+  auto add = [&](int64_t dir, int64_t div, int64_t kb, int64_t fwd_hubs = 1) {
     Options o = base;
     o.direction = dir;
     o.dense_div = div;
     o.hub_smem_kb = kb;
+    o.bc_fwd_hubs = fwd_hubs;
     out.push_back(o);
   };
   // hub budgets: 4 KiB (the 512 hottest ids) keeps the push at full
@@ -43,9 +44,13 @@ std::vector<Options> candidates(int app, bool hubs, const Options& base) {
         for (int64_t div : {20, 80}) add(0, div, kb);
       for (int64_t div : {2, 5, 20}) add(1, div, 0);
       break;
-    default:  // BC pushes (its pull scans every unvisited vertex: measured slower)
+    default:  // BC pushes (its pull scans every unvisited vertex: measured slower),
+              // with hub copies in both phases or in the backward phase only
       for (int64_t kb : kbs)
-        for (int64_t div : {20, 80}) add(0, div, kb);
+        for (int64_t div : {20, 80}) {
+          add(0, div, kb);
+          if (kb > 0) add(0, div, kb, 0);
+        }
       break;
   }
   return out;
@@ -112,6 +117,7 @@ extern "C" rg_status rg_graph_tuned_option(const rg_graph* g, int app, rg_option
     case RG_OPT_HUB_SMEM_KB: *value = o.hub_smem_kb; return RG_OK;
     case RG_OPT_DENSE_DIV: *value = o.dense_div; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: *value = o.sweep_shape; return RG_OK;
+    case RG_OPT_BC_FWD_HUBS: *value = o.bc_fwd_hubs; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -129,6 +135,7 @@ extern "C" rg_status rg_graph_set_tuned_option(rg_graph* g, int app, rg_option o
     case RG_OPT_HUB_SMEM_KB: o.hub_smem_kb = value; return RG_OK;
     case RG_OPT_DENSE_DIV: o.dense_div = value; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: o.sweep_shape = value; return RG_OK;
+    case RG_OPT_BC_FWD_HUBS: o.bc_fwd_hubs = value; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }

@@ -168,7 +168,7 @@ class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("launches", C.c_int64), ("batched", C.c_int64),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("qps", C.c_double)]
 
-OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3, "sweep_shape": 4}
+OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3, "sweep_shape": 4, "bc_fwd_hubs": 5}
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
             "rg_host_free": None}
 

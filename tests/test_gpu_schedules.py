@@ -90,12 +90,13 @@ def test_pagerank_delta_schedules(graph, div, direction, kb, variant):
 
 @pytest.mark.parametrize("div", [5, 20, 80])
 @pytest.mark.parametrize("kb", [0, 4, 16, 48])
+@pytest.mark.parametrize("fwd_hubs", [1, 0])
 @pytest.mark.parametrize("variant", ["radar", "hubdup", "push-pull"])
-def test_bc_schedules(graph, div, kb, variant):
+def test_bc_schedules(graph, div, kb, fwd_hubs, variant):
     G_ = graph.gs if variant == "radar" else graph.g
-    with options(dense_div=div, hub_smem_kb=kb):
+    with options(dense_div=div, hub_smem_kb=kb, bc_fwd_hubs=fwd_hubs):
         d, _ = G_.bc_sources(graph.bc_src, variant)
-    assert_close(d, graph.bc, what=f"bc {variant} div {div} kb {kb}")
+    assert_close(d, graph.bc, what=f"bc {variant} div {div} kb {kb} fwd_hubs {fwd_hubs}")
 
 
 def test_autotune_keeps_results(graph):
