@@ -127,6 +127,40 @@ def test_library_exports_every_declared_symbol():
     assert rg.version().startswith("radar-graph-gb300")
 
 
+def test_engine_options_round_trip_and_validate():
+    """Scheduling options are host state of the calling thread: each reads
+    back what was set, out-of-range values are RG_EINVAL and leave the old
+    value, and another thread starts from the defaults."""
+    import threading
+    valid = {"direction": [0, 1], "hub_slots": [0, 512], "hub_smem_kb": [0, 4, 227],
+             "dense_div": [1, 1000, 20], "sweep_shape": [40, 42, 80, 82], "bc_fwd_hubs": [0, 1]}
+    bad = {"direction": [2, -1], "hub_slots": [-1], "hub_smem_kb": [-1, 228], "dense_div": [0],
+           "sweep_shape": [43, 50, 91], "bc_fwd_hubs": [2, -1]}
+    assert set(valid) == set(rg.OPTIONS)
+    for name in valid:
+        old = rg.get_option(name)
+        try:
+            for v in valid[name]:
+                rg.set_option(name, v)
+                assert rg.get_option(name) == v, name
+            for v in bad[name]:
+                with pytest.raises(rg.RgError) as e:
+                    rg.set_option(name, v)
+                assert e.value.status == 1, (name, v)
+                assert rg.get_option(name) == valid[name][-1], name
+        finally:
+            rg.set_option(name, old)
+    rg.set_option("dense_div", 7)
+    try:
+        seen = []
+        t = threading.Thread(target=lambda: seen.append(rg.get_option("dense_div")))
+        t.start()
+        t.join()
+        assert seen == [20] and rg.get_option("dense_div") == 7
+    finally:
+        rg.set_option("dense_div", 20)
+
+
 def test_no_cuda_device_is_a_clean_error():
     """Without a GPU the device entry points fail with a status, not a crash."""
     try:
