@@ -226,39 +226,54 @@ rg_status scan_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n, 
 // vertexSubset.h:196-211 toSparse)
 // ---------------------------------------------------------------------------
 constexpr int kCompThreads = 256;
-constexpr int kCompWords = 8;  // words per thread
-constexpr int kCompTile = kCompThreads * kCompWords;
+constexpr int kCompWords = 8;  // words per lane
+constexpr int kCompTile = kCompThreads * kCompWords;  // words per block
+constexpr int kCompWarps = kCompThreads / 32;
+constexpr int kWarpWords = kCompWords * 32;  // consecutive words per warp
 
-struct CountDeg {
-  uint32_t c, d;
-};
+// Count and degree sum of the set bits of word x (vertices vb .. vb+31).  The
+// degrees of a run of consecutive set bits [a, e) telescope to
+// off[vb+e] - off[vb+a], so a dense word costs two loads, not 64.  Bits at
+// or above n are never set, so vb + e <= n.
+__device__ __forceinline__ void word_count_deg(uint32_t x, uint32_t vb, const uint32_t* __restrict__ off,
+                                               uint32_t& c, uint32_t& d) {
+  c += __popc(x);
+  uint32_t starts = x & ~(x << 1);
+  while (starts) {
+    const int a = __ffs(starts) - 1;
+    starts &= starts - 1;
+    const uint32_t rest = ~x >> a;  // bit 0 is clear: bit a of x is set
+    const int e = rest ? a + __ffs(rest) - 1 : 32;
+    d += off[vb + e] - off[vb + a];
+  }
+}
 
-__device__ __forceinline__ CountDeg count_words(const uint32_t* __restrict__ bits, int64_t nwords,
-                                                const uint32_t* __restrict__ off, int64_t w0) {
-  CountDeg r{0, 0};
+// A warp owns kWarpWords consecutive words, lane l the words l, l+32, ...
+// (coalesced loads of the bitmap).
+__device__ __forceinline__ void warp_words(const uint32_t* __restrict__ bits, int64_t nwords, int64_t wbase,
+                                           uint32_t (&xs)[kCompWords]) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int i = 0; i < kCompWords; i++) {
-    int64_t w = w0 + i;
-    if (w >= nwords) break;
-    uint32_t x = bits[w];
-    r.c += __popc(x);
-    while (x) {
-      int b = __ffs(x) - 1;
-      x &= x - 1;
-      uint32_t v = (uint32_t)(w * 32 + b);
-      r.d += off[v + 1] - off[v];
-    }
+    const int64_t w = wbase + i * 32 + lane;
+    xs[i] = w < nwords ? bits[w] : 0u;
   }
-  return r;
 }
 
 __global__ void comp_count(const uint32_t* __restrict__ bits, int64_t nwords, const uint32_t* __restrict__ off,
                            uint32_t* __restrict__ part_c, uint32_t* __restrict__ part_d) {
-  int64_t w0 = ((int64_t)blockIdx.x * kCompThreads + threadIdx.x) * kCompWords;
-  CountDeg r = count_words(bits, nwords, off, w0);
+  const int lane = threadIdx.x & 31;
+  const int64_t wbase = (int64_t)blockIdx.x * kCompTile + (int64_t)(threadIdx.x >> 5) * kWarpWords;
+  uint32_t xs[kCompWords];
+  warp_words(bits, nwords, wbase, xs);
+  uint32_t c = 0, d = 0;
+#pragma unroll
+  for (int i = 0; i < kCompWords; i++) {
+    if (xs[i]) word_count_deg(xs[i], (uint32_t)((wbase + i * 32 + lane) * 32), off, c, d);
+  }
   __shared__ uint32_t tc, td;
-  block_exclusive_sum<kCompThreads>(r.c, &tc);
-  block_exclusive_sum<kCompThreads>(r.d, &td);
+  block_exclusive_sum<kCompThreads>(c, &tc);
+  block_exclusive_sum<kCompThreads>(d, &td);
   if (threadIdx.x == 0) {
     part_c[blockIdx.x] = tc;
     part_d[blockIdx.x] = td;
@@ -289,30 +304,65 @@ __global__ void comp_scan(uint32_t* part_c, uint32_t* part_d, int64_t nt, uint64
   }
 }
 
+// Emission: the warp walks its non-zero words in order, one word per step
+// with lane b on bit b, so the queue, qoff and depth stores of a word are
+// consecutive (coalesced) and its degrees come from 33 consecutive offsets.
 __global__ void comp_emit(const uint32_t* __restrict__ bits, int64_t nwords, const uint32_t* __restrict__ off,
                           const uint32_t* __restrict__ part_c, const uint32_t* __restrict__ part_d,
                           uint32_t* __restrict__ queue, uint32_t* __restrict__ qoff, int32_t* depth,
                           int32_t level, uint32_t* or_into) {
-  int64_t w0 = ((int64_t)blockIdx.x * kCompThreads + threadIdx.x) * kCompWords;
-  CountDeg r = count_words(bits, nwords, off, w0);
-  __shared__ uint32_t tc, td;
-  uint32_t pc = block_exclusive_sum<kCompThreads>(r.c, &tc) + part_c[blockIdx.x];
-  uint32_t pd = block_exclusive_sum<kCompThreads>(r.d, &td) + part_d[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t wbase = (int64_t)blockIdx.x * kCompTile + (int64_t)warp * kWarpWords;
+  uint32_t xs[kCompWords];
+  warp_words(bits, nwords, wbase, xs);
+  uint32_t c = 0, d = 0;
 #pragma unroll
   for (int i = 0; i < kCompWords; i++) {
-    int64_t w = w0 + i;
-    if (w >= nwords) break;
-    uint32_t x = bits[w];
-    if (or_into && x) or_into[w] |= x;
-    while (x) {
-      int b = __ffs(x) - 1;
-      x &= x - 1;
-      uint32_t v = (uint32_t)(w * 32 + b);
-      queue[pc] = v;
-      qoff[pc] = pd;
-      if (depth) depth[v] = level;
-      pc++;
-      pd += off[v + 1] - off[v];
+    if (xs[i]) {
+      const int64_t w = wbase + i * 32 + lane;
+      word_count_deg(xs[i], (uint32_t)(w * 32), off, c, d);
+      if (or_into) or_into[w] |= xs[i];
+    }
+  }
+  // the warp's place in the block, after the block's place in the frontier
+  __shared__ uint32_t wc[kCompWarps], wd[kCompWarps];
+  c = __reduce_add_sync(0xffffffffu, c);
+  d = __reduce_add_sync(0xffffffffu, d);
+  if (lane == 0) {
+    wc[warp] = c;
+    wd[warp] = d;
+  }
+  __syncthreads();
+  uint32_t pc = part_c[blockIdx.x], pd = part_d[blockIdx.x];
+  for (int j = 0; j < warp; j++) {
+    pc += wc[j];
+    pd += wd[j];
+  }
+  const uint32_t below_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int i = 0; i < kCompWords; i++) {
+    unsigned nz = __ballot_sync(0xffffffffu, xs[i] != 0u);
+    while (nz) {
+      const int j = __ffs(nz) - 1;
+      nz &= nz - 1;
+      const uint32_t x = __shfl_sync(0xffffffffu, xs[i], j);
+      const uint32_t v = (uint32_t)((wbase + i * 32 + j) * 32) + (uint32_t)lane;
+      const bool set = (x >> lane) & 1u;
+      const uint32_t dg = set ? off[v + 1] - off[v] : 0u;
+      uint32_t inc = dg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      if (set) {
+        const uint32_t at = pc + (uint32_t)__popc(x & below_mask);
+        queue[at] = v;
+        qoff[at] = pd + inc - dg;
+        if (depth) depth[v] = level;
+      }
+      pc += (uint32_t)__popc(x);
+      pd += __shfl_sync(0xffffffffu, inc, 31);
     }
   }
 }
