@@ -251,9 +251,10 @@ rg_status bfs_run(rg_graph* g, int variant, uint32_t root_orig, uint32_t* h_pare
 // ---------------------------------------------------------------------------
 // BC (BC-manyiter-v2.C:205-367)
 // ---------------------------------------------------------------------------
-__global__ void bc_invert(double* p, int64_t n) {
+// inverseNumPaths (BC-manyiter-v2.C:324-325), kept beside the path counts.
+__global__ void bc_invert(const double* __restrict__ sigma, double* __restrict__ inv, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = 1 / p[i];
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) inv[i] = 1 / sigma[i];
 }
 // BC_Back_Vertex_F over a level queue: visited[i] = 1; deps[i] += inv[i].
 __global__ void bc_back_vertex(const uint32_t* __restrict__ q, int64_t k, uint32_t* visited, double* deps,
@@ -265,10 +266,14 @@ __global__ void bc_back_vertex(const uint32_t* __restrict__ q, int64_t k, uint32
     deps[i] += inv[i];
   }
 }
-// Final transform (BC-manyiter-v2.C:347-349): D = (D - 1/sigma) / (1/sigma).
-__global__ void bc_final(double* deps, const double* __restrict__ inv, int64_t n) {
+// Final transform (BC-manyiter-v2.C:347-349): D = (D - 1/sigma) / (1/sigma),
+// computed as (D - 1/sigma) * sigma: GB300 issues FP64 slowly and a divide is
+// an iteration of several FP64 operations, a multiply one.  The two differ
+// by a rounding of the last step (relative 1e-16); an unreached vertex
+// (sigma 0, 1/sigma inf) still gives NaN.
+__global__ void bc_final(double* deps, const double* __restrict__ inv, const double* __restrict__ sigma, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) deps[i] = (deps[i] - inv[i]) / inv[i];
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) deps[i] = (deps[i] - inv[i]) * sigma[i];
 }
 __global__ void set_f64(double* a, uint32_t i, double v) { a[i] = v; }
 
@@ -298,7 +303,7 @@ rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t coun
 }
 
 struct BcState {
-  DevBuf num_paths, deps, visited, levels_q, levels_qo, bits0, bits1, tmp, qdeg;
+  DevBuf num_paths, inv_paths, deps, visited, levels_q, levels_qo, bits0, bits1, tmp, qdeg;
 };
 
 rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, double* h_deps, int64_t* levels_out,
@@ -317,6 +322,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
   const int64_t nwords = (n + 31) / 32;
   static thread_local BcState S;
   RG_TRY(S.num_paths.reserve(8 * n));
+  RG_TRY(S.inv_paths.reserve(8 * n));
   RG_TRY(S.deps.reserve(8 * n));
   RG_TRY(S.visited.reserve(4 * (nwords + 8)));
   RG_TRY(S.levels_q.reserve(4 * (n + 64)));
@@ -325,6 +331,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
   RG_TRY(S.bits1.reserve(4 * (nwords + 8)));
   CallTimer timer(g);
   double* np = S.num_paths.as<double>();
+  double* inv = S.inv_paths.as<double>();
   double* deps = S.deps.as<double>();
   uint32_t* visited = S.visited.as<uint32_t>();
   uint32_t* LQ = S.levels_q.as<uint32_t>();
@@ -381,7 +388,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
       cur = nxt;
     }
     total_levels += round;
-    bc_invert<<<vblocks, 256, 0, st>>>(np, n);
+    bc_invert<<<vblocks, 256, 0, st>>>(np, inv, n);
     RG_CUDA(cudaMemsetAsync(visited, 0, 4 * nwords, st));
     g_timing.kernel_launches++;
     auto level_view = [&](int64_t r) {
@@ -390,7 +397,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     auto back_vertex = [&](int64_t r) {
       if (lcount[r] > 0) {
         bc_back_vertex<<<(unsigned)((lcount[r] + 255) / 256), 256, 0, st>>>(LQ + lstart[r], lcount[r], visited, deps,
-                                                                          np);
+                                                                          inv);
         g_timing.kernel_launches++;
       }
     };
@@ -417,7 +424,7 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
       RG_TRY(edge_map(g, lv, bop, nullptr, ob, st));
       back_vertex(r);
     }
-    bc_final<<<vblocks, 256, 0, st>>>(deps, np, n);
+    bc_final<<<vblocks, 256, 0, st>>>(deps, inv, np, n);
     RG_CUDA(cudaGetLastError());
     g_timing.kernel_launches++;
   }

@@ -187,7 +187,7 @@ rg_status calibrate_bc(rg_graph* g, int* breakeven) {
 size_t working_bytes(const rg_graph* g, int kind, int k) {
   const size_t n = (size_t)g->n;
   // multi-source BC: two rows of ceil4(k) columns, the level store, masks and frontiers
-  if (kind == RG_QUERY_BC) return k > 1 ? (size_t)(16 * ((k + 3) & ~3) + 112) * n : 64 * n;
+  if (kind == RG_QUERY_BC) return k > 1 ? (size_t)(16 * ((k + 3) & ~3) + 112) * n : 72 * n;
   if (kind == RG_QUERY_RADII) {  // two mask rows of W words, radii rows and their copy, two frontiers
     int W = 1;
     while (W < k) W *= 2;
