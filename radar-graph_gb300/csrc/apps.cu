@@ -276,6 +276,20 @@ __global__ void bc_final(double* deps, const double* __restrict__ inv, const dou
   for (; i < n; i += (int64_t)gridDim.x * blockDim.x) deps[i] = (deps[i] - inv[i]) * sigma[i];
 }
 __global__ void set_f64(double* a, uint32_t i, double v) { a[i] = v; }
+// The next BC frontier after a forward push without marks: the unvisited
+// vertices that now have paths (their counts were 0 before the push and only
+// grow).  A warp writes one bitmap word, so no atomics.
+__global__ void bc_mark_reached(const double* __restrict__ np, const uint32_t* __restrict__ visited,
+                                uint32_t* __restrict__ next_bits, int64_t n) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += warps) {
+    const int64_t v = w * 32 + lane;
+    const bool r = v < n && !((visited[w] >> lane) & 1u) && np[v] != 0.0;
+    const unsigned bits = __ballot_sync(0xffffffffu, r);
+    if (lane == 0) next_bits[w] = bits;
+  }
+}
 
 // qoff = exclusive scan of the degrees (from deg_off) of a queue's vertices,
 // *degsum = their sum: a frontier's edge layout in another orientation.
@@ -379,7 +393,22 @@ rg_status bc_run(rg_graph* g, int variant, const uint32_t* src_orig, int nsrc, d
     while (cur.count > 0) {
       round++;
       FView nxt{LQ + qpos, LQO + qpos + round, spare_bits, 0, 0};
-      RG_TRY(edge_map(g, cur, fop, &nxt, of, st, nullptr, 0, visited));
+      if (cur.degsum >= n / 4) {
+        // a large level: one pass over the vertices finds the next frontier
+        // for less than a bitmap test per edge
+        RG_TRY(edge_map(g, cur, OpBcFwdT<false>{np, visited}, nullptr, of, st));
+        bc_mark_reached<<<vblocks, 256, 0, st>>>(np, visited, nxt.bits, n);
+        Frontier shell;  // non-owning view of nxt for the compaction (which syncs)
+        shell.bits.p = nxt.bits;
+        RG_TRY(compact_bits(g, shell, st, true, nullptr, 0, visited, nxt.queue, nxt.qoff,
+                            (of.transpose && g->directed) ? g->in_off.as<uint32_t>() : nullptr));
+        shell.bits.p = nullptr;
+        nxt.count = shell.count;
+        nxt.degsum = shell.degsum;
+        g_timing.kernel_launches += 4;
+      } else {
+        RG_TRY(edge_map(g, cur, fop, &nxt, of, st, nullptr, 0, visited));
+      }
       spare_bits = cur.bits;
       lstart.push_back(qpos);
       lcount.push_back(nxt.count);

@@ -164,13 +164,16 @@ struct OpPrDelta {
 };
 
 // BC_F (BC-manyiter-v2.C:32-101): num_paths[d] += num_paths[s] for unvisited
-// d; d joins the next frontier when it receives its first paths.
-struct OpBcFwd {
+// d; d joins the next frontier when it receives its first paths.  kMark
+// false: the same adds without marking the next frontier, which the caller
+// then reads off the counts (an unvisited vertex with paths was reached).
+template <bool kMark>
+struct OpBcFwdT {
   double* num_paths;
   const uint32_t* __restrict__ visited;
   using HubT = double;
   static constexpr int kPull = kPullSum;
-  static constexpr bool kOutput = true;
+  static constexpr bool kOutput = kMark;
   __device__ __forceinline__ bool cond(uint32_t d) const { return !bit_test(visited, d); }
   __device__ __forceinline__ bool push(uint32_t s, uint32_t d) const {
     atomicAdd(num_paths + d, num_paths[s]);
@@ -195,6 +198,7 @@ struct OpBcFwd {
     return x != 0.0 || o != 0.0;
   }
 };
+using OpBcFwd = OpBcFwdT<true>;
 
 // BC_Back_F (BC-manyiter-v2.C:103-161): deps[d] += deps[s] for unvisited d.
 struct OpBcBwd {
