@@ -145,9 +145,10 @@ def allreduce(pg, x, op):
 
 
 def measured_traffic(kernel, scale):
-    """DRAM bytes (read + write) of one launch of `kernel` on the RMAT graph of
-    this scale, from the ncu capture recorded in profiles/traffic.json (None
-    when no capture of that kernel and workload is recorded)."""
+    """DRAM bytes (read + write) of one launch of `kernel` (its template
+    instance) on the RMAT graph of this scale, from the ncu capture recorded in
+    profiles/traffic.json (None when no capture of that kernel and workload is
+    recorded)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
@@ -632,8 +633,12 @@ def main():
     sweep_ms = pr["edge_ms"] / max(pr["edge_launches"], 1)
     sweep_bytes = 4 * m + 4 * (n + 1) + 8 * n + 8 * n
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
-    pr_dir = tuning["pagerank"][1]["direction"]
-    sweep_kernel = "pr_pull_sweep" if pr_dir == 1 else "pr_push_sweep"
+    pr_opts = tuning["pagerank"][1]
+    if pr_opts["direction"] == 1:  # the pull sweep's template: <hub cache, edges per lane, cache mode>
+        shape = pr_opts["sweep_shape"]
+        sweep_kernel = f"pr_pull_sweep<{int(pr_opts['hub_smem_kb'] > 0)}, {shape // 10}, {shape % 10}>"
+    else:
+        sweep_kernel = "pr_push_sweep"
     # the graph's gather ceiling: stream the edge array and gather 8 bytes per
     # edge, nothing else -- what any pull over this graph must at least do
     gather_ms = gs.gather_probe(5)
