@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <utility>
 #include <vector>
 
@@ -43,8 +44,37 @@ struct CallTimer {
   rg_status stop();
 };
 
-int device_sms();
-int max_dyn_smem();
+int device_sms();     // of the calling thread's current device
+int max_dyn_smem();   // opt-in shared memory per block, same device
+
+// Runs fn (returning rg_status) once per device, however many threads call:
+// kernel attributes are per device, and a flag without the device id would
+// leave a second device unset.  `done` holds one bit per device id.
+template <class Fn>
+inline rg_status once_per_device(std::atomic<uint64_t>& done, Fn&& fn) {
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return RG_OK;
+  const rg_status s = fn();
+  if (s == RG_OK) done.fetch_or(bit, std::memory_order_acq_rel);
+  return s;
+}
+
+// Lets `kern` take all the opt-in dynamic shared memory next to its static
+// arrays, once per device.  Launches then pass their own size; setting the
+// limit per call instead would let one thread lower it under another's
+// launch.
+template <class K>
+inline rg_status allow_max_dyn_smem(std::atomic<uint64_t>& done, K kern) {
+  return once_per_device(done, [&]() -> rg_status {
+    cudaFuncAttributes fa;
+    RG_CUDA(cudaFuncGetAttributes(&fa, kern));
+    RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 max_dyn_smem() - (int)fa.sharedSizeBytes));
+    return RG_OK;
+  });
+}
 
 // App drivers (pagerank.cu, apps.cu, multi.cu).  Host outputs are in original
 // id order; the optional device outputs (d_*) receive the same arrays on the
@@ -147,14 +177,8 @@ rg_status launch_push(rg_graph* g, const DevGraph& pg, const FView& in, const Op
   if (kHub == kHubNone) {
     grid = (int)std::min<int64_t>(tiles, (int64_t)device_sms() * 8);
   } else {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncAttributes fa;
-      RG_CUDA(cudaFuncGetAttributes(&fa, kern));
-      RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   max_dyn_smem() - (int)fa.sharedSizeBytes));
-      attr_set = true;
-    }
+    static std::atomic<uint64_t> limit_set{0};
+    RG_TRY(allow_max_dyn_smem(limit_set, kern));
     int per_sm = 0;
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kT, dyn));
     if (per_sm < 1) per_sm = 1;
@@ -181,11 +205,17 @@ rg_status launch_push(rg_graph* g, const DevGraph& pg, const FView& in, const Op
 // cleared; the caller compacts it afterwards.
 static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
                                           uint32_t* next_bits, cudaStream_t st) {
-  static int per_sm = 0;  // one copy per translation unit, like the kernel
+  static std::atomic<uint64_t> carveout_set{0};  // one copy per translation unit, like the kernel
+  RG_TRY(once_per_device(carveout_set, [] {
+    RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+    return RG_OK;
+  }));
+  static std::atomic<int> resident{0};
+  int per_sm = resident.load(std::memory_order_relaxed);
   if (!per_sm) {
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mask_pull_sweep, 256, 0));
-    RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
     per_sm = std::max(per_sm, 1);
+    resident.store(per_sm, std::memory_order_relaxed);
   }
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);

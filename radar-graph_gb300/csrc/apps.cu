@@ -68,24 +68,26 @@ rg_status CallTimer::stop() {
   return RG_OK;
 }
 
-int device_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
-}
-int max_dyn_smem() {
-  static int v = 0;
+// Device properties, cached per device id (threads may drive different devices).
+static int device_attr(std::atomic<int>* cache, cudaDeviceAttr attr) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int>& c = cache[dev & 63];
+  int v = c.load(std::memory_order_relaxed);
   if (!v) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&v, attr, dev);
+    if (v <= 0) v = 1;
+    c.store(v, std::memory_order_relaxed);
   }
   return v;
+}
+int device_sms() {
+  static std::atomic<int> cache[64];
+  return device_attr(cache, cudaDevAttrMultiProcessorCount);
+}
+int max_dyn_smem() {
+  static std::atomic<int> cache[64];
+  return device_attr(cache, cudaDevAttrMaxSharedMemoryPerBlockOptin);
 }
 
 // ---------------------------------------------------------------------------

@@ -23,6 +23,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "app_common.cuh"
@@ -203,6 +206,32 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
 using PullFn = void (*)(DevGraph, const uint32_t*, uint32_t, const uint64_t*, unsigned long long*, uint32_t,
                         const uint64_t*);
 
+// The sweeps are picked at run time among their template instances: their
+// dynamic shared memory limit is raised to the device maximum once per
+// (kernel, device), under a lock (the per-instance form of
+// allow_max_dyn_smem).
+template <class K>
+rg_status allow_pr_dyn_smem(K kern) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, uint64_t>> done;  // kernel, device bits
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  const uint64_t bit = 1ull << (dev & 63);
+  const void* key = reinterpret_cast<const void*>(kern);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = std::find_if(done.begin(), done.end(), [&](const std::pair<const void*, uint64_t>& d) {
+    return d.first == key;
+  });
+  if (it != done.end() && (it->second & bit)) return RG_OK;
+  cudaFuncAttributes fa;
+  RG_CUDA(cudaFuncGetAttributes(&fa, kern));
+  RG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               max_dyn_smem() - (int)fa.sharedSizeBytes));
+  if (it == done.end()) done.emplace_back(key, bit);
+  else it->second |= bit;
+  return RG_OK;
+}
+
 
 template <bool kCache>
 PullFn pull_variant(int64_t shape) {
@@ -320,14 +349,14 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     return (int)std::min<size_t>(100, (need * 100 + (size_t)smem_per_sm - 1) / (size_t)std::max(smem_per_sm, 1));
   };
   if (pull) {
-    if (pull_dyn) RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_dyn));
+    if (pull_dyn) RG_TRY(allow_pr_dyn_smem(pull_fn));
     RG_CUDA(cudaFuncSetAttribute(pull_fn, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cache ? carveout(pull_dyn, std::max(1, 2048 / pull_threads)) : 0));
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pull_fn, pull_threads, pull_dyn));
     sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
                                         std::max<int64_t>((g->nchunks * 32 + pull_threads - 1) / pull_threads, 1));
   } else {
-    if (dyn) RG_CUDA(cudaFuncSetAttribute(sweep_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    if (dyn) RG_TRY(allow_pr_dyn_smem(sweep_fn));
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_fn, kSweepThreads, dyn));
     sweep_grid = (int)std::min<int64_t>((int64_t)sms * std::max(per_sm, 1),
                                         std::max<int64_t>((g->nchunks * 32 + kSweepThreads - 1) / kSweepThreads, 1));

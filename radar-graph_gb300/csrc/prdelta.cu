@@ -179,11 +179,17 @@ rg_status pagerank_delta_run(rg_graph* g, int variant, int64_t max_iters, double
   while (round++ < max_iters) {
     const bool dense = cur.count + cur.degsum > g->m / std::max<int64_t>(g_opts.dense_div, 1);
     if (dense && g->m > 0 && (variant == RG_PUSH_PULL || g_opts.direction == 1)) {
-      static int per_sm = 0;
+      static std::atomic<uint64_t> carveout_set{0};
+      RG_TRY(once_per_device(carveout_set, [] {
+        RG_CUDA(cudaFuncSetAttribute(prd_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+        return RG_OK;
+      }));
+      static std::atomic<int> resident{0};
+      int per_sm = resident.load(std::memory_order_relaxed);
       if (!per_sm) {
         RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prd_pull_sweep, 256, 0));
-        RG_CUDA(cudaFuncSetAttribute(prd_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
         per_sm = std::max(per_sm, 1);
+        resident.store(per_sm, std::memory_order_relaxed);
       }
       const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
       g_timing.edges_traversed += cur.degsum;

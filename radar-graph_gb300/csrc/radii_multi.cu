@@ -201,10 +201,12 @@ rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned l
                           cudaStream_t st) {
   constexpr int kItems = W <= 2 ? 8 : 16 / W;  // about 16 mask words in flight per lane
   auto kern = rq_pull_sweep<W, kItems>;
-  static int per_sm = 0;
+  static std::atomic<int> resident{0};
+  int per_sm = resident.load(std::memory_order_relaxed);
   if (!per_sm) {
     RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
     per_sm = std::max(per_sm, 1);
+    resident.store(per_sm, std::memory_order_relaxed);
   }
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);

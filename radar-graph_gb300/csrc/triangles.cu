@@ -209,7 +209,8 @@ rg_status triangle_run(rg_graph* g, uint64_t* h_counts, uint64_t* total_out) {
     const uint32_t H = hubs ? (uint32_t)std::min<int64_t>(n, g_opts.hub_smem_kb * 1024 / 8) : 0;
     auto kern = hubs ? count_triangles<true> : count_triangles<false>;
     const size_t dyn = 8 * (size_t)H;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    static std::atomic<uint64_t> limit_set[2];  // count_triangles<false>, <true>
+    e = allow_max_dyn_smem(limit_set[hubs ? 1 : 0], kern) == RG_OK ? cudaSuccess : cudaErrorInvalidValue;
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, dyn);
     const int64_t grid = std::min<int64_t>((gt->nchunks * 32 + 255) / 256, (int64_t)device_sms() * std::max(per_sm, 1));
