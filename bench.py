@@ -44,7 +44,8 @@ sys.path.insert(0, os.path.join(ROOT, "radar-graph_gb300"))
 
 METRIC = "GTEPS + % HBM roofline per app (RMAT s24); batched queries/s, p50/p99 vs plain"
 APPS = ("pagerank", "bfs", "bc", "radii")
-EXTRA_LEGS = ("graph_build", "triangles", "directed", "batched", "batched_sources", "serving")
+EXTRA_LEGS = ("er_contrast", "config2", "graph_build", "triangles", "directed", "batched", "batched_sources",
+              "serving")
 
 
 def peaks():
@@ -144,6 +145,20 @@ def allreduce(pg, x, op):
     return float(t.item())
 
 
+def gather_ceiling_ms(gs, reps=5):
+    """Best time (ms) to stream gs's edge array and gather 8 bytes per edge,
+    the ceiling of any pull over that graph, from the benchmark's measurement
+    library (librg_probe.so, built beside librg.so; not in the product ABI)."""
+    L = ctypes.CDLL(os.path.join(ROOT, "radar-graph_gb300", "librg_probe.so"))
+    L.rg_probe_gather_ceiling.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.rg_probe_gather_ceiling.restype = ctypes.c_int
+    ms = ctypes.c_double()
+    st = L.rg_probe_gather_ceiling(gs.handle, reps, ctypes.byref(ms))
+    if st != 0:
+        raise RuntimeError(f"gather probe failed: status {st}")
+    return ms.value
+
+
 def measured_traffic(kernel, scale):
     """DRAM bytes (read + write) of one launch of `kernel` (its template
     instance) on the RMAT graph of this scale, from the ncu capture recorded in
@@ -235,8 +250,7 @@ def bench_directed(rg, scale, with_cpu, ef=16, seed=1, reps=3):
             build_ms.append((time.perf_counter() - t0) * 1e3)
         if i < reps:
             g.free()
-    off, _, _ = g.download()
-    root = pick_root(off)
+    root = int(g.pick_roots(1)[0])
     gs = g.degree_sort()  # in-degree order (-preprocess 1)
     g.free()
     bc_src = gs.bc_pick_sources(1)
@@ -329,16 +343,6 @@ def make_graph(rg, scale, ef, seed, uniform=False):
     return rg.csr_from_edges(1 << scale, src, dst)
 
 
-def pick_root(off, seed=27491095):
-    """SourcePicker rule (GAP benchmark.h:47-64): uniform, nonzero degree."""
-    rng = np.random.default_rng(seed)
-    deg = np.diff(off.astype(np.int64))
-    while True:
-        r = int(rng.integers(0, len(deg)))
-        if deg[r] > 0:
-            return r
-
-
 def run_step(rg, gs, root, bc_src, stats):
     """One pass of the four RADAR apps over the resident graph."""
     ms, edges, launches = 0.0, 0, 0
@@ -364,6 +368,106 @@ def run_step(rg, gs, root, bc_src, stats):
     return ms, edges, launches
 
 
+def app_rates(stats, reps, hbm):
+    return {k: {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3), "ms": round(s["ms"] / reps, 3),
+                "hbm_frac_of_measured": round(s["bytes"] / (s["ms"] / 1e3) / 1e9 / hbm, 4)}
+            for k, s in stats.items()}
+
+
+def bench_er_contrast(rg, scale, with_cpu, hbm, reps=3, pr_iters_cpu=5):
+    """The low-skew contrast: an Erdos-Renyi graph with the bench graph's
+    vertex count and generated edge count (GAP MakeUniformEL,
+    generator.h:64-79), degree-sorted, the same four RADAR apps (autotuned),
+    and the oracle port on it with every result compared."""
+    off, adj = make_graph(rg, scale, 16, 1, uniform=True)
+    with rg.Graph.from_csr(off, adj) as g:
+        gs = g.degree_sort()
+    root = int(gs.pick_roots(1)[0])
+    bc_src = gs.bc_pick_sources(1)
+    gs.autotune("radar")
+    stats = {}
+    for i in range(reps + 1):
+        run_step(rg, gs, root, bc_src, stats if i else {})
+    tot_e = sum(s["edges"] for s in stats.values())
+    tot_ms = sum(s["ms"] for s in stats.values())
+    out = {"n": gs.n, "m": int(gs.m), "gteps": round(tot_e / (tot_ms / 1e3) / 1e9, 3),
+           "ms_per_step": round(tot_ms / reps, 3), "apps": app_rates(stats, reps, hbm),
+           "workload": f"RADAR PageRank(20 it)+BFS+BC(1 src)+Radii(64) on Erdos-Renyi s{scale}, "
+                       f"{16 << scale} generated edges, seed 1, symmetric, degree-sorted"}
+    if with_cpu:
+        t, e, port = port_run(off, adj, root, bc_src, pr_iters_cpu)
+        out["parity"] = parity(gpu_results(gs, root, bc_src, pr_iters_cpu), port)
+        out["parity"]["pagerank"]["iterations"] = pr_iters_cpu
+        out["cpu_port"] = {"gteps": round(sum(e.values()) / sum(t.values()) / 1e9, 4), "cores": os.cpu_count(),
+                           "seconds": {k: round(v, 3) for k, v in t.items()},
+                           "sample": f"PageRank {pr_iters_cpu} iterations + BFS + BC 1 source + Radii 64"}
+    gs.free()
+    return out
+
+
+def bench_config2(rg, with_cpu, scale=22, nroots=16, reps=3):
+    """RADAR PageRank (20 iterations, degree-sorted, autotuned) and push-pull
+    BFS from 16 GAP SourcePicker roots (benchmark.h:47-64) on R-MAT s22 ef16
+    seed 1.  The push-pull variant does not degree-sort, so its BFS runs on
+    the graph as loaded; the 16 roots also run as one 16-source traversal
+    (rg_bfs_multi).  The oracle port runs the same apps and every result is
+    compared (ranks 1e-9 relative, depths bit-exact)."""
+    off, adj = make_graph(rg, scale, 16, 1)
+    g = rg.Graph.from_csr(off, adj)
+    gs = g.degree_sort()
+    roots = g.pick_roots(nroots)
+    gs.autotune("radar")
+    pr_ms, pr_e, bfs_ms, bfs_e, multi_ms = [], 0, [], 0, []
+    for i in range(reps + 1):
+        ranks, pr_it, _ = gs.pagerank("radar", 20)
+        t = rg.last_timing()
+        if i:
+            pr_ms.append(t["total_ms"])
+            pr_e = t["edges_traversed"]
+        ms, e, depths = 0.0, 0, []
+        for r in roots:
+            depths.append(g.bfs("push-pull", int(r), parents=False)[1].copy())
+            t = rg.last_timing()
+            ms += t["total_ms"]
+            e += t["edges_traversed"]
+        if i:
+            bfs_ms.append(ms)
+            bfs_e = e
+        rows, _ = g.bfs_multi(roots)
+        if i:
+            multi_ms.append(rg.last_timing()["total_ms"])
+    out = {"n": g.n, "m": int(g.m), "roots": [int(r) for r in roots],
+           "pagerank": {"gteps": round(pr_e / (min(pr_ms) / 1e3) / 1e9, 3), "ms": round(min(pr_ms), 3),
+                        "iterations": pr_it},
+           "bfs_push_pull_16_roots": {"gteps": round(bfs_e / (min(bfs_ms) / 1e3) / 1e9, 3),
+                                      "ms_all_roots": round(min(bfs_ms), 3),
+                                      "one_16_source_traversal_ms": round(min(multi_ms), 3),
+                                      "multi_equals_single": bool(all(np.array_equal(rows[q], depths[q])
+                                                                      for q in range(nroots)))},
+           "workload": f"RADAR PageRank 20 it + push-pull BFS from {nroots} SourcePicker roots, RMAT s{scale} ef16"}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        cores = os.cpu_count() or 1
+        ids, so, sa = orc.degree_sort(off, adj)
+        orc.take_edges()
+        t0 = time.time()
+        pr_port = orc.pagerank(so, sa, "radar", 20, cores)[0][ids]
+        t_pr, e_pr = time.time() - t0, orc.take_edges()
+        t0 = time.time()
+        d_port = [orc.depths_from_parents(orc.bfs(off, adj, int(r), "push-pull", cores)[0]) for r in roots]
+        t_bfs, e_bfs = time.time() - t0, orc.take_edges()
+        r, same_nan = max_rel(ranks, pr_port)
+        same = [bool(np.array_equal(d, dp)) for d, dp in zip(depths, d_port)]
+        out["parity"] = {"pagerank": {"max_rel": float(f"{r:.3e}"), "ok": bool(same_nan and r <= 1e-9)},
+                         "bfs_depths_identical_roots": int(sum(same)), "all_ok": bool(same_nan and r <= 1e-9 and all(same))}
+        out["cpu_port"] = {"pagerank_gteps": round(e_pr / t_pr / 1e9, 4), "bfs_gteps": round(e_bfs / t_bfs / 1e9, 4),
+                           "seconds": {"pagerank": round(t_pr, 3), "bfs_16_roots": round(t_bfs, 3)}, "cores": cores}
+    gs.free()
+    g.free()
+    return out
+
+
 # ---------------------------------------------------------------------------
 # batched launch: 512 uneven graphs, one persistent launch vs one query per launch
 # ---------------------------------------------------------------------------
@@ -383,35 +487,48 @@ def bench_batched(rg, ngraphs=512, k=64, pr_iters=10, plain_graphs=24, seed=7):
     sources = np.stack(srcs)
     B = rg.Batch(csrs)
     B.run(sources, pr_iters)  # warm
-    runs = []
+    dev, wall = [], []
     for _ in range(3):
+        t0 = time.perf_counter()
         depths, ranks, iters, ms = B.run(sources, pr_iters)
-        runs.append(ms)
-    ms = min(runs)
+        wall.append((time.perf_counter() - t0) * 1e3)
+        dev.append(ms)
     nq = ngraphs * (k + 1)
-    batched_qps = nq / (ms / 1e3)
-    # plain: every query alone through the single-query entry points
-    plain_ms, plain_q, identical = 0.0, 0, True
+    # plain: every query alone through the single-query entry points, timed
+    # in the same two scopes as the batched launch: device time (CUDA events
+    # around the call's kernels, as rg_batch_run's device_ms) and wall-clock
+    # (the call through ctypes including its result copy to the host)
+    plain_dev, plain_wall, plain_q, identical = 0.0, 0.0, 0, True
     for i in range(plain_graphs):
         off, adj = csrs[i]
         with rg.Graph.from_csr(off, adj) as G:
             G.bfs("push", int(sources[i, 0]))  # warm this graph's buffers
-            t0 = time.perf_counter()
             for q in range(k):
+                t0 = time.perf_counter()
                 _, d, _, _ = G.bfs("push", int(sources[i, q]))
+                plain_wall += (time.perf_counter() - t0) * 1e3
+                plain_dev += rg.last_timing()["total_ms"]
                 identical &= bool(np.array_equal(d, depths[i][q]))
+            t0 = time.perf_counter()
             r, _, _ = G.pagerank("push-pull", pr_iters)
+            plain_wall += (time.perf_counter() - t0) * 1e3
+            plain_dev += rg.last_timing()["total_ms"]
             identical &= bool(np.array_equal(r, ranks[i]))
-            plain_ms += (time.perf_counter() - t0) * 1e3
             plain_q += k + 1
-    plain_qps = plain_q / (plain_ms / 1e3)
     B.free()
     total_e = int(sum(len(a) for _, a in csrs))
+    qps_dev, qps_wall = nq / (min(dev) / 1e3), nq / (min(wall) / 1e3)
+    plain_qps_dev, plain_qps_wall = plain_q / (plain_dev / 1e3), plain_q / (plain_wall / 1e3)
     return {"graphs": ngraphs, "scales": "U[10,16]", "edge_factor": "U[8,32]", "sources_per_graph": k,
-            "pr_iters": pr_iters, "total_directed_edges": total_e, "queries": nq, "launch_ms": round(ms, 3),
-            "queries_per_s": round(batched_qps, 1), "plain_queries_per_s": round(plain_qps, 1),
-            "plain_sample_queries": plain_q, "speedup_vs_plain": round(batched_qps / plain_qps, 2),
-            "identical_results": identical, "graph_build_s": round(gen_s, 1)}
+            "pr_iters": pr_iters, "total_directed_edges": total_e, "queries": nq,
+            "launch_ms": round(min(dev), 3), "call_wall_ms": round(min(wall), 3),
+            "queries_per_s": round(qps_dev, 1), "plain_queries_per_s": round(plain_qps_dev, 1),
+            "speedup_vs_plain": round(qps_dev / plain_qps_dev, 2),
+            "timing_scope": "device time on both sides (CUDA events around the kernels, result copies excluded)",
+            "wall": {"queries_per_s": round(qps_wall, 1), "plain_queries_per_s": round(plain_qps_wall, 1),
+                     "speedup_vs_plain": round(qps_wall / plain_qps_wall, 2),
+                     "scope": "wall-clock of the API call on both sides, result copies to the host included"},
+            "plain_sample_queries": plain_q, "identical_results": identical, "graph_build_s": round(gen_s, 1)}
 
 
 # ---------------------------------------------------------------------------
@@ -507,68 +624,131 @@ def workload_name(scale):
             "degree-sorted, autotuned schedule")
 
 
-def cpu_sample(off, adj, pr_iters=2, with_delta=True):
-    """The oracle port on all host cores, on the bench graph: RADAR PageRank
-    (pr_iters iterations), BFS, BC (1 source), Radii (64 samples) and
-    PageRankDelta (3 rounds).  Returns seconds and edges traversed per app
-    (edges counted by the oracle's own edgeMap, as the GPU counts them)."""
+def host_cpu():
+    """Host CPU the CPU legs ran on: logical cores, model and last-level cache."""
+    info = {"nproc": os.cpu_count()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            k, v = k.strip(), v.strip()
+            if k in ("Model name", "Vendor ID", "Architecture", "L3 cache", "L2 cache", "Socket(s)"):
+                info[k.lower().replace(" ", "_").replace("(s)", "s")] = v
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
+
+
+def port_run(off, adj, root, bc_src, pr_iters, with_delta=False, cores=None):
+    """The oracle port (OpenMP, all host cores) on the degree-sorted graph, as
+    the RADAR binaries run: PageRank (pr_iters iterations), BFS from `root`,
+    BC from bc_src, Radii (64 hashInt samples) and optionally PageRankDelta
+    (3 rounds).  Inputs are ORIGINAL ids.  Returns (seconds, edges, results):
+    edges counted by the port's own edgeMap as the GPU counts them; results
+    in ORIGINAL id order (PageRank ranks, BFS depths, BC dependencies, radii)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
-    cores = os.cpu_count() or 1
+    cores = cores or os.cpu_count() or 1
     ids, so, sa = orc.degree_sort(off, adj)
-    n, m = len(off) - 1, len(adj)
-    root = pick_root(off)
-    deg = np.diff(off.astype(np.int64)).astype(np.uint32)
-    src = orc.bc_sources(deg, 1)
+    n = len(off) - 1
     seeds = orc.radii_seeds(n)
-    t, e = {}, {}
+    t, e, res = {}, {}, {}
     runs = {
-        "pagerank": lambda: orc.pagerank(so, sa, "radar", pr_iters, cores),
-        "bfs": lambda: orc.bfs(so, sa, int(ids[root]), "radar", cores),
-        "bc": lambda: orc.bc(so, sa, ids[src], "radar", cores),
-        "radii": lambda: orc.radii(so, sa, ids[seeds], "radar", cores),
+        "pagerank": lambda: orc.pagerank(so, sa, "radar", pr_iters, cores)[0],
+        "bfs": lambda: orc.bfs(so, sa, int(ids[root]), "radar", cores)[0],
+        "bc": lambda: orc.bc(so, sa, ids[bc_src], "radar", cores)[0],
+        "radii": lambda: orc.radii(so, sa, ids[seeds], "radar", cores)[0],
     }
     if with_delta:
-        runs["pagerank_delta_3"] = lambda: orc.pagerank_delta(so, sa, "radar", 3, cores)
+        runs["pagerank_delta_3"] = lambda: orc.pagerank_delta(so, sa, "radar", 3, cores)[0]
     for k, fn in runs.items():
         orc.take_edges()
         t0 = time.time()
-        fn()
+        res[k] = fn()
         t[k] = time.time() - t0
         e[k] = orc.take_edges()
-    return t, e, cores
+    out = {"pagerank": res["pagerank"][ids], "bfs": orc.depths_from_parents(res["bfs"])[ids],
+           "bc": res["bc"][ids], "radii": res["radii"][ids]}
+    return t, e, out
+
+
+def gpu_results(gs, root, bc_src, pr_iters):
+    """The same four results from the GPU (ORIGINAL id order), untimed."""
+    return {"pagerank": gs.pagerank("radar", pr_iters)[0], "bfs": gs.bfs("radar", root, parents=False)[1],
+            "bc": gs.bc_sources(bc_src, "radar")[0], "radii": gs.radii("radar")[0]}
+
+
+def max_rel(a, b):
+    """Largest |a-b| / max(|a|,|b|) over the values that are finite in both
+    (0 where both are 0), and whether NaN positions agree."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    nan_ok = bool(np.array_equal(np.isnan(a), np.isnan(b)))
+    fin = np.isfinite(a) & np.isfinite(b)
+    den = np.maximum(np.abs(a[fin]), np.abs(b[fin]))
+    err = np.abs(a[fin] - b[fin])
+    rel = np.where(den > 0, err / np.where(den > 0, den, 1), 0.0)
+    inf_ok = bool(np.array_equal(a[~fin & ~np.isnan(a)], b[~fin & ~np.isnan(b)]))
+    return float(rel.max()) if rel.size else 0.0, nan_ok and inf_ok
+
+
+def parity(gpu, port, rtol=1e-9):
+    """Per app: bit-exact for depths and radii, relative 1e-9 with NaN
+    positions equal for ranks and dependencies (the tolerances of the tests)."""
+    out = {}
+    for k in ("pagerank", "bc"):
+        r, same_nan = max_rel(gpu[k], port[k])
+        out[k] = {"max_rel": float(f"{r:.3e}"), "nan_positions_equal": same_nan, "ok": bool(same_nan and r <= rtol)}
+    for k in ("bfs", "radii"):
+        out[k] = {"identical": bool(np.array_equal(gpu[k], port[k]))}
+        out[k]["ok"] = out[k]["identical"]
+    out["all_ok"] = all(v["ok"] for v in out.values())
+    return out
 
 
 def reference_arm(args):
     """--impl reference: the reference algorithm on the host cores (the oracle
-    port, OpenMP, all threads), same workload and metric as the GPU arm."""
+    port, OpenMP, all threads), same workload, metric and config as the GPU
+    arm.  The graph is generated and cleaned by the oracle itself (the GAP
+    generator and the loader's clean-up restated in oracle.cc), so this arm
+    loads no product library."""
     world, rank, local, pg = dist_init()
     if rank != 0:
         return 0
-    import radar_graph as rg
-    off, adj = make_graph(rg, args.scale, 16, 1)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    off, adj = orc.rmat_csr(args.scale, 16, 1)
     n, m = len(off) - 1, len(adj)
+    deg = np.diff(off.astype(np.int64)).astype(np.uint32)
+    root = int(orc.source_picker(deg, 1)[0])
+    bc_src = orc.bc_sources(deg, 1)
     steps = []
     for i in range(args.warmup + args.steps):
-        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters, with_delta=False)  # the headline: four apps
+        t, e, _ = port_run(off, adj, root, bc_src, args.cpu_pr_iters)  # the headline: four apps
         if i >= args.warmup:
             steps.append((t, e))
     tot_t = sum(sum(t.values()) for t, _ in steps)
     tot_e = sum(sum(e.values()) for _, e in steps)
     v = tot_e / tot_t / 1e9
+    cores = os.cpu_count() or 1
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GTEPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tot_t / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args.scale), "n": n, "m": m, "parallelism": "replicas",
-                   "l2": "inputs larger than L2 (no flush)"},
+        "config": bench_config(args.scale, n, m),
         "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
                          "sample": f"PageRank {args.cpu_pr_iters} iterations + BFS + BC 1 source + Radii 64 "
-                                   "sources per step on the full graph, edges counted by the port's edgeMap"},
+                                   "sources per step on the full graph, edges counted by the port's edgeMap",
+                         "host": host_cpu()},
         "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def bench_config(scale, n, m):
+    """The `config` both arms print (identical keys and values)."""
+    return {"workload": workload_name(scale), "n": n, "m": m, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (no flush)"}
 
 
 def main():
@@ -596,12 +776,12 @@ def main():
     off, adj = make_graph(rg, args.scale, 16, 1)
     gen_s = time.time() - t0
     n, m = len(off) - 1, len(adj)
-    root = pick_root(off)
     hbm, peak_kind = peaks()
 
     g = rg.Graph.from_csr(off, adj)
     gs = g.degree_sort()
     g.free()
+    root = int(gs.pick_roots(1)[0])  # GAP SourcePicker, as the reference arm picks it
     bc_src = gs.bc_pick_sources(1)
     tuning = gs.autotune("radar")
     rg.set_kernel_timing(True)
@@ -641,13 +821,11 @@ def main():
         sweep_kernel = "pr_push_sweep"
     # the graph's gather ceiling: stream the edge array and gather 8 bytes per
     # edge, nothing else -- what any pull over this graph must at least do
-    gather_ms = gs.gather_probe(5)
+    gather_ms = gather_ceiling_ms(gs)
     traffic = measured_traffic(sweep_kernel, args.scale)
-    apps = {}
-    for k, s in stats.items():
-        apps[k] = {"gteps": round(s["edges"] / (s["ms"] / 1e3) / 1e9, 3), "ms": round(s["ms"] / args.steps, 3),
-                   "hbm_frac_of_measured": round(s["bytes"] / (s["ms"] / 1e3) / 1e9 / hbm, 4),
-                   "tuned": tuning[k][1]}
+    apps = app_rates(stats, args.steps, hbm)
+    for k in apps:
+        apps[k]["tuned"] = tuning[k][1]
 
     # e2e through the C ABI: every step moves the CSR from pinned host memory
     # and degree-sorts it (rg_graph_create_sorted: offsets uploaded, the
@@ -696,14 +874,19 @@ def main():
                                "hbm_frac_of_measured": round(prd["bytes"] / (prd_ms / 1e3) / 1e9 / hbm, 4),
                                "variant": "radar", "max_iters": 100}
     legs = set(args.only.split(",")) if args.only else set(EXTRA_LEGS)
+    with_cpu = world == 1 and not args.no_cpu
     if rank == 0 and not args.no_extra:
         cuda_profiler(True)
+        if "er_contrast" in legs:
+            extra["er_contrast"] = bench_er_contrast(rg, args.scale, with_cpu, hbm)
+        if "config2" in legs:
+            extra["config2_rmat22"] = bench_config2(rg, with_cpu)
         if "graph_build" in legs:
             extra["graph_build"] = bench_input(rg, args.scale)
         if "triangles" in legs:
-            extra["triangles"] = bench_triangles(rg, gs, world == 1 and not args.no_cpu)
+            extra["triangles"] = bench_triangles(rg, gs, with_cpu)
         if "directed" in legs:
-            extra["directed"] = bench_directed(rg, args.scale, world == 1 and not args.no_cpu)
+            extra["directed"] = bench_directed(rg, args.scale, with_cpu)
         if "batched" in legs:
             extra["batched"] = bench_batched(rg)
         if "batched_sources" in legs:
@@ -720,25 +903,30 @@ def main():
                 G.free()
         cuda_profiler(False)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        t, e, cores = cpu_sample(off, adj, args.cpu_pr_iters)
+    # CPU baseline and parity on the bench graph: the oracle port (all host
+    # cores) runs the four RADAR apps with the same inputs -- PageRank for the
+    # full 20 iterations -- and every GPU result is compared with its output
+    cpu, par = None, None
+    if rank == 0 and with_cpu:
+        t, e, port = port_run(off, adj, root, bc_src, 20, with_delta=True)
         t_prd, e_prd = t.pop("pagerank_delta_3"), e.pop("pagerank_delta_3")
+        par = parity(gpu_results(gs, root, bc_src, 20), port)
         tot_t = sum(t.values())
         extra["pagerank_delta"]["cpu_port_gteps_3_rounds"] = round(e_prd / t_prd / 1e9, 4)
-        cpu = {"value": round(sum(e.values()) / tot_t / 1e9, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
-               "sample": "oracle port, OpenMP, all host cores: RADAR PageRank 2 iterations + BFS + BC 1 source + "
+        cpu = {"value": round(sum(e.values()) / tot_t / 1e9, 4), "unit": "GTEPS", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": "oracle port, OpenMP, all host cores: RADAR PageRank 20 iterations + BFS + BC 1 source + "
                          f"Radii 64 sources on the full graph ({tot_t:.1f} s)",
-               "seconds": {k: round(v, 3) for k, v in t.items()}}
+               "seconds": {k: round(v, 3) for k, v in t.items()}, "host": host_cpu()}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(args.scale), "n": n, "m": m,
-                       "parallelism": "replicas", "l2": "inputs larger than L2 (no flush)",
-                       "graph_build_s": round(gen_s, 1)},
+            "config": bench_config(args.scale, n, m),
+            "parity": par,
+            "apps_hbm_frac": {k: v["hbm_frac_of_measured"] for k, v in apps.items()},
             "apps": apps,
             "roofline": {"bound": "hbm", "kernel": sweep_kernel,
                          "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
@@ -751,6 +939,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "wall_s": round(wall, 3),
+            "graph_generation_s": round(gen_s, 1),
         }
         line.update(extra)
         print(json.dumps(line), flush=True)

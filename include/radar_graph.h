@@ -219,6 +219,11 @@ rg_status rg_bc_sources(rg_graph* g, rg_variant variant, const uint32_t* h_sourc
                         double* h_deps, int64_t* levels_out);
 /* The sources rg_bc would use (ORIGINAL ids). */
 rg_status rg_bc_pick_sources(const rg_graph* g, int k, uint32_t* h_sources);
+/* k search roots (ORIGINAL ids) drawn like GAP's SourcePicker
+ * (GAP/src/benchmark.h:47-64): mt19937(27491095) with
+ * uniform_int_distribution<int32_t> over [0, n-1], redrawn while the vertex
+ * has out-degree 0, the k picks continuing one generator. */
+rg_status rg_pick_roots(const rg_graph* g, int k, uint32_t* h_roots);
 
 /* Radii (Radii.C:140-218): min(n,64) seeds hashInt(i) % n.  h_radii: n int32
  * (-1 unreached, 0 seed, else last round the vertex's mask grew). */
@@ -393,11 +398,16 @@ rg_status rg_synchronize(void);
  * as device pointers; the function allocates nothing.  Its working memory
  * (two frontier queues, a visited bitmap, a counter) is one fixed 16.25 MiB
  * __device__ array that every GPU loading the library holds until exit, so
- * n is limited to RG_NOALLOC_MAX_VERTICES (larger n -> RG_EINVAL).  The
- * first call on each device looks up that array's device address; make it
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU (other streams, other threads) race and must be
- * serialized by the caller.  Results equal rg_bfs's depths on the same CSR.
+ * n is limited to RG_NOALLOC_MAX_VERTICES (larger n -> RG_EINVAL).
+ * Preconditions the function cannot check without reading device memory:
+ * d_off must be a valid CSR (non-decreasing, d_off[0] = 0, d_off[n] = m);
+ * a neighbour id >= n in d_adj is skipped by the kernel (never written
+ * through).  Each call looks up the array's device address for the current
+ * device (cudaGetSymbolAddress); the first call on a device may also load
+ * the library's device code there, so make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU (other
+ * streams, other threads) race and must be serialized by the caller.
+ * Results equal rg_bfs's depths on the same CSR.
  * ------------------------------------------------------------------------ */
 #define RG_NOALLOC_MAX_VERTICES 2097152
 rg_status rg_bfs_depth_noalloc(const uint32_t* d_off, const uint32_t* d_adj, int64_t n, int64_t m,
@@ -465,13 +475,6 @@ rg_status rg_last_timing(rg_timing* t);
 /* on != 0: every edge-kernel launch of the following app calls is bracketed
  * by CUDA events on its stream and rg_timing.edge_ms reports their sum. */
 rg_status rg_set_kernel_timing(int on);
-
-/* Gather ceiling of g (no counterpart in the reference; a measurement aid):
- * the best of `reps` timed passes that stream g's edge array and gather one
- * 8-byte value per edge with perfect balance and no other work.  Every pull
- * over g does at least this, so kernels are compared with it beside the HBM
- * copy bandwidth. */
-rg_status rg_gather_probe(rg_graph* g, int reps, double* best_ms);
 
 #ifdef __cplusplus
 }

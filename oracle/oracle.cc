@@ -989,4 +989,110 @@ void orc_bfs_depths(int64_t n, const uint32_t* off, const uint32_t* adj, uint32_
   }
 }
 
+
+// Seeded edge list of the GAP generator (GAP/src/generator.h:52-114), so the
+// oracle builds the benchmark's graphs without the product library.
+// R-MAT (uniform = 0): per edge, `scale` draws of a float in [0,1) pick one of
+// four quadrants with A=0.57, B=0.19, C=0.19 (generator.h:82-105); edges come
+// in 2^18-edge blocks and block b's mt19937 is seeded with seed + b
+// (generator.h:90), then every id goes through a permutation made by
+// shuffling 0..n-1 with mt19937(seed) (PermuteIDs, generator.h:52-62).
+// Erdos-Renyi (uniform = 1): both endpoints uniform over [0, n-1] from
+// uniform_int_distribution<int32_t> (NodeID), same blocks, no permutation
+// (MakeUniformEL, generator.h:64-79).  GAP seeds with kRandSeed; the
+// benchmark passes its own seed.
+int orc_generate_edges(int scale, int edge_factor, uint64_t seed, int uniform, uint32_t* src, uint32_t* dst) {
+  if (scale < 1 || scale > 31 || edge_factor < 1) return 1;
+  const int64_t n = int64_t(1) << scale;
+  const int64_t ne = n * edge_factor;
+  const int64_t block = int64_t(1) << 18;  // generator.h:152
+  const int64_t nblocks = (ne + block - 1) / block;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t b = 0; b < nblocks; b++) {
+    std::mt19937 rng((uint32_t)(seed + (uint64_t)b));
+    const int64_t lo = b * block, hi = std::min(ne, lo + block);
+    if (uniform) {
+      std::uniform_int_distribution<int32_t> pick(0, (int32_t)(n - 1));
+      for (int64_t e = lo; e < hi; e++) {
+        const int32_t u = pick(rng);  // sequenced: u is drawn before v
+        const int32_t v = pick(rng);
+        src[e] = (uint32_t)u;
+        dst[e] = (uint32_t)v;
+      }
+      continue;
+    }
+    std::uniform_real_distribution<float> unit(0, 1.0f);
+    const float a = 0.57f, ab = 0.57f + 0.19f, abc = 0.57f + 0.19f + 0.19f;
+    for (int64_t e = lo; e < hi; e++) {
+      uint32_t u = 0, v = 0;
+      for (int d = 0; d < scale; d++) {
+        const float x = unit(rng);
+        const bool right = x < ab ? (x > a) : (x > abc);
+        u = (u << 1) | (x < ab ? 0u : 1u);
+        v = (v << 1) | (right ? 1u : 0u);
+      }
+      src[e] = u;
+      dst[e] = v;
+    }
+  }
+  if (!uniform) {
+    std::vector<uint32_t> perm(n);
+    for (int64_t i = 0; i < n; i++) perm[i] = (uint32_t)i;
+    std::mt19937 rng((uint32_t)seed);
+    std::shuffle(perm.begin(), perm.end(), rng);
+#pragma omp parallel for
+    for (int64_t e = 0; e < ne; e++) {
+      src[e] = perm[src[e]];
+      dst[e] = perm[dst[e]];
+    }
+  }
+  return 0;
+}
+
+// Symmetric CSR of an edge list: both directions of every edge bucketed by
+// source, then the symmetric loader's clean-up (sort, unique, drop self
+// loops; IO.h:429-474) through orc_dedup_symmetric.  out_off: n+1 entries;
+// out_adj: room for 2 * num_edges entries.  Returns m, or -1 when an id is out
+// of range or m does not fit in 32 bits.
+int64_t orc_csr_from_edges(int64_t n, int64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                           uint32_t* out_off, uint32_t* out_adj) {
+  std::vector<std::atomic<uint32_t>> cnt(n);
+  for (auto& c : cnt) c.store(0, std::memory_order_relaxed);
+  bool bad = false;
+#pragma omp parallel for reduction(|| : bad)
+  for (int64_t e = 0; e < num_edges; e++) {
+    if (src[e] >= n || dst[e] >= n) { bad = true; continue; }
+    cnt[src[e]].fetch_add(1, std::memory_order_relaxed);
+    cnt[dst[e]].fetch_add(1, std::memory_order_relaxed);
+  }
+  if (bad || 2 * num_edges >= (int64_t)0xFFFFFFFFu) return -1;
+  std::vector<uint32_t> start(n);
+  uint64_t acc = 0;
+  for (int64_t v = 0; v < n; v++) { start[v] = (uint32_t)acc; acc += cnt[v].load(std::memory_order_relaxed); }
+  std::vector<std::atomic<uint32_t>> cur(n);
+  for (int64_t v = 0; v < n; v++) cur[v].store(start[v], std::memory_order_relaxed);
+  std::vector<uint32_t> raw(2 * num_edges);
+#pragma omp parallel for
+  for (int64_t e = 0; e < num_edges; e++) {
+    raw[cur[src[e]].fetch_add(1, std::memory_order_relaxed)] = dst[e];
+    raw[cur[dst[e]].fetch_add(1, std::memory_order_relaxed)] = src[e];
+  }
+  return orc_dedup_symmetric(n, 2 * num_edges, start.data(), raw.data(), out_off, out_adj);
+}
+
+// GAP's SourcePicker (GAP/src/benchmark.h:47-64): one mt19937 seeded with
+// kRandSeed (27491095, util.h:22) drives uniform_int_distribution<int32_t>
+// (NodeID) over [0, n-1]; each pick redraws until the vertex has out-degree
+// > 0, and k successive picks continue the same generator.  deg_orig is
+// indexed by the ids the picks are in.
+void orc_source_picker(int64_t n, const uint32_t* deg_orig, int k, uint32_t* out) {
+  std::mt19937 rng(27491095u);
+  std::uniform_int_distribution<int32_t> pick(0, (int32_t)(n - 1));
+  for (int i = 0; i < k; i++) {
+    int32_t v;
+    do { v = pick(rng); } while (deg_orig[v] == 0);
+    out[i] = (uint32_t)v;
+  }
+}
+
 }  // extern "C"

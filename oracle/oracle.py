@@ -50,6 +50,11 @@ def lib():
         L.orc_depths_from_parents.restype = None
         L.orc_bfs_depths.argtypes = [C.c_int64, u32p, u32p, C.c_uint32, i32p]
         L.orc_bfs_depths.restype = None
+        L.orc_generate_edges.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, u32p, u32p]
+        L.orc_csr_from_edges.argtypes = [C.c_int64, C.c_int64, u32p, u32p, u32p, u32p]
+        L.orc_csr_from_edges.restype = C.c_int64
+        L.orc_source_picker.argtypes = [C.c_int64, u32p, C.c_int, u32p]
+        L.orc_source_picker.restype = None
         _lib = L
     return _lib
 
@@ -60,6 +65,42 @@ def _p(a, t):
 
 def _u32(a):
     return np.ascontiguousarray(a, np.uint32)
+
+
+def generate_edges(scale, edge_factor, seed=1, uniform=False):
+    """The GAP generator's seeded edge list (generator.h:52-114)."""
+    ne = edge_factor << scale
+    src, dst = np.empty(ne, np.uint32), np.empty(ne, np.uint32)
+    if lib().orc_generate_edges(scale, edge_factor, seed, 1 if uniform else 0, _p(src, C.c_uint32),
+                                _p(dst, C.c_uint32)):
+        raise ValueError("bad scale or edge factor")
+    return src, dst
+
+
+def csr_from_edges(n, src, dst):
+    """Symmetric CSR of an edge list with the loader's clean-up (IO.h:429-474)."""
+    src, dst = _u32(src), _u32(dst)
+    off = np.empty(n + 1, np.uint32)
+    adj = np.empty(max(2 * len(src), 1), np.uint32)
+    m = lib().orc_csr_from_edges(n, len(src), _p(src, C.c_uint32), _p(dst, C.c_uint32), _p(off, C.c_uint32),
+                                 _p(adj, C.c_uint32))
+    if m < 0:
+        raise ValueError("edge id out of range or too many edges")
+    return off, adj[:m].copy()
+
+
+def rmat_csr(scale, edge_factor, seed=1, uniform=False):
+    """Symmetric R-MAT (or Erdos-Renyi) CSR built by the oracle alone."""
+    src, dst = generate_edges(scale, edge_factor, seed, uniform)
+    return csr_from_edges(1 << scale, src, dst)
+
+
+def source_picker(deg, k):
+    """GAP SourcePicker (benchmark.h:47-64): k roots with nonzero degree."""
+    deg = _u32(deg)
+    out = np.empty(k, np.uint32)
+    lib().orc_source_picker(len(deg), _p(deg, C.c_uint32), k, _p(out, C.c_uint32))
+    return out
 
 
 def dedup_symmetric(n, off_n, adj):

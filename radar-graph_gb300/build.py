@@ -3,7 +3,9 @@
 Compiles every CUDA translation unit for sm_103a only and the host C++ with
 OpenMP, in parallel, into radar-graph_gb300/_build/, links
 radar-graph_gb300/librg.so, then builds the command-line apps (apps/*.cc ->
-bin/PageRank, bin/BFS, bin/BC, bin/Radii) against it.  Incremental: a unit is
+bin/PageRank, bin/BFS, bin/BC, bin/Radii) against it, and the benchmark's
+measurement aid (measure/*.cu -> librg_probe.so, linked against librg.so;
+not part of the product ABI).  Incremental: a unit is
 rebuilt when its source or any header in csrc/ is newer than its object.
 
     python radar-graph_gb300/build.py [-v] [--force]
@@ -20,6 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg.so")
+MEASURE = os.path.join(HERE, "measure")
+PROBE_LIB = os.path.join(HERE, "librg_probe.so")
 APPS = os.path.join(HERE, "apps")
 BIN = os.path.join(HERE, "bin")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
@@ -93,7 +97,26 @@ def build(force=False, verbose=False):
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
     build_apps(verbose)
+    build_probe(force, verbose)
     return LIB
+
+
+def build_probe(force=False, verbose=False):
+    """librg_probe.so: measurement aids for the benchmark, linked against
+    librg.so (graph handles, the thread's stream); librg.so does not export
+    them."""
+    srcs = sorted(f for f in os.listdir(MEASURE) if f.endswith(".cu"))
+    newest = max([os.path.getmtime(os.path.join(MEASURE, f)) for f in srcs] + [_headers_mtime(), os.path.getmtime(LIB)])
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= newest:
+        return PROBE_LIB
+    cmd = [_nvcc()] + NVCC_FLAGS + ["-shared", "-o", PROBE_LIB] + [os.path.join(MEASURE, f) for f in srcs] + [
+        "-L", HERE, "-lrg", "-L", _cuda_lib_dir(), "-lcudart", "-Xlinker", "-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"probe library build failed\n{r.stdout}\n{r.stderr}")
+    return PROBE_LIB
 
 
 def build_apps(verbose=False):

@@ -502,6 +502,29 @@ rg_status bc_pick(const rg_graph* g, int k, uint32_t* out) {
   return RG_OK;
 }
 
+// Search roots by GAP's SourcePicker (GAP/src/benchmark.h:47-64): one
+// mt19937(27491095) drives uniform_int_distribution<int32_t> (NodeID) over
+// [0, n-1]; a pick is redrawn while the vertex (original id) has out-degree
+// 0, and the k picks continue the same generator.
+rg_status pick_roots(const rg_graph* g, int k, uint32_t* out) {
+  if (!g || k < 0 || (k > 0 && !out)) return fail(RG_EINVAL, "bad arguments");
+  if (g->n > 0x7FFFFFFFll) return fail(RG_EUNSUPPORTED, "SourcePicker draws int32 ids");
+  RG_TRY(host_arrays(g));
+  if (g->h_deg.size() != (size_t)g->n || (g->sorted && g->h_new_ids.size() != (size_t)g->n))
+    return fail(RG_EUNSUPPORTED, "host degree arrays missing");
+  bool any = false;
+  for (int64_t v = 0; v < g->n && !any; v++) any = g->h_deg[v] > 0;
+  if (!any && k > 0) return fail(RG_EINVAL, "graph has no edges; no root can be drawn");
+  std::mt19937 rng(27491095);
+  std::uniform_int_distribution<int32_t> ud(0, (int32_t)(g->n - 1));
+  for (int i = 0; i < k; i++) {
+    int32_t s;
+    do { s = ud(rng); } while (g->h_deg[g->sorted ? g->h_new_ids[s] : (uint32_t)s] == 0);
+    out[i] = (uint32_t)s;
+  }
+  return RG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Radii (Radii.C:140-218)
 // ---------------------------------------------------------------------------
@@ -629,6 +652,8 @@ rg_status rg_bfs(rg_graph* g, rg_variant variant, uint32_t root, uint32_t* h_par
 }
 
 rg_status rg_bc_pick_sources(const rg_graph* g, int k, uint32_t* h_sources) { return bc_pick(g, k, h_sources); }
+
+rg_status rg_pick_roots(const rg_graph* g, int k, uint32_t* h_roots) { return pick_roots(g, k, h_roots); }
 
 rg_status rg_bc(rg_graph* g, rg_variant variant, int max_iters, double* h_deps, int64_t* levels_out) {
   if (!g || max_iters < 0) return fail(RG_EINVAL, "bad arguments");

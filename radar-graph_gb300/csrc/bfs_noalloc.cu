@@ -18,7 +18,6 @@
 #include <stdint.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "rg_device.cuh"
 
@@ -35,24 +34,15 @@ constexpr size_t kScratchBytes = 2 * kQueueBytes + kBitmapBytes + kCounterBytes;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
 // Device address of the scratch array for the current device.  The symbol's
 // host-side name is only a stand-in; the address must come from
-// cudaGetSymbolAddress with the device current.  Looked up once per device.
+// cudaGetSymbolAddress with the device current.  It is looked up on every
+// call (a cheap driver query next to the per-level host syncs), so a context
+// that was reset and re-created never leaves a stale address behind.
 rg_status scratch_address(unsigned char** out) {
-  int dev = 0;
-  RG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(RG_EUNSUPPORTED, "device ordinal %d too large", dev);
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    RG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  void* p = nullptr;
+  RG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  *out = static_cast<unsigned char*>(p);
   return RG_OK;
 }
 
@@ -67,10 +57,13 @@ __global__ void noalloc_init(int32_t* depth, uint32_t n, uint32_t root, uint32_t
 }
 
 // One warp per frontier vertex; the first claim of a neighbour's visited bit
-// gives it depth `level` and a slot in the next queue.
+// gives it depth `level` and a slot in the next queue.  A neighbour id >= n
+// (a malformed CSR the caller passed as device pointers) is skipped, so it
+// can reach neither the bitmap, the queues nor depth[].
 __global__ void __launch_bounds__(256) noalloc_expand(const uint32_t* __restrict__ off, const uint32_t* __restrict__ adj,
-                                                      const uint32_t* __restrict__ q, uint32_t k, uint32_t* visited,
-                                                      uint32_t* nq, uint32_t* ncount, int32_t* depth, int32_t level) {
+                                                      const uint32_t* __restrict__ q, uint32_t k, uint32_t n,
+                                                      uint32_t* visited, uint32_t* nq, uint32_t* ncount, int32_t* depth,
+                                                      int32_t level) {
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < k; i += nwarps) {
@@ -78,6 +71,7 @@ __global__ void __launch_bounds__(256) noalloc_expand(const uint32_t* __restrict
     const uint32_t b = off[s], e = off[s + 1];
     for (uint32_t j = b + lane; j < e; j += 32) {
       const uint32_t d = adj[j];
+      if (d >= n) continue;
       const uint32_t bit = 1u << (d & 31);
       if (visited[d >> 5] & bit) continue;
       if (atomicOr(visited + (d >> 5), bit) & bit) continue;
@@ -120,7 +114,7 @@ extern "C" rg_status rg_bfs_depth_noalloc(const uint32_t* d_off, const uint32_t*
     rounds++;
     RG_CUDA(cudaMemsetAsync(counter, 0, 4, st));
     const int eb = (int)std::min<int64_t>(((int64_t)k * 32 + 255) / 256, 8192);
-    noalloc_expand<<<eb, 256, 0, st>>>(d_off, d_adj, q[cur], k, visited, q[1 - cur], counter, d_depth, (int32_t)rounds);
+    noalloc_expand<<<eb, 256, 0, st>>>(d_off, d_adj, q[cur], k, (uint32_t)n, visited, q[1 - cur], counter, d_depth, (int32_t)rounds);
     RG_CUDA(cudaGetLastError());
     uint32_t next = 0;
     RG_CUDA(cudaMemcpyAsync(&next, counter, 4, cudaMemcpyDeviceToHost, st));

@@ -67,8 +67,9 @@ __device__ __forceinline__ uint32_t hub_vertex(const HubInfo& h, uint32_t slot) 
 struct OpPr {
   const double* __restrict__ contrib;
   double* p_next;
-  // hub copies accumulate in fx63 fixed point (integer shared-memory atomics)
-  using HubT = unsigned long long;
+  // hub copies are FP64 like the reference's thread-private p_next_dup
+  // (PageRank.C:42-70): shared-memory double adds, merged with one add
+  using HubT = double;
   static constexpr int kPull = kPullSum;
   static constexpr bool kOutput = false;
   __device__ __forceinline__ bool cond(uint32_t) const { return true; }
@@ -76,12 +77,12 @@ struct OpPr {
     atomicAdd(p_next + d, contrib[s]);
     return false;
   }
-  __device__ static HubT hub_identity() { return 0ull; }
+  __device__ static HubT hub_identity() { return 0.0; }
   __device__ __forceinline__ void hub_push(HubT* hs, uint32_t slot, uint32_t s, uint32_t) const {
-    atomicAdd(hs + slot, (unsigned long long)to_fx63(contrib[s]));
+    atomicAdd(hs + slot, contrib[s]);
   }
   __device__ __forceinline__ bool hub_merge(uint32_t v, HubT x) const {
-    if (x != 0ull) atomicAdd(p_next + v, from_fx63(x));
+    if (x != 0.0) atomicAdd(p_next + v, x);
     return false;
   }
   using PullT = double;

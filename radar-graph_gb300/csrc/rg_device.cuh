@@ -278,26 +278,12 @@ __device__ __forceinline__ uint32_t upper_index(const T* a, uint32_t lo, uint32_
 
 // ---- exact fixed-point accumulation on the integer pipes -----------------
 // GB300 executes few FP64 operations per clock, so per-edge double additions
-// (and double CAS loops on shared memory) bound the PageRank sweeps.  Sums of
-// non-negative doubles are instead accumulated as integers:
-//   fx63:  u64, value * 2^63, for sums in [0, 2) (PageRank: a vertex's
-//          incoming mass never exceeds the total mass 1).  Each term is
-//          truncated below 2^-63 (absolute error < 1.1e-19 per term).
+// (and double CAS loops on shared memory) bound the sweeps.  Sums of
+// non-negative doubles can instead be accumulated as integers:
 //   fx100: 128 bits (hi, lo), value * 2^100, for sums below 2^27; terms are
 //          truncated below 2^-100.
 // Conversion reads the IEEE fields with integer operations only; converting
 // a finished sum back to double rounds once.
-
-__device__ __forceinline__ uint64_t to_fx63(double x) {
-  const uint64_t b = (uint64_t)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) return 0;  // zero or subnormal (below 2^-1022)
-  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = e - 1075 + 63;  // x = m * 2^(e-1075)
-  if (sh >= 0) return m << sh;   // sh <= 11 for x < 2
-  return sh <= -64 ? 0ull : (m >> (-sh));
-}
-__device__ __forceinline__ double from_fx63(uint64_t v) { return __ull2double_rn(v) * 1.0842021724855044340e-19; }
 
 struct Fx100 {
   uint64_t lo, hi;

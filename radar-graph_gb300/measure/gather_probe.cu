@@ -4,6 +4,11 @@
 // Every pull over the graph (the PageRank sweep, the bitmask sweeps) does at
 // least this work, so it is the achievable ceiling those kernels are measured
 // against, next to the HBM copy bandwidth.
+//
+// A measurement aid, not part of the engine: it is built into its own
+// library (librg_probe.so, linked against librg.so for the graph handle and
+// the thread's stream) that only the benchmark loads; librg.so does not
+// export it.
 
 #include <cuda_runtime.h>
 
@@ -33,9 +38,9 @@ __global__ void __launch_bounds__(256) gather_probe(const uint32_t* __restrict__
 
 using namespace rg;
 
-extern "C" rg_status rg_gather_probe(rg_graph* g, int reps, double* best_ms) {
-  if (!g || reps < 1 || !best_ms) return fail(RG_EINVAL, "rg_gather_probe: bad arguments");
-  if (g->m == 0) return fail(RG_EINVAL, "rg_gather_probe: graph has no edges");
+extern "C" rg_status rg_probe_gather_ceiling(rg_graph* g, int reps, double* best_ms) {
+  if (!g || reps < 1 || !best_ms) return fail(RG_EINVAL, "rg_probe_gather_ceiling: bad arguments");
+  if (g->m == 0) return fail(RG_EINVAL, "rg_probe_gather_ceiling: graph has no edges");
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   cudaStream_t st = cx->stream;

@@ -78,6 +78,7 @@ _SIGS = {
     "rg_bc": [C.c_void_p, C.c_int, C.c_int, _f64p, _i64p],
     "rg_bc_sources": [C.c_void_p, C.c_int, _u32p, C.c_int, _f64p, _i64p],
     "rg_bc_pick_sources": [C.c_void_p, C.c_int, _u32p],
+    "rg_pick_roots": [C.c_void_p, C.c_int, _u32p],
     "rg_radii": [C.c_void_p, C.c_int, _i32p, _i64p],
     "rg_radii_seeds": [C.c_void_p, C.c_int, _u32p, C.c_int, _i32p, _i64p],
     "rg_frontier_create": [C.c_void_p, C.c_void_p],
@@ -117,7 +118,6 @@ _SIGS = {
     "rg_graph_clear_tuning": [C.c_void_p],
     "rg_graph_set_tuned_option": [C.c_void_p, C.c_int, C.c_int, C.c_int64],
     "rg_pinned_alloc": [C.c_size_t, _P(C.c_void_p)],
-    "rg_gather_probe": [C.c_void_p, C.c_int, _P(C.c_double)],
     "rg_graph_create_directed": [C.c_int64, C.c_int64, _u32p, _u32p, _P(C.c_void_p)],
     "rg_graph_is_directed": [C.c_void_p, _P(C.c_int)],
     "rg_graph_degree_sort_by": [C.c_void_p, C.c_int, _P(C.c_void_p), _u32p],
@@ -507,6 +507,12 @@ class Graph:
         _check(lib().rg_bc_pick_sources(self._h, k, _ptr(out, C.c_uint32)))
         return out
 
+    def pick_roots(self, k):
+        """k search roots (original ids) by GAP's SourcePicker rule."""
+        out = np.empty(k, np.uint32)
+        _check(lib().rg_pick_roots(self._h, k, _ptr(out, C.c_uint32)))
+        return out
+
     def radii(self, variant="push", out=None):
         r = np.empty(self.n, np.int32) if out is None else out
         rounds = C.c_int64()
@@ -551,17 +557,6 @@ def _graph_autotune(self, variant="radar"):
 
 
 Graph.autotune = _graph_autotune
-
-
-def _graph_gather_probe(self, reps=5):
-    """Best time (ms) to stream the edge array and gather 8 bytes per edge:
-    the ceiling of any pull over this graph."""
-    ms = C.c_double()
-    _check(lib().rg_gather_probe(self._h, reps, C.byref(ms)))
-    return ms.value
-
-
-Graph.gather_probe = _graph_gather_probe
 
 
 def _graph_set_tuning(self, tuning):

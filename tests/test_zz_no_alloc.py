@@ -67,3 +67,24 @@ def test_noalloc_rejects_graphs_beyond_the_scratch_limit():
         assert b"scratch limit" in L.rg_last_error()
     finally:
         L.rg_device_free(tiny)
+
+
+def test_noalloc_skips_neighbour_ids_beyond_n():
+    """A CSR passed as device pointers cannot be validated on the host: a
+    neighbour id >= n is skipped by the kernel instead of indexing past the
+    caller's depth array (path 0-1-2 with a stray id 7 in vertex 0's list)."""
+    L = rg.lib()
+    off = np.array([0, 2, 4, 5], np.uint32)
+    adj = np.array([1, 7, 0, 2, 1], np.uint32)
+    d_off, d_adj = _dev_copy(L, off), _dev_copy(L, adj)
+    d_depth = _dev_copy(L, np.zeros(3, np.int32))
+    try:
+        rounds = C.c_int64()
+        rg._check(L.rg_bfs_depth_noalloc(d_off, d_adj, 3, 5, 0, d_depth, None, C.byref(rounds)))
+        got = np.empty(3, np.int32)
+        rg._check(L.rg_copy_to_host(got.ctypes.data, d_depth, got.nbytes))
+        assert got.tolist() == [0, 1, 2]
+        assert rounds.value == 3
+    finally:
+        for p in (d_off, d_adj, d_depth):
+            L.rg_device_free(p)
