@@ -762,6 +762,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served legs")
     ap.add_argument("--only", default="", help="comma list of extra legs to run (default all): " + ",".join(EXTRA_LEGS))
     ap.add_argument("--cpu-pr-iters", type=int, default=2)
+    ap.add_argument("--step-only", action="store_true",
+                    help="stop after the timed step (for profiler captures of it): no e2e, legs or CPU baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -806,6 +808,14 @@ def main():
     clk = clocks.stop()
     rg.set_kernel_timing(False)
     value, ms_step = replica_rate(pg, tot_ms / args.steps, tot_edges / args.steps)
+    if args.step_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+                              "config": bench_config(args.scale, n, m), "gpu_launches": int(launches),
+                              "note": "--step-only: the timed step alone, for profiler captures"}), flush=True)
+        gs.free()
+        return 0
 
     # roofline of the dominant kernel: the PageRank edge sweep (pull or push,
     # whichever the autotuner chose), timed per launch with CUDA events

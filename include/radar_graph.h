@@ -41,8 +41,9 @@ typedef enum rg_status {
   RG_EIO = 4,           /* a file could not be opened or read */
   RG_EFORMAT = 5,       /* malformed input ("Bad input file", IO.h:235-248) */
   RG_EUNSUPPORTED = 6,  /* option or size the engine does not implement */
-  RG_ETIMEOUT = 7,      /* a bounded device-side wait ran out */
-  RG_ENODEV = 8         /* no usable CUDA device */
+  RG_ETIMEOUT = 7,      /* a bounded wait ran out (rg_server_wait_for) */
+  RG_ENODEV = 8,        /* no usable CUDA device */
+  RG_ECANCELED = 9      /* the query was cancelled (rg_server_cancel) */
 } rg_status;
 
 /* The five reference variants (src/<variant>/). */
@@ -287,7 +288,8 @@ rg_status rg_batch_free(rg_batch* b);
  * (rg_bfs_multi / rg_bc_multi) when the batch reaches the size at which that
  * beats one traversal per query (measured per graph at creation); a batch is
  * admitted when its estimated device memory fits hbm_fraction of the HBM free
- * at start.  Results equal the single-query entry points (BC within 1e-9
+ * at start beside running batches and unfetched results, or when no other
+ * batch is running.  Results equal the single-query entry points (BC within 1e-9
  * relative):
  *   RG_QUERY_BFS   source = root (ORIGINAL id) -> int32[n] depths (rg_bfs)
  *   RG_QUERY_BC    source = BC source           -> double[n] (rg_bc_sources
@@ -304,6 +306,9 @@ typedef struct rg_server_stats {
   double p50_ms;      /* submit-to-result latency percentiles */
   double p99_ms;
   double qps;         /* completed / (last completion - first submission) */
+  int64_t admission_waits; /* batches that waited for HBM budget before running */
+  int64_t cancelled;  /* rg_server_cancel calls that took effect */
+  int32_t peak_running; /* most batches on the device at once */
 } rg_server_stats;
 rg_status rg_server_create(rg_graph* const* graphs, int ngraphs, int nworkers, int max_batch,
                            double hbm_fraction, rg_server** out);
@@ -311,9 +316,23 @@ rg_status rg_server_submit(rg_server* s, int graph, rg_query_kind kind, uint32_t
                            uint64_t* ticket);
 /* Blocks until the query is done and copies its result (bytes >= result)
  * from device memory straight into h_result (fastest when h_result comes
- * from rg_pinned_alloc); the result's device memory is then released. */
+ * from rg_pinned_alloc); the result's device memory is then released.
+ * RG_ECANCELED if the query was cancelled. */
 rg_status rg_server_wait(rg_server* s, uint64_t ticket, void* h_result, size_t bytes,
                          double* latency_ms);
+/* rg_server_wait with a limit: RG_ETIMEOUT when the query is not done within
+ * timeout_ms (negative = no limit); the ticket stays valid, to be waited on
+ * again or cancelled.  The reference has no serving layer; this is the
+ * bounded wait its error model lacks (it blocks or aborts). */
+rg_status rg_server_wait_for(rg_server* s, uint64_t ticket, void* h_result, size_t bytes,
+                             double* latency_ms, double timeout_ms);
+/* Cancels a query: a query still waiting never runs; a running one has its
+ * result dropped when its batch ends; a finished, unfetched one releases its
+ * result now.  A later wait on the ticket returns RG_ECANCELED. */
+rg_status rg_server_cancel(rg_server* s, uint64_t ticket);
+/* paused != 0: workers take no new queries (running batches finish);
+ * 0 resumes.  Queries submitted meanwhile wait in arrival order. */
+rg_status rg_server_pause(rg_server* s, int paused);
 /* Page-locked host memory for result buffers (cudaHostAlloc). */
 rg_status rg_pinned_alloc(size_t bytes, void** h_ptr);
 rg_status rg_pinned_free(void* h_ptr);
@@ -387,6 +406,9 @@ rg_status rg_device_free(void* d_ptr);
 rg_status rg_copy_to_device(void* d_dst, const void* h_src, size_t bytes);
 rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes);
 rg_status rg_synchronize(void);
+/* The current device: its name (NUL-terminated, at most name_len bytes), SM
+ * count and nominal HBM bandwidth in GB/s (memory clock x bus width x 2). */
+rg_status rg_device_info(char* name, int name_len, int32_t* sms, double* nominal_hbm_gbs);
 
 /* ------------------------------------------------------------------------
  * Allocation-free BFS.  No counterpart in the reference: it exists for
@@ -475,6 +497,23 @@ rg_status rg_last_timing(rg_timing* t);
 /* on != 0: every edge-kernel launch of the following app calls is bracketed
  * by CUDA events on its stream and rg_timing.edge_ms reports their sum. */
 rg_status rg_set_kernel_timing(int on);
+
+/* Per-level trace of the calling thread's edgeMaps: the GPU form of Ligra's
+ * frontierStats (ligra.h:357-370), which prints PUSH or PULL and the
+ * frontier's size per iteration.  While tracing is on (rg_set_trace(1)) each
+ * edgeMap of the apps and of rg_edgemap appends one record; rg_trace_take
+ * copies up to cap records (oldest first) and clears the list.  Each edgeMap
+ * is also an NVTX range ("edgeMap sparse-push", "edgeMap dense-push",
+ * "edgeMap pull") for a profiler that records NVTX. */
+typedef struct rg_level_trace {
+  int32_t mode;       /* 0 sparse push, 1 dense push, 2 pull */
+  int32_t hub_mode;   /* push hub copies: 0 none, 1 ids < H (RADAR), 2 hub map (HUBDUP) */
+  int64_t frontier;   /* vertices in the input frontier */
+  int64_t degsum;     /* their out-degree sum (edges the map examines) */
+  int64_t threshold;  /* dense when frontier + degsum > threshold (ligra.h:283) */
+} rg_level_trace;
+rg_status rg_set_trace(int on);
+rg_status rg_trace_take(rg_level_trace* h_out, int64_t cap, int64_t* count);
 
 #ifdef __cplusplus
 }

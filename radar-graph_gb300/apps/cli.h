@@ -62,6 +62,10 @@ struct Graph {
   rg_variant variant = RG_RADAR;
   int64_t n = 0, m = 0;
   bool sorted = false;
+  const char* file = "";
+  const char* variant_name = "radar";
+  double peak_gbs = 0;    // HBM roofline denominator of the JSON line
+  const char* peak_kind = "nominal";
 };
 
 inline void die(const char* what) {
@@ -119,12 +123,42 @@ void write_output(const commandLine& P, const std::vector<T>& v) {
   fclose(f);
 }
 
+// JSON string body: the path with quotes, backslashes and control bytes escaped
+inline void json_str(FILE* f, const char* x) {
+  fputc('"', f);
+  for (const unsigned char* c = (const unsigned char*)x; *c; c++) {
+    if (*c == '"' || *c == '\\') fprintf(f, "\\%c", *c);
+    else if (*c < 0x20) fprintf(f, "\\u%04x", *c);
+    else fputc(*c, f);
+  }
+  fputc('"', f);
+}
+
+// The reference's "Run Time(sec)" line (PageRank.C:185-186 and the other
+// apps' ends), then one JSON result line: app, variant, graph, size, time,
+// GTEPS and the fraction of the HBM roofline the call's algorithmic bytes
+// reached (peak: -hbm-gbs or $RG_HBM_GBS, e.g. a measured copy bandwidth;
+// else the device's nominal figure).
 inline void report(const char* app, const Graph& G, double secs) {
   rg_timing t;
   if (rg_last_timing(&t) != RG_OK) memset(&t, 0, sizeof t);
+  const double gteps = t.total_ms > 0 ? (double)t.edges_traversed / (t.total_ms * 1e6) : 0.0;
   printf("Run Time(sec) : %.6f   [%s, %s graph, device %.3f ms, %lld edges, %.2f GTEPS]\n", secs, app,
-         G.sorted ? "degree-sorted" : "original", t.total_ms, (long long)t.edges_traversed,
-         t.total_ms > 0 ? (double)t.edges_traversed / (t.total_ms * 1e6) : 0.0);
+         G.sorted ? "degree-sorted" : "original", t.total_ms, (long long)t.edges_traversed, gteps);
+  char gpu[256] = "";
+  rg_device_info(gpu, sizeof gpu, nullptr, nullptr);
+  const double gbs = t.total_ms > 0 ? (double)t.algorithmic_bytes / (t.total_ms * 1e6) : 0.0;
+  printf("{\"app\": \"%s\", \"variant\": \"%s\", \"graph\": ", app, G.variant_name);
+  json_str(stdout, G.file);
+  printf(", \"n\": %lld, \"m\": %lld, \"degree_sorted\": %s, \"run_time_s\": %.6f, \"device_ms\": %.4f, "
+         "\"edges\": %lld, \"gteps\": %.6g, \"algorithmic_bytes\": %lld, \"achieved_gbs\": %.6g, "
+         "\"hbm_peak_gbs\": %.1f, \"peak_kind\": \"%s\", \"hbm_frac\": %.6g, \"gpu\": ",
+         (long long)G.n, (long long)G.m, G.sorted ? "true" : "false", secs, t.total_ms,
+         (long long)t.edges_traversed, gteps, (long long)t.algorithmic_bytes, gbs, G.peak_gbs, G.peak_kind,
+         G.peak_gbs > 0 ? gbs / G.peak_gbs : 0.0);
+  json_str(stdout, gpu);
+  printf("}\n");
+  fflush(stdout);
 }
 
 using ComputeFn = void (*)(Graph&, commandLine&);
@@ -136,12 +170,21 @@ inline int run(int argc, char** argv, ComputeFn compute) {
   if (argc < 2 || !file || file[0] == '-') {
     fprintf(stderr,
             "usage: %s [-s] [-b] [-rounds R] [-preprocess p] [-r root] [-maxiters k] "
-            "[-variant push|push-pull|degree-sorting|hubdup|radar] [-out file] <graph>\n",
+            "[-variant push|push-pull|degree-sorting|hubdup|radar] [-out file] [-hbm-gbs GB/s] <graph>\n",
             argv[0]);
     return 2;
   }
   Graph G;
-  G.variant = parse_variant(P.getOptionValue("-variant", "radar"));
+  G.file = file;
+  G.variant_name = P.getOptionValue("-variant", "radar");
+  G.variant = parse_variant(G.variant_name);
+  const char* peak = P.getOptionValue("-hbm-gbs", getenv("RG_HBM_GBS"));
+  if (peak && atof(peak) > 0) {
+    G.peak_gbs = atof(peak);
+    G.peak_kind = "given";
+  } else {
+    rg_device_info(nullptr, 0, nullptr, &G.peak_gbs);  // nominal; 0 without a device
+  }
   const bool symmetric = P.getOption("-s");  // without -s the graph is directed
   const long rounds = P.getOptionLongValue("-rounds", 3);
   // degree-sorting and RADAR sort by default (-preprocess 1); the others do not

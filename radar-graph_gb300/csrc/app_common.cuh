@@ -10,6 +10,8 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.cuh"
 #include "rg_device.cuh"
 
@@ -17,6 +19,15 @@ namespace rg {
 
 extern thread_local rg_timing g_timing;
 extern bool g_kernel_timing;
+// rg_set_trace: the calling thread's per-level edgeMap records
+extern thread_local bool g_trace_on;
+extern thread_local std::vector<rg_level_trace> g_trace;
+
+// NVTX range for the lifetime of the object (no cost without a profiler)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 // rg_set_option values
 // The calling thread's options (rg_set_option).  An app call on a graph that
@@ -243,6 +254,12 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
     // direction 1 pulls dense levels whatever the variant (no atomics; BFS's
     // pull also exits at the first frontier neighbour)
     const bool pull = dense && (!o.dense_forward || g_opts.direction == 1);
+    NvtxRange nvtx(pull ? "edgeMap pull" : dense ? "edgeMap dense-push" : "edgeMap sparse-push");
+    if (g_trace_on) {
+      const int hm_t = (!pull && o.hubs && in.degsum >= kHubMinEdges && g_opts.hub_smem_kb > 0) ? hub_mode_of(o.variant)
+                                                                                                : kHubNone;
+      g_trace.push_back(rg_level_trace{pull ? 2 : dense ? 1 : 0, hm_t, in.count, in.degsum, threshold});
+    }
     const bool tr = o.transpose && g->directed;
     const DevGraph push_g = tr ? g->in_view() : g->view();
     const DevGraph pull_g = tr ? g->view() : g->in_view();

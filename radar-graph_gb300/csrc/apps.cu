@@ -27,6 +27,8 @@ namespace rg {
 // ---------------------------------------------------------------------------
 thread_local rg_timing g_timing;
 bool g_kernel_timing = false;
+thread_local bool g_trace_on = false;
+thread_local std::vector<rg_level_trace> g_trace;
 thread_local std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_kt_events;
 thread_local size_t g_kt_used = 0;
 
@@ -678,6 +680,21 @@ rg_status rg_radii(rg_graph* g, rg_variant variant, int32_t* h_radii, int64_t* r
 rg_status rg_radii_seeds(rg_graph* g, rg_variant variant, const uint32_t* h_seeds, int k, int32_t* h_radii,
                          int64_t* rounds_out) {
   return radii_run(g, variant, h_seeds, k, h_radii, rounds_out, 0);
+}
+
+rg_status rg_set_trace(int on) {
+  g_trace_on = on != 0;
+  if (!g_trace_on) g_trace.clear();
+  return RG_OK;
+}
+
+rg_status rg_trace_take(rg_level_trace* h_out, int64_t cap, int64_t* count) {
+  if (cap < 0 || (cap > 0 && !h_out) || !count) return fail(RG_EINVAL, "rg_trace_take: bad arguments");
+  const int64_t k = std::min<int64_t>(cap, (int64_t)g_trace.size());
+  std::copy(g_trace.begin(), g_trace.begin() + k, h_out);
+  *count = k;
+  g_trace.clear();
+  return RG_OK;
 }
 
 rg_status rg_set_option(rg_option opt, int64_t value) {

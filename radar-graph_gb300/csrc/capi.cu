@@ -1,6 +1,7 @@
 // C ABI glue: error strings, host-side format entry points, device buffers.
 
 #include <cuda_runtime.h>
+#include <stdio.h>
 #include <stdlib.h>
 
 #include "rg_device.cuh"
@@ -25,8 +26,9 @@ const char* rg_status_str(rg_status s) {
     case RG_EIO: return "I/O error";
     case RG_EFORMAT: return "bad input format";
     case RG_EUNSUPPORTED: return "unsupported";
-    case RG_ETIMEOUT: return "device wait timed out";
+    case RG_ETIMEOUT: return "wait timed out";
     case RG_ENODEV: return "no CUDA device";
+    case RG_ECANCELED: return "cancelled";
   }
   return "unknown status";
 }
@@ -85,6 +87,24 @@ rg_status rg_copy_to_device(void* d_dst, const void* h_src, size_t bytes) {
 rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes) {
   if ((!h_dst || !d_src) && bytes) return fail(RG_EINVAL, "null pointer");
   RG_CUDA(cudaMemcpy(h_dst, d_src, bytes, cudaMemcpyDeviceToHost));
+  return RG_OK;
+}
+
+rg_status rg_device_info(char* name, int name_len, int32_t* sms, double* nominal_hbm_gbs) {
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  if (name && name_len > 0) {
+    cudaDeviceProp p;
+    RG_CUDA(cudaGetDeviceProperties(&p, dev));
+    snprintf(name, (size_t)name_len, "%s", p.name);
+  }
+  if (sms) RG_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
+  if (nominal_hbm_gbs) {
+    int khz = 0, bits = 0;
+    RG_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrMemoryClockRate, dev));
+    RG_CUDA(cudaDeviceGetAttribute(&bits, cudaDevAttrGlobalMemoryBusWidth, dev));
+    *nominal_hbm_gbs = 2.0 * (double)khz * 1e3 * (double)bits / 8.0 / 1e9;
+  }
   return RG_OK;
 }
 

@@ -10,7 +10,7 @@
 // up to 64 BFS queries cost one traversal.
 //
 // The persistent batch kernel runs, for every graph of a set, a 64-source BFS
-// and a PageRank (the integer pipeline of pagerank.cu), each task owned by one
+// and a PageRank (the exact-sum arithmetic of pagerank.cu), each task owned by one
 // CTA from start to finish: CTAs take tasks from an atomic counter (largest
 // graphs first) and synchronise only with __syncthreads, never with each
 // other, so no CTA ever waits on another.
@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "app_common.cuh"
+#include "pr_exact.cuh"
 
 namespace rg {
 
@@ -184,8 +185,7 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
 namespace {
 
 constexpr int kBatchThreads = 1024;
-constexpr uint64_t kDampFx64 = 15679732462653118464ull;  // double(0.85) * 2^64 (as in pagerank.cu)
-constexpr uint64_t kEpsFx = 922337203686ull;              // 1e-7 * 2^63, rounded up
+constexpr double kDamp = 0.85;  // PageRank.C:126
 
 struct BatchDesc {
   const uint64_t* vbase;    // per graph: first vertex slot in the per-vertex arrays
@@ -199,9 +199,9 @@ struct BatchDesc {
   unsigned long long* N;
   unsigned long long* seen;
   int32_t* depth;           // per graph: k rows of n_g depths at 64 * vbase[g]
-  uint64_t* p;              // PageRank ranks (fx63)
-  uint64_t* acc;
-  uint64_t* contrib;
+  double* p;                // PageRank ranks
+  double* acc;              // the iteration's new ranks
+  double* contrib;          // p / deg
   double* ranks;            // results
   int32_t* pr_iters;        // per graph: iterations run (PageRank.C's iter)
   const int32_t* task;      // task list: graph * 2 + kind (0 BFS, 1 PageRank), largest first
@@ -292,59 +292,73 @@ __device__ void batch_msbfs(const BatchDesc& D, int gi) {
   }
 }
 
+// One graph's PageRank inside the persistent kernel, with the arithmetic of
+// pagerank.cu's pull (pr_exact.cuh): FP64 contributions p/deg, each
+// vertex's sum formed exactly (128-bit fixed point) and rounded once,
+// p' = fma(0.85, sum, 0.15/n), exact L1.  Sums do not depend on the order of
+// the additions, so the ranks equal rg_pagerank's bit for bit.
 __device__ void batch_pagerank(const BatchDesc& D, int gi) {
   const uint64_t vb = D.vbase[gi];
   const uint32_t n = D.nv[gi];
   const uint32_t* off = D.off + vb + gi;
   const uint32_t* adj = D.adj + D.ebase[gi];
-  uint64_t* p = D.p + vb;
-  uint64_t* acc = D.acc + vb;
-  uint64_t* contrib = D.contrib + vb;
+  double* p = D.p + vb;
+  double* acc = D.acc + vb;
+  double* contrib = D.contrib + vb;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kBatchThreads / 32;
-  // the reference's constants (PageRank.C:126-138), scaled exactly as in pagerank.cu
-  const double one_over_n = 1 / (double)n;
-  const uint64_t p0 = (uint64_t)(one_over_n * 9.223372036854775808e18);
-  const uint64_t added = (uint64_t)((1 - 0.85) * (1 / (double)n) * 9.223372036854775808e18);
-  __shared__ unsigned long long s_l1;
+  // the reference's constants (PageRank.C:126-138)
+  const double p0 = 1 / (double)n;
+  const double added = (1 - kDamp) * (1 / (double)n);
+  const U128 eps = pr_eps_fx();
+  __shared__ U128 s_l1;
   for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) {
     p[v] = p0;
     const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? p0 / d : 0ull;
+    contrib[v] = d ? p0 / (double)d : 0.0;
   }
   __syncthreads();
   int64_t it = 0;
   bool broke = false;
   while (it < D.max_iters) {
     it++;
-    if (threadIdx.x == 0) s_l1 = 0;
+    if (threadIdx.x == 0) s_l1 = U128{0ull, 0ull};
     __syncthreads();
-    unsigned long long l1 = 0;
+    U128 l1{0ull, 0ull};
     for (uint32_t v = warp; v < n; v += nw) {  // pull: a warp per row
-      unsigned long long s = 0;
-      for (uint32_t j = off[v] + lane; j < off[v + 1]; j += 32) s += contrib[adj[j]];
-      s = warp_sum(s);
+      U128 s{0ull, 0ull};
+      for (uint32_t j = off[v] + lane; j < off[v + 1]; j += 32) add128(s, fx_from_double(contrib[adj[j]]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        add128(s, U128{__shfl_xor_sync(0xffffffffu, s.lo, o), __shfl_xor_sync(0xffffffffu, s.hi, o)});
+      }
       if (lane == 0) {
-        const uint64_t pn = __umul64hi(s, kDampFx64) + added;
-        const uint64_t po = p[v];
-        l1 += pn > po ? pn - po : po - pn;
+        const double pn = fma(kDamp, fx_to_double(s), added);
+        add128(l1, fx_from_double(fabs(p[v] - pn)));
         acc[v] = pn;
       }
     }
-    l1 = warp_sum(l1);
-    if (lane == 0) atomicAdd(&s_l1, l1);
-    __syncthreads();
-    for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) {
-      const uint64_t pn = acc[v];
-      p[v] = pn;
-      const uint32_t d = off[v + 1] - off[v];
-      contrib[v] = d ? pn / d : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      add128(l1, U128{__shfl_xor_sync(0xffffffffu, l1.lo, o), __shfl_xor_sync(0xffffffffu, l1.hi, o)});
+    }
+    if (lane == 0 && (l1.lo | l1.hi)) {
+      const unsigned long long old = atomicAdd(&s_l1.lo, l1.lo);
+      const unsigned long long hi = l1.hi + (old + l1.lo < old ? 1ull : 0ull);
+      if (hi) atomicAdd(&s_l1.hi, hi);
     }
     __syncthreads();
-    const bool conv = s_l1 < kEpsFx;
+    for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) {
+      const double pn = acc[v];
+      p[v] = pn;
+      const uint32_t d = off[v + 1] - off[v];
+      contrib[v] = d ? pn / (double)d : 0.0;
+    }
+    __syncthreads();
+    const bool conv = less128(s_l1, eps);
     __syncthreads();  // every thread has read the sum before thread 0 resets it
     if (conv) { broke = true; break; }
   }
-  for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) D.ranks[vb + v] = __ull2double_rn(p[v]) * 1.0842021724855044340e-19;
+  for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) D.ranks[vb + v] = p[v];
   if (threadIdx.x == 0) D.pr_iters[gi] = (int32_t)(broke ? it : D.max_iters + 1);
 }
 
@@ -487,9 +501,9 @@ extern "C" rg_status rg_batch_run(rg_batch* b, const uint32_t* h_sources, int k,
   D.N = b->d_N.as<unsigned long long>();
   D.seen = b->d_seen.as<unsigned long long>();
   D.depth = b->d_depth.as<int32_t>();
-  D.p = b->d_p.as<uint64_t>();
-  D.acc = b->d_acc.as<uint64_t>();
-  D.contrib = b->d_contrib.as<uint64_t>();
+  D.p = b->d_p.as<double>();
+  D.acc = b->d_acc.as<double>();
+  D.contrib = b->d_contrib.as<double>();
   D.ranks = b->d_ranks.as<double>();
   D.pr_iters = b->d_iters.as<int32_t>();
   D.task = b->d_task.as<int32_t>();

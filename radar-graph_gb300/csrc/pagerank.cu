@@ -1,23 +1,25 @@
-// PageRank (PageRank.C:120-189) on the device.
+// PageRank (PageRank.C:120-189) on the device, in the reference's double
+// precision.
 //
-// The iteration is kept entirely on the integer pipes: GB300 issues very few
-// FP64 instructions per clock, so a double add per edge -- or a double divide
-// per vertex -- costs more than the memory traffic.  Ranks, contributions and
-// sums are held in fx63 fixed point (u64 = value * 2^63).  This is exact for
-// PageRank's value range: every rank and every vertex's incoming sum is at
-// most the total mass 1 < 2.
-//   contrib[s] = floor(p[s] * 2^63 / deg(s))        (PR_F's p_curr[s]/deg(s))
-//   acc[d]    += contrib[s]  over the edges          (exact integer sums)
-//   p'[v]      = floor(acc[v] * 0.85) + 0.15/n       (PR_Vertex_F, 0.85 and
-//                0.15/n are the reference's double constants scaled by 2^64
-//                and 2^63)
-//   L1         = sum |p[v] - p'[v]|                  (exact, u64)
-// Each term is truncated below 2^-63 (1.1e-19), far below the 1e-9 relative
-// tolerance for graphs up to ~2^28 vertices; the sums are order independent,
-// so results are deterministic.  Ranks are converted to double once, at the
-// end.  The L1 < 1e-7 break (PageRank.C:172) is taken on the device: every
-// kernel of iteration i returns at once if iteration i-1 converged, so a whole
-// run is enqueued without host round trips.
+// Per iteration, like the reference:
+//   contrib[s] = p[s] / deg(s)            the IEEE double quotient PR_F forms
+//                                         per edge (PageRank.C:48), formed once
+//                                         per vertex
+//   acc[d]    += contrib[s] over edges     PR_F's additions
+//   p'[v]      = 0.85 * acc[v] + 0.15/n    PR_Vertex_F (fused multiply-add, as
+//                                         the reference compiles it with FMA)
+//   L1         = sum |p[v] - p'[v]|        PageRank.C:168-170, break at < 1e-7
+// The edge pass differs from the reference only in how it adds.  The pull
+// (every schedule the autotuner picks on large graphs, and the push-pull
+// variant) forms each acc[d] EXACTLY, as a 128-bit fixed-point sum of the
+// doubles (pr_exact.cuh), rounded to the nearest double once: the ranks are
+// the correctly rounded sums of the reference's own terms, the same in every
+// run.  The push (the reference's dense_forward schedule) adds with FP64
+// atomics in arbitrary order, as the reference's CAS loop (utils.h:334-339)
+// does; its per-CTA hub copies sum exactly and merge with one FP64 add.
+// The L1 sum is exact too.  The L1 < 1e-7 break is taken on the device:
+// every kernel of iteration i returns at once if iteration i-1 converged, so
+// a whole run is enqueued without host round trips.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -29,6 +31,7 @@
 #include <vector>
 
 #include "app_common.cuh"
+#include "pr_exact.cuh"
 
 namespace rg {
 
@@ -36,40 +39,75 @@ namespace {
 
 constexpr int kSweepThreads = 1024;  // push sweep CTA (one per SM with hub copies)
 constexpr int kPullThreads = 256;
-// double(0.85) * 2^64, exact (the double nearest 0.85 times a power of two)
-constexpr uint64_t kDampFx64 = 15679732462653118464ull;
-// 1e-7 * 2^63 rounded up: L1_fx < kEpsFx  <=>  L1 < 1e-7
-constexpr uint64_t kEpsFx = 922337203686ull;
+constexpr double kDamp = 0.85;       // PageRank.C:126
+constexpr uint32_t kNoRow = 0xFFFFFFFFu;
 
-__device__ __forceinline__ bool converged(const uint64_t* l1_prev) {
-  return l1_prev != nullptr && *l1_prev < kEpsFx;
+// L1 of the previous iteration (exact) below 1e-7: this iteration is skipped.
+__device__ __forceinline__ bool converged(const U128* l1_prev) {
+  return l1_prev != nullptr && less128(*l1_prev, pr_eps_fx());
 }
 
-__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, uint64_t* p, uint64_t* acc,
-                        uint64_t* contrib, uint64_t p0) {
+// acc[v] += x for a 128-bit sum shared with other warps: the low word's
+// atomic returns the old value, so the carry out of it is known and goes into
+// the high word.  Every carry is counted once, so the final sum is exact.
+__device__ __forceinline__ void atomic_add128(U128* p, const U128& x) {
+  const unsigned long long old = atomicAdd(&p->lo, x.lo);
+  const unsigned long long hi = x.hi + (old + x.lo < old ? 1ull : 0ull);
+  if (hi) atomicAdd(&p->hi, hi);
+}
+
+__device__ __forceinline__ void store128(U128* p, const U128& x) {
+  asm volatile("st.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(x.lo), "l"(x.hi) : "memory");
+}
+
+__device__ __forceinline__ U128 shfl_up128(const U128& x, int o) {
+  return U128{__shfl_up_sync(0xffffffffu, x.lo, o), __shfl_up_sync(0xffffffffu, x.hi, o)};
+}
+
+__device__ __forceinline__ U128 block_sum128(U128 v) {
+  __shared__ U128 ws[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    add128(v, U128{__shfl_xor_sync(0xffffffffu, v.lo, o), __shfl_xor_sync(0xffffffffu, v.hi, o)});
+  }
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  U128 t{0ull, 0ull};
+  if (threadIdx.x < 32) {
+    if (threadIdx.x < (blockDim.x >> 5)) t = ws[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      add128(t, U128{__shfl_xor_sync(0xffffffffu, t.lo, o), __shfl_xor_sync(0xffffffffu, t.hi, o)});
+    }
+  }
+  return t;  // valid in thread 0
+}
+
+// p = 1/n, contrib = p/deg (PageRank.C:126-138); the accumulators start at 0.
+__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p, double* contrib, double p0) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     p[v] = p0;
-    acc[v] = 0;
     const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? p0 / d : 0ull;
+    contrib[v] = d ? p0 / (double)d : 0.0;
   }
 }
 
 // Dense push over every edge (edgeMapDenseForward with a full frontier):
-// acc[d] += contrib[s].  Each warp owns kSweepChunk consecutive edges read as
-// 16-byte vectors; chunk_v gives the chunk's first source so a lane finds its
-// source with a short search.  Hub copies (RADAR: ids < H; HUBDUP: bitmap +
-// index map) are per-CTA shared-memory u64 counters merged once per CTA.
+// acc[d] += contrib[s] with FP64 atomics, as the reference's CAS loop.  Each
+// warp owns kSweepChunk consecutive edges read as 16-byte vectors; chunk_v
+// gives the chunk's first source so a lane finds its source with a short
+// search.  Hub copies (RADAR: ids < H; HUBDUP: bitmap + index map) are
+// per-CTA shared-memory 128-bit exact sums, merged once per CTA with one FP64
+// add each.
 template <int kHub>
 __global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
-                                                               uint32_t nchunks, const uint64_t* __restrict__ contrib,
-                                                               unsigned long long* acc, HubInfo hub,
-                                                               const uint64_t* l1_prev) {
+                                                               uint32_t nchunks, const double* __restrict__ contrib,
+                                                               double* acc, HubInfo hub, const U128* l1_prev) {
   if (converged(l1_prev)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  unsigned long long* hs = reinterpret_cast<unsigned long long*>(smem_raw);
+  U128* hs = reinterpret_cast<U128*>(smem_raw);
   if (kHub != kHubNone) {
-    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = 0ull;
+    for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) hs[h] = U128{0ull, 0ull};
     __syncthreads();
   }
   const int lane = threadIdx.x & 31;
@@ -84,7 +122,7 @@ __global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const
       const uint4 d4 = __ldg(reinterpret_cast<const uint4*>(g.adj + e));
       uint32_t s = upper_index(g.off, vlo, vhi, e);
       uint32_t nxt = g.off[s + 1];
-      unsigned long long cs = contrib[s];
+      double cs = contrib[s];
       const uint32_t dd[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
       for (int i = 0; i < 4; i++) {
@@ -96,41 +134,50 @@ __global__ void __launch_bounds__(kSweepThreads) pr_push_sweep(DevGraph g, const
         }
         const uint32_t d = dd[i];
         uint32_t slot;
-        if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) atomicAdd(hs + slot, cs);
-        else atomicAdd(acc + d, cs);
+        if (kHub != kHubNone && hub_slot<kHub>(hub, d, slot)) {
+          const U128 x = fx_from_double(cs);
+          const unsigned long long old = atomicAdd(&hs[slot].lo, x.lo);
+          const unsigned long long hi = x.hi + (old + x.lo < old ? 1ull : 0ull);
+          if (hi) atomicAdd(&hs[slot].hi, hi);
+        } else {
+          atomicAdd(acc + d, cs);
+        }
       }
     }
   }
   if (kHub != kHubNone) {
     __syncthreads();
     for (uint32_t h = threadIdx.x; h < hub.H; h += blockDim.x) {
-      const unsigned long long x = hs[h];
-      if (x) atomicAdd(acc + hub_vertex<kHub>(hub, h), x);
+      const U128 x = hs[h];
+      if (x.lo | x.hi) atomicAdd(acc + hub_vertex<kHub>(hub, h), fx_to_double(x));
     }
   }
 }
 
 // Dense pull over every vertex (edgeMapDense with a full frontier, the
-// push-pull variant): acc[v] = sum of contrib[u] over in-neighbours u.
-// Edge-balanced like the push sweep: each lane takes kItems consecutive edges
-// (one 16- or 32-byte load of the edge array) and gathers their
-// contributions; it sums its row pieces in registers, lanes holding the same
-// row are combined by a segmented scan (rows are non-decreasing across
-// lanes), and each row piece is added to acc once.  The sweep is bound by the
-// gathers' L2 requests, so kMode can stream the edge array past the caches
-// (1) and also keep gathered lines in L1/L2 (2).
+// push-pull variant): acc[v] = the exact sum of contrib[u] over in-neighbours
+// u.  Edge-balanced like the push sweep: each lane takes kItems consecutive
+// edges of a warp step (one 16- or 32-byte load of the edge array) and
+// gathers their contributions.  A row that starts and ends inside one lane
+// is stored by that lane.  The first row of a lane may have started in an
+// earlier lane and its last row may continue in a later one: those pieces
+// are combined across the warp by a segmented scan (rows are non-decreasing
+// across lanes); a row that starts and ends inside the warp step is then
+// stored once, and only rows that cross a warp step's edge (at most two per
+// step) are added with 128-bit atomics into the zeroed accumulator.
+// The sweep is bound by the gathers' L2 requests, so kMode can stream the
+// edge array past the caches (1) and also keep gathered lines in L1/L2 (2).
 // kCache (degree-sorted graphs): the contributions of the H hubs (ids < H)
 // are copied into shared memory once per CTA -- RADAR's duplication of hub
 // data, used here for the reads of a pull instead of the writes of a push.
 template <bool kCache, int kItems, int kMode>
 __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
     pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v, uint32_t nchunks,
-                  const uint64_t* __restrict__ contrib, unsigned long long* acc, uint32_t H,
-                  const uint64_t* l1_prev) {
+                  const double* __restrict__ contrib, U128* acc, uint32_t H, const U128* l1_prev) {
   static_assert(kItems == 4 || kItems == 8, "4 or 8 edges per lane");
   if (converged(l1_prev)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* hc = reinterpret_cast<uint64_t*>(smem_raw);
+  double* hc = reinterpret_cast<double*>(smem_raw);
   if (kCache) {
     for (uint32_t h = threadIdx.x; h < H; h += blockDim.x) hc[h] = contrib[h];
     __syncthreads();
@@ -138,6 +185,7 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
   constexpr int kStep = 32 * kItems;  // edges per warp step
   const uint64_t first = kMode >= 1 ? policy_evict_first() : 0;
   const uint64_t keep = kMode == 2 ? policy_evict_last() : 0;
+  const uint64_t* contrib_bits = reinterpret_cast<const uint64_t*>(contrib);
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -145,9 +193,11 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
     const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
 #pragma unroll
     for (int r = 0; r < kSweepChunk / kStep; r++) {
-      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
-      uint32_t row = 0xFFFFFFFFu;
-      unsigned long long part = 0;
+      const uint32_t s0 = c * kSweepChunk + r * kStep;  // this warp step's first edge
+      const uint32_t e = s0 + lane * kItems;
+      uint32_t row = kNoRow, head_row = kNoRow;
+      U128 part{0ull, 0ull}, head{0ull, 0ull};
+      bool cont = false;      // the lane's last row continues past the lane
       if (e < g.m) {
         // in bounds: adj is padded by 8 entries and 32-byte aligned
         uint32_t uu[kItems];
@@ -168,43 +218,67 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
         }
         uint32_t v = upper_index(g.off, vlo, vhi, e);
         uint32_t nxt = g.off[v + 1];
-        unsigned long long x[kItems];
+        const bool first_started_before = g.off[v] < e;
+        double x[kItems];
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
           const uint32_t u = uu[i];
           x[i] = (e + i < g.m) ? ((kCache && u < H) ? hc[u]
-                                  : kMode == 2      ? ld_keep_u64(contrib + u, keep)
-                                                    : (unsigned long long)__ldg(contrib + u))
-                               : 0ull;
+                                  : kMode == 2      ? __longlong_as_double((long long)ld_keep_u64(contrib_bits + u, keep))
+                                                    : __ldg(contrib + u))
+                               : 0.0;
         }
         row = v;
+        bool at_first = true;
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
           const uint32_t ee = e + i;
           if (ee >= g.m) break;
           if (ee >= nxt) {
-            if (part) atomicAdd(acc + row, part);  // a row piece that ends inside this lane
-            part = 0;
+            // row `row` ends inside this lane: it is the lane's head piece if
+            // it began in an earlier lane, else complete and stored here
+            if (at_first && first_started_before) {
+              head = part;
+              head_row = row;
+            } else {
+              store128(acc + row, part);
+            }
+            at_first = false;
+            part = U128{0ull, 0ull};
             do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
             row = v;
           }
-          part += x[i];
+          add128(part, fx_from_double(x[i]));
         }
+        cont = nxt > e + kItems;
       }
+      // segmented inclusive scan of the lanes' last-row pieces
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o);
+        const U128 t = shfl_up128(part, o);
         const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
-        if (lane >= o && tr == row) part += t;
+        if (lane >= o && tr == row) add128(part, t);
       }
-      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
-      if (row != 0xFFFFFFFFu && (lane == 31 || next_row != row) && part) atomicAdd(acc + row, part);
+      const uint32_t step_end = min(s0 + (uint32_t)kStep, g.m);
+      // a head piece completes the row the previous lanes' pieces began
+      const U128 prev = shfl_up128(part, 1);
+      const uint32_t prev_row = __shfl_up_sync(0xffffffffu, row, 1);
+      if (head_row != kNoRow) {
+        if (lane > 0 && prev_row == head_row) add128(head, prev);
+        if (g.off[head_row] >= s0) store128(acc + head_row, head);  // began inside this step
+        else atomic_add128(acc + head_row, head);
+      }
+      // the last-row piece ends its segment where the row ends inside this
+      // lane, or at the end of the step
+      if (row != kNoRow && (!cont || lane == 31)) {
+        if (!cont && g.off[row] >= s0 && g.off[row + 1] <= step_end) store128(acc + row, part);
+        else atomic_add128(acc + row, part);
+      }
     }
   }
 }
 
-using PullFn = void (*)(DevGraph, const uint32_t*, uint32_t, const uint64_t*, unsigned long long*, uint32_t,
-                        const uint64_t*);
+using PullFn = void (*)(DevGraph, const uint32_t*, uint32_t, const double*, U128*, uint32_t, const U128*);
 
 // The sweeps are picked at run time among their template instances: their
 // dynamic shared memory limit is raised to the device maximum once per
@@ -246,43 +320,45 @@ PullFn pull_variant(int64_t shape) {
 }
 
 // vertexMap(PR_Vertex_F) + the L1 step + the reset, fused:
-//   p' = acc*0.85 + 0.15/n;  l1 += |p - p'|;  acc = p';  p = 0 (becomes the
-//   next accumulator);  contrib = p'/deg (next iteration's edge pass).
-__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, uint64_t* acc,
-                                                   uint64_t* p, uint64_t* contrib, uint64_t added,
-                                                   unsigned long long* l1_out, const uint64_t* l1_prev) {
+//   p' = fma(0.85, sum, 0.15/n);  L1 += |p - p'| (exact);  p = p';
+//   acc = 0 (the next iteration's accumulator);  contrib = p'/deg.
+// kExact: acc holds the pull's exact 128-bit sums; else the push's doubles.
+template <bool kExact>
+__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, U128* acc, double* p,
+                                                   double* contrib, double added, U128* l1_out,
+                                                   const U128* l1_prev) {
   if (converged(l1_prev)) return;
-  unsigned long long local = 0;
+  U128 local{0ull, 0ull};
+  double* accd = reinterpret_cast<double*>(acc);
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t pn = __umul64hi(acc[v], kDampFx64) + added;
-    const uint64_t po = p[v];
-    local += pn > po ? pn - po : po - pn;
-    acc[v] = pn;
-    p[v] = 0;
+    double sum;
+    if (kExact) {
+      sum = fx_to_double(acc[v]);
+      acc[v] = U128{0ull, 0ull};
+    } else {
+      sum = accd[v];
+      accd[v] = 0.0;
+    }
+    const double pn = fma(kDamp, sum, added);
+    add128(local, fx_from_double(fabs(p[v] - pn)));
+    p[v] = pn;
     const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? pn / d : 0ull;
+    contrib[v] = d ? pn / (double)d : 0.0;
   }
-  local = warp_sum(local);
-  __shared__ unsigned long long ws[8];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    unsigned long long t = threadIdx.x < 8 ? ws[threadIdx.x] : 0ull;
-    t = warp_sum(t);
-    if (threadIdx.x == 0) atomicAdd(l1_out, t);
-  }
+  const U128 t = block_sum128(local);
+  if (threadIdx.x == 0 && (t.lo | t.hi)) atomic_add128(l1_out, t);
 }
 
-// Ranks to double, in original-id order when the graph is degree-sorted.
-__global__ void pr_to_double(const uint64_t* __restrict__ p, const uint32_t* __restrict__ new_ids, int64_t n,
-                             double* __restrict__ out) {
+// Ranks in original-id order when the graph is degree-sorted.
+__global__ void pr_gather(const double* __restrict__ p, const uint32_t* __restrict__ new_ids, int64_t n,
+                          double* __restrict__ out) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    out[v] = __ull2double_rn(p[new_ids ? new_ids[v] : v]) * 1.0842021724855044340e-19;
+    out[v] = p[new_ids ? new_ids[v] : v];
   }
 }
 
 struct PrState {
-  DevBuf a, b, contrib, l1, out;
+  DevBuf acc, p, contrib, l1, out;
 };
 
 }  // namespace
@@ -298,22 +374,20 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   cudaStream_t st = cx->stream;
   const int64_t n = g->n;
   static thread_local PrState S;
-  RG_TRY(S.a.reserve(8 * n));
-  RG_TRY(S.b.reserve(8 * n));
+  RG_TRY(S.acc.reserve(sizeof(U128) * n));
+  RG_TRY(S.p.reserve(8 * n));
   RG_TRY(S.contrib.reserve(8 * n));
-  RG_TRY(S.l1.reserve(8 * (max_iters + 1)));
+  RG_TRY(S.l1.reserve(sizeof(U128) * (max_iters + 1)));
   RG_TRY(S.out.reserve(8 * n));
-  // the reference's constants (PageRank.C:126-138), scaled exactly
-  const double one_over_n = 1 / (double)n;
-  const double added_d = (1 - 0.85) * (1 / (double)n);
-  const uint64_t p0 = (uint64_t)(one_over_n * 9.223372036854775808e18);
-  const uint64_t added = (uint64_t)(added_d * 9.223372036854775808e18);
+  // the reference's constants (PageRank.C:126-138)
+  const double p0 = 1 / (double)n;
+  const double added = (1 - kDamp) * (1 / (double)n);
   // hub set-up (host side, before the timed span).  The full sweeps run one
   // CTA per SM, so their hub copies may use the whole shared memory.
   // hub copies only with a shared-memory budget; the push kernel's hub mode is
   // the one actually set up (a HUBDUP map kernel needs the map's arrays)
   const int hm = g_opts.hub_smem_kb > 0 ? hub_mode_of(variant) : kHubNone;
-  uint32_t pr_budget = (uint32_t)std::min<int64_t>((max_dyn_smem() - 1024) / (int)sizeof(uint64_t), n);
+  uint32_t pr_budget = (uint32_t)std::min<int64_t>((max_dyn_smem() - 1024) / (int)sizeof(U128), n);
   if (g_opts.hub_slots > 0) pr_budget = (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_slots);
   if (hub_h) pr_budget = std::min(pr_budget, hub_h);
   // pull: the push-pull variant (threshold 0, PageRank.C:122 in src/push-pull)
@@ -326,18 +400,21 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   if (!pull && hm != kHubNone) {
     if (hm == kHubPrefix) hub.H = pr_budget;
     else RG_TRY(hub_map(g, pr_budget, hub));
-    dyn = sizeof(uint64_t) * hub.H;
+    dyn = sizeof(U128) * hub.H;
   }
   // the pull's hub cache holds hub_smem_kb KiB of contributions per CTA
   const uint32_t cacheH =
-      cache ? (uint32_t)std::min<int64_t>(pr_budget, g_opts.hub_smem_kb * 1024 / (int64_t)sizeof(uint64_t)) : 0;
+      cache ? (uint32_t)std::min<int64_t>({n, g_opts.hub_smem_kb * 1024 / (int64_t)sizeof(double),
+                                           (max_dyn_smem() - 1024) / (int64_t)sizeof(double),
+                                           g_opts.hub_slots > 0 ? g_opts.hub_slots : n, hub_h ? (int64_t)hub_h : n})
+            : 0;
   const int push_hm = pull ? kHubNone : hm;
   auto sweep_fn = push_hm == kHubPrefix ? pr_push_sweep<kHubPrefix>
                   : push_hm == kHubMap  ? pr_push_sweep<kHubMap>
                                         : pr_push_sweep<kHubNone>;
   PullFn pull_fn = cache ? pull_variant<true>(g_opts.sweep_shape) : pull_variant<false>(g_opts.sweep_shape);
   const int pull_threads = cache ? 1024 : kPullThreads;
-  const size_t pull_dyn = sizeof(uint64_t) * cacheH;
+  const size_t pull_dyn = sizeof(double) * cacheH;
   const int sms = device_sms();
   int sweep_grid = 1, per_sm = 0;
   // L1 caches the gathered contributions that shared memory does not: the
@@ -364,45 +441,46 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   const int vblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16);
 
   CallTimer timer(g);
-  uint64_t* A = S.a.as<uint64_t>();
-  uint64_t* B = S.b.as<uint64_t>();
-  uint64_t* C = S.contrib.as<uint64_t>();
-  uint64_t* L1 = S.l1.as<uint64_t>();
+  U128* A = S.acc.as<U128>();
+  double* P = S.p.as<double>();
+  double* C = S.contrib.as<double>();
+  U128* L1 = S.l1.as<U128>();
   // The whole run (init + every iteration) is enqueued without host round
   // trips; it is captured once as a CUDA graph and replayed on later calls
   // with the same graph, buffers and schedule (not while per-kernel timing
   // is on, which needs the launches one by one).
   int64_t launches = 0, edge_launches = 0;
   auto enqueue = [&]() -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(L1, 0, 8 * (max_iters + 1), st);
+    cudaError_t e = cudaMemsetAsync(L1, 0, sizeof(U128) * (max_iters + 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A, 0, sizeof(U128) * n, st);
     if (e != cudaSuccess) return e;
-    pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, B, C, p0);
+    pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), P, C, p0);
     launches++;
-    // acc alternates B, A, B, ...; iteration i's kernels return at once when
-    // iteration i-1 already reached L1 < 1e-7
-    uint64_t* acc = B;
-    uint64_t* cur = A;
+    // iteration i's kernels return at once when iteration i-1 already
+    // reached L1 < 1e-7
     for (int64_t it = 0; it < max_iters; it++) {
-      const uint64_t* prev = it ? L1 + it - 1 : nullptr;
+      const U128* prev = it ? L1 + it - 1 : nullptr;
       if (g->m > 0) {
         kt_begin(st);
         if (pull) {
           pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->in_view(), g->in_chunks(),
-                                                              (uint32_t)g->nchunks, C, (unsigned long long*)acc,
-                                                              cacheH, prev);
+                                                              (uint32_t)g->nchunks, C, A, cacheH, prev);
         } else {
           sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
-                                                           (uint32_t)g->nchunks, C, (unsigned long long*)acc, hub,
-                                                           prev);
+                                                           (uint32_t)g->nchunks, C, reinterpret_cast<double*>(A),
+                                                           hub, prev);
         }
         kt_end(st);
         launches++;
         edge_launches++;
       }
-      pr_finalize<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), acc, cur, C, added,
-                                           (unsigned long long*)(L1 + it), prev);
+      if (pull) {
+        pr_finalize<true><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, P, C, added, L1 + it, prev);
+      } else {
+        pr_finalize<false><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, P, C, added, L1 + it,
+                                                    prev);
+      }
       launches++;
-      std::swap(acc, cur);
     }
     return cudaGetLastError();
   };
@@ -410,7 +488,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   // a new graph whose buffers reuse a freed graph's addresses from matching
   struct GraphKey {
     uint64_t uid;
-    const void *off, *adj, *chunk_v, *hub_bits, *hub_slot, *hub_vertex, *a, *b, *c, *l1;
+    const void *off, *adj, *chunk_v, *hub_bits, *hub_slot, *hub_vertex, *a, *p, *c, *l1;
     int64_t n, m, iters;
     int variant, grid, pull, cacheH, hubH, hubmode, shape;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof *this) == 0; }
@@ -428,7 +506,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   key.hub_slot = hub.slot;
   key.hub_vertex = hub.vertex;
   key.a = A;
-  key.b = B;
+  key.p = P;
   key.c = C;
   key.l1 = L1;
   key.n = n;
@@ -472,28 +550,33 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   g_timing.kernel_launches += launches;
   g_timing.edge_launches += edge_launches;
   RG_TRY(timer.stop());  // device work done; result copies are outside the timed span
-  std::vector<uint64_t> l1h(max_iters + 1, 0);
-  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, 8 * (max_iters + 1), cudaMemcpyDeviceToHost, st));
+  std::vector<U128> l1h(max_iters + 1, U128{0ull, 0ull});
+  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, sizeof(U128) * (max_iters + 1), cudaMemcpyDeviceToHost, st));
   RG_CUDA(cudaStreamSynchronize(st));
   int64_t done = max_iters;
   bool broke = false;
+  const U128 eps = pr_eps_fx();
   for (int64_t it = 0; it < max_iters; it++) {
-    if (l1h[it] < kEpsFx) { done = it; broke = true; break; }
+    if (less128(l1h[it], eps)) { done = it; broke = true; break; }
   }
   const int64_t last = broke ? done : max_iters - 1;
-  const uint64_t* ranks = max_iters == 0 ? A : ((last % 2 == 0) ? B : A);
   if (h_ranks) {
-    pr_to_double<<<vblocks, 256, 0, st>>>(ranks, g->sorted ? g->new_ids.as<uint32_t>() : nullptr, n,
-                                          S.out.as<double>());
-    RG_CUDA(cudaGetLastError());
-    RG_CUDA(cudaMemcpyAsync(h_ranks, S.out.p, 8 * n, cudaMemcpyDeviceToHost, st));
+    // P holds the last computed ranks (p_next after a break, p_curr after
+    // the final reset and swap of a run that used every iteration)
+    if (g->sorted) {
+      pr_gather<<<vblocks, 256, 0, st>>>(P, g->new_ids.as<uint32_t>(), n, S.out.as<double>());
+      RG_CUDA(cudaGetLastError());
+      RG_CUDA(cudaMemcpyAsync(h_ranks, S.out.p, 8 * n, cudaMemcpyDeviceToHost, st));
+    } else {
+      RG_CUDA(cudaMemcpyAsync(h_ranks, P, 8 * n, cudaMemcpyDeviceToHost, st));
+    }
     RG_CUDA(cudaStreamSynchronize(st));
   }
   const int64_t iters_run = broke ? done + 1 : max_iters;
   g_timing.edges_traversed = g->m * iters_run;
   g_timing.algorithmic_bytes = (4 * g->m + 4 * (n + 1) + 16 * n) * iters_run;
   if (iters_out) *iters_out = broke ? done + 1 : max_iters + 1;
-  if (l1_out) *l1_out = max_iters ? (double)l1h[last] * 1.0842021724855044340e-19 : 0.0;
+  if (l1_out) *l1_out = max_iters ? fx_to_double(l1h[last]) : 0.0;
   return RG_OK;
 }
 

@@ -276,41 +276,6 @@ __device__ __forceinline__ uint32_t upper_index(const T* a, uint32_t lo, uint32_
   return lo;
 }
 
-// ---- exact fixed-point accumulation on the integer pipes -----------------
-// GB300 executes few FP64 operations per clock, so per-edge double additions
-// (and double CAS loops on shared memory) bound the sweeps.  Sums of
-// non-negative doubles can instead be accumulated as integers:
-//   fx100: 128 bits (hi, lo), value * 2^100, for sums below 2^27; terms are
-//          truncated below 2^-100.
-// Conversion reads the IEEE fields with integer operations only; converting
-// a finished sum back to double rounds once.
-
-struct Fx100 {
-  uint64_t lo, hi;
-};
-__device__ __forceinline__ void fx100_add(Fx100& a, double x) {
-  const uint64_t b = (uint64_t)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) return;
-  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = e - 1075 + 100;
-  uint64_t lo, hi;
-  if (sh >= 64) { lo = 0; hi = m << (sh - 64); }
-  else if (sh > 0) { lo = m << sh; hi = m >> (64 - sh); }
-  else if (sh > -64) { lo = m >> (-sh); hi = 0; }
-  else return;
-  a.lo += lo;
-  a.hi += hi + (a.lo < lo ? 1ull : 0ull);
-}
-__device__ __forceinline__ void fx100_add(Fx100& a, const Fx100& b) {
-  a.lo += b.lo;
-  a.hi += b.hi + (a.lo < b.lo ? 1ull : 0ull);
-}
-__device__ __forceinline__ double fx100_to_double(const Fx100& a) {
-  // hi * 2^-36 + lo * 2^-100; the low word's contribution is added first
-  return fma(__ull2double_rn(a.hi), 1.4551915228366851807e-11, __ull2double_rn(a.lo) * 7.8886090522101180541e-31);
-}
-
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

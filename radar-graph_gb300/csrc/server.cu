@@ -23,9 +23,10 @@
 // Results stay in device memory (stream-ordered allocations) until the client
 // fetches them with rg_server_wait, which copies one query's array straight
 // into the client's buffer.  A batch is admitted only when its working set
-// and results fit the HBM budget taken at start-up; otherwise it waits for
-// running batches and unfetched results to release theirs (or runs alone if
-// nothing else holds memory).  Every result equals the same query run alone
+// and results fit the HBM budget taken at start-up beside what running
+// batches and unfetched results hold; otherwise it waits for running batches
+// to finish, and runs once none is running (unfetched results alone never
+// hold a batch back, whatever order the clients fetch in).  Every result equals the same query run alone
 // through the single-query entry points.
 
 #include <cuda_runtime.h>
@@ -87,6 +88,7 @@ struct Result {
   double latency_ms = 0;
   rg_status status = RG_OK;
   bool done = false;
+  bool cancelled = false;  // rg_server_cancel while it ran: its result is dropped at completion
 };
 
 }  // namespace
@@ -105,11 +107,14 @@ struct rg_server {
   std::unordered_map<uint64_t, Result> results;
   std::vector<std::thread> workers;
   bool stop = false;
+  bool paused = false;  // rg_server_pause: workers take no new queries
   uint64_t next_ticket = 1;
   // statistics since the last reset
   std::vector<double> latencies;
   double t_first = 0, t_last = 0;
   int64_t completed = 0, launches = 0, batched = 0;
+  int64_t admission_waits = 0, cancelled = 0;
+  int peak_running = 0;
 };
 
 namespace {
@@ -206,8 +211,8 @@ void worker_main(rg_server* S) {
     size_t work = 0, res = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_work.wait(lk, [&] { return S->stop || !S->pending.empty(); });
-      if (S->stop && S->pending.empty()) return;
+      S->cv_work.wait(lk, [&] { return S->stop || (!S->paused && !S->pending.empty()); });
+      if (S->stop && (S->paused || S->pending.empty())) return;
       const Query q0 = S->pending.front();
       S->pending.pop_front();
       batch.push_back(q0);
@@ -228,10 +233,19 @@ void worker_main(rg_server* S) {
       work = working_bytes(g, q0.kind, k);
       res = result_bytes(g, q0.kind, k);
       // admission by free HBM: wait while running batches and unfetched
-      // results hold the budget
-      S->cv_mem.wait(lk, [&] { return S->hbm_in_use == 0 || S->hbm_in_use + work + res <= S->hbm_budget; });
+      // results hold the budget -- but never for unfetched results alone: a
+      // client may fetch in any order, and one waiting for this batch while
+      // holding the results of an earlier one would otherwise wait forever.
+      // With nothing running the batch is admitted (then only the client's
+      // unfetched results exceed the budget).
+      auto fits = [&] { return S->running == 0 || S->hbm_in_use + work + res <= S->hbm_budget; };
+      if (!fits()) {
+        S->admission_waits++;
+        S->cv_mem.wait(lk, [&] { return S->stop || fits(); });
+      }
       S->hbm_in_use += work + res;
       S->running++;
+      S->peak_running = std::max(S->peak_running, S->running);
     }
     rg_graph* g = S->graphs[batch[0].graph];
     const int64_t n = g->n;
@@ -304,14 +318,15 @@ void worker_main(rg_server* S) {
       }
       if (multi) S->batched += (int64_t)batch.size();
       const size_t row = kind == RG_QUERY_BC ? 8 * n : 4 * n;
-      block->refs = status == RG_OK ? (int)batch.size() : 0;
+      block->refs = 0;
       for (size_t i = 0; i < batch.size(); i++) {
         Result& r = S->results[batch[i].ticket];
-        r.status = status;
-        if (status == RG_OK) {
+        r.status = r.cancelled ? RG_ECANCELED : status;
+        if (status == RG_OK && !r.cancelled) {
           r.block = block;
           r.offset = i * row;
           r.bytes = row;
+          block->refs++;
         }
         r.latency_ms = t_done - batch[i].t_submit;
         r.done = true;
@@ -320,9 +335,25 @@ void worker_main(rg_server* S) {
         if (S->t_first == 0 || batch[i].t_submit < S->t_first) S->t_first = batch[i].t_submit;
       }
       S->t_last = std::max(S->t_last, t_done);
+      if (block->refs == 0) S->hbm_in_use -= status == RG_OK ? res : 0;  // every query of the batch was cancelled
     }
-    if (status != RG_OK && block->p) cudaFreeAsync(block->p, st);
+    if (block->refs == 0 && block->p) cudaFreeAsync(block->p, st);
     S->cv_done.notify_all();
+    S->cv_mem.notify_all();
+  }
+}
+
+// One fetched (or dropped) result of a batch: the batch's block is freed and
+// its bytes returned to the admission budget when its last result goes.
+void release_result(rg_server* S, const std::shared_ptr<Block>& block, cudaStream_t st) {
+  bool last = false;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    last = --block->refs == 0;
+    if (last) S->hbm_in_use -= block->bytes;
+  }
+  if (last) {
+    cudaFreeAsync(block->p, st);
     S->cv_mem.notify_all();
   }
 }
@@ -387,18 +418,26 @@ rg_status rg_server_submit(rg_server* S, int graph, rg_query_kind kind, uint32_t
   return RG_OK;
 }
 
-rg_status rg_server_wait(rg_server* S, uint64_t ticket, void* h_result, size_t bytes, double* latency_ms) {
+rg_status rg_server_wait_for(rg_server* S, uint64_t ticket, void* h_result, size_t bytes, double* latency_ms,
+                             double timeout_ms) {
   if (!S) return fail(RG_EINVAL, "null server");
   Ctx* cx = nullptr;
   RG_TRY(get_ctx(&cx));
   std::unique_lock<std::mutex> lk(S->mu);
   auto it = S->results.find(ticket);
   if (it == S->results.end()) return fail(RG_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
-  S->cv_done.wait(lk, [&] { return S->results[ticket].done; });
+  auto ready = [&] { return S->results[ticket].done; };
+  if (timeout_ms < 0) {
+    S->cv_done.wait(lk, ready);
+  } else if (!S->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+    // the ticket stays valid: wait again later, or cancel it
+    return fail(RG_ETIMEOUT, "ticket %llu not done after %.3f ms", (unsigned long long)ticket, timeout_ms);
+  }
   Result r = std::move(S->results[ticket]);
   S->results.erase(ticket);
   lk.unlock();
   rg_status st = r.status;
+  if (st == RG_ECANCELED) return fail(RG_ECANCELED, "ticket %llu was cancelled", (unsigned long long)ticket);
   if (st == RG_OK && h_result && bytes < r.bytes) {
     st = fail(RG_EINVAL, "result buffer too small: need %zu bytes", r.bytes);
   }
@@ -410,20 +449,55 @@ rg_status rg_server_wait(rg_server* S, uint64_t ticket, void* h_result, size_t b
       st = cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "server result copy", __FILE__, __LINE__);
     }
   }
-  if (r.block) {  // the last fetch of a batch frees its block
-    bool last = false;
-    {
-      std::lock_guard<std::mutex> lk2(S->mu);
-      last = --r.block->refs == 0;
-      if (last) S->hbm_in_use -= r.block->bytes;
-    }
-    if (last) {
-      cudaFreeAsync(r.block->p, cx->stream);
-      S->cv_mem.notify_all();
-    }
-  }
+  if (r.block) release_result(S, r.block, cx->stream);
   if (st == RG_OK && latency_ms) *latency_ms = r.latency_ms;
   return st;
+}
+
+rg_status rg_server_wait(rg_server* S, uint64_t ticket, void* h_result, size_t bytes, double* latency_ms) {
+  return rg_server_wait_for(S, ticket, h_result, bytes, latency_ms, -1.0);
+}
+
+rg_status rg_server_cancel(rg_server* S, uint64_t ticket) {
+  if (!S) return fail(RG_EINVAL, "null server");
+  std::shared_ptr<Block> drop;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->results.find(ticket);
+    if (it == S->results.end()) return fail(RG_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
+    Result& r = it->second;
+    if (r.cancelled || r.status == RG_ECANCELED) return RG_OK;
+    auto q = std::find_if(S->pending.begin(), S->pending.end(), [&](const Query& x) { return x.ticket == ticket; });
+    if (q != S->pending.end()) {  // not started: it never runs
+      S->pending.erase(q);
+      r.status = RG_ECANCELED;
+      r.done = true;
+    } else if (!r.done) {  // running: the worker drops its result
+      r.cancelled = true;
+    } else {  // finished and not fetched: release the result now
+      drop = std::move(r.block);
+      r.block.reset();
+      if (r.status == RG_OK) r.status = RG_ECANCELED;
+    }
+    S->cancelled++;
+  }
+  if (drop) {
+    Ctx* cx = nullptr;
+    RG_TRY(get_ctx(&cx));
+    release_result(S, drop, cx->stream);
+  }
+  S->cv_done.notify_all();
+  return RG_OK;
+}
+
+rg_status rg_server_pause(rg_server* S, int paused) {
+  if (!S) return fail(RG_EINVAL, "null server");
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->paused = paused != 0;
+  }
+  S->cv_work.notify_all();
+  return RG_OK;
 }
 
 rg_status rg_server_get_stats(rg_server* S, rg_server_stats* out) {
@@ -433,6 +507,9 @@ rg_status rg_server_get_stats(rg_server* S, rg_server_stats* out) {
   out->completed = S->completed;
   out->launches = S->launches;
   out->batched = S->batched;
+  out->admission_waits = S->admission_waits;
+  out->cancelled = S->cancelled;
+  out->peak_running = S->peak_running;
   if (!S->latencies.empty()) {
     std::vector<double> l(S->latencies);
     std::sort(l.begin(), l.end());
@@ -449,7 +526,8 @@ rg_status rg_server_reset_stats(rg_server* S) {
   if (!S) return fail(RG_EINVAL, "null server");
   std::lock_guard<std::mutex> lk(S->mu);
   S->latencies.clear();
-  S->completed = S->launches = S->batched = 0;
+  S->completed = S->launches = S->batched = S->admission_waits = S->cancelled = 0;
+  S->peak_running = S->running;
   S->t_first = S->t_last = 0;
   return RG_OK;
 }
@@ -461,6 +539,7 @@ rg_status rg_server_free(rg_server* S) {
     S->stop = true;
   }
   S->cv_work.notify_all();
+  S->cv_mem.notify_all();
   for (auto& t : S->workers) t.join();
   // results never fetched: release their blocks
   for (auto& kv : S->results) {

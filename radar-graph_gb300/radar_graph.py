@@ -28,7 +28,7 @@ NO_OUTPUT = 1
 DENSE_FORWARD = 8
 
 STATUS = {0: "RG_OK", 1: "RG_EINVAL", 2: "RG_ENOMEM", 3: "RG_ECUDA", 4: "RG_EIO",
-          5: "RG_EFORMAT", 6: "RG_EUNSUPPORTED", 7: "RG_ETIMEOUT", 8: "RG_ENODEV"}
+          5: "RG_EFORMAT", 6: "RG_EUNSUPPORTED", 7: "RG_ETIMEOUT", 8: "RG_ENODEV", 9: "RG_ECANCELED"}
 
 
 class RgError(RuntimeError):
@@ -41,6 +41,11 @@ class Timing(C.Structure):
     _fields_ = [("total_ms", C.c_double), ("edge_ms", C.c_double), ("edges_traversed", C.c_int64),
                 ("algorithmic_bytes", C.c_int64), ("edge_launches", C.c_int64),
                 ("kernel_launches", C.c_int64)]
+
+
+class LevelTrace(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("hub_mode", C.c_int32), ("frontier", C.c_int64), ("degsum", C.c_int64),
+                ("threshold", C.c_int64)]
 
 
 class OpArgs(C.Structure):
@@ -97,6 +102,9 @@ _SIGS = {
     "rg_synchronize": [],
     "rg_last_timing": [_P(Timing)],
     "rg_set_kernel_timing": [C.c_int],
+    "rg_set_trace": [C.c_int],
+    "rg_trace_take": [_P(LevelTrace), C.c_int64, _i64p],
+    "rg_device_info": [C.c_char_p, C.c_int, _i32p, _f64p],
     "rg_bfs_depth_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_uint32, C.c_void_p, C.c_void_p,
                              _i64p],
     "rg_set_option": [C.c_int, C.c_int64],
@@ -110,6 +118,9 @@ _SIGS = {
     "rg_server_create": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p],
     "rg_server_submit": [C.c_void_p, C.c_int, C.c_int, C.c_uint32, _P(C.c_uint64)],
     "rg_server_wait": [C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t, _f64p],
+    "rg_server_wait_for": [C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t, _f64p, C.c_double],
+    "rg_server_cancel": [C.c_void_p, C.c_uint64],
+    "rg_server_pause": [C.c_void_p, C.c_int],
     "rg_server_get_stats": [C.c_void_p, C.c_void_p],
     "rg_server_reset_stats": [C.c_void_p],
     "rg_server_free": [C.c_void_p],
@@ -166,7 +177,8 @@ QUERY_KINDS = {"bfs": 0, "bc": 1, "radii": 2}
 
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("launches", C.c_int64), ("batched", C.c_int64),
-                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("qps", C.c_double)]
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("qps", C.c_double),
+                ("admission_waits", C.c_int64), ("cancelled", C.c_int64), ("peak_running", C.c_int32)]
 
 OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3, "sweep_shape": 4, "bc_fwd_hubs": 5}
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
@@ -222,6 +234,31 @@ def get_option(name):
     v = C.c_int64()
     _check(lib().rg_get_option(OPTIONS[name], C.byref(v)))
     return v.value
+
+
+TRACE_MODES = {0: "sparse-push", 1: "dense-push", 2: "pull"}
+
+
+def set_trace(on):
+    """Record one entry per edgeMap of this thread (rg_set_trace)."""
+    _check(lib().rg_set_trace(1 if on else 0))
+
+
+def take_trace(cap=4096):
+    """The recorded edgeMaps, oldest first, as dicts; clears the record."""
+    buf = (LevelTrace * cap)()
+    k = C.c_int64()
+    _check(lib().rg_trace_take(buf, cap, C.byref(k)))
+    return [{"mode": TRACE_MODES[buf[i].mode], "hub_mode": buf[i].hub_mode, "frontier": buf[i].frontier,
+             "degsum": buf[i].degsum, "threshold": buf[i].threshold} for i in range(k.value)]
+
+
+def device_info():
+    """(name, SM count, nominal HBM GB/s) of the current device."""
+    name = C.create_string_buffer(256)
+    sms, gbs = C.c_int32(), C.c_double()
+    _check(lib().rg_device_info(name, 256, C.byref(sms), C.byref(gbs)))
+    return name.value.decode(), sms.value, gbs.value
 
 
 def set_kernel_timing(on):
@@ -570,6 +607,14 @@ def _graph_set_tuning(self, tuning):
 Graph.set_tuning = _graph_set_tuning
 
 
+def _graph_clear_tuning(self):
+    """Forgets the autotuner's choices: later calls use the thread's options."""
+    _check(lib().rg_graph_clear_tuning(self._h))
+
+
+Graph.clear_tuning = _graph_clear_tuning
+
+
 class Batch:
     """Many graphs resident on the device, run by one persistent launch."""
 
@@ -631,14 +676,24 @@ class Server:
         _check(lib().rg_server_submit(self._h, graph, QUERY_KINDS[kind], int(source), C.byref(t)))
         return t.value
 
-    def wait(self, ticket, graph, kind, out=None):
-        """Result of `ticket` (into `out` if given, e.g. a pinned_empty array)."""
+    def wait(self, ticket, graph, kind, out=None, timeout_ms=None):
+        """Result of `ticket` (into `out` if given, e.g. a pinned_empty array).
+        With timeout_ms, raises RgError RG_ETIMEOUT if it is not done in time
+        (the ticket stays valid); a cancelled ticket raises RG_ECANCELED."""
         n = self.graphs[graph].n
         if out is None:
             out = np.empty(n, np.float64 if kind == "bc" else np.int32)
         lat = C.c_double()
-        _check(lib().rg_server_wait(self._h, ticket, out.ctypes.data, out.nbytes, C.byref(lat)))
+        _check(lib().rg_server_wait_for(self._h, ticket, out.ctypes.data, out.nbytes, C.byref(lat),
+                                        -1.0 if timeout_ms is None else float(timeout_ms)))
         return out, lat.value
+
+    def cancel(self, ticket):
+        _check(lib().rg_server_cancel(self._h, ticket))
+
+    def pause(self, paused=True):
+        """Workers take no new queries while paused (running batches finish)."""
+        _check(lib().rg_server_pause(self._h, 1 if paused else 0))
 
     def stats(self):
         s = ServerStats()

@@ -109,3 +109,22 @@ def test_cli_pagerank_delta(golden, tmp_path, variant):
     r = _run("PageRankDelta", "-s", "-rounds", "0", "-maxiters", "20", "-variant", variant, "-out", out, path)
     assert r.returncode == 0, r.stderr
     assert_close(np.loadtxt(out), g[f"prd_{variant}"], what="PageRankDelta via CLI")
+
+
+@pytest.mark.gpu
+def test_cli_prints_a_json_result_line(golden, tmp_path):
+    """Every run ends with one JSON result line: app, variant, graph, size,
+    time, GTEPS and the fraction of the HBM roofline (here against a given
+    peak), and the GPU's name."""
+    import json
+    path = _write_raw(golden, "rmat12", tmp_path)
+    r = _run("BFS", "-s", "-rounds", "0", "-r", 1, "-hbm-gbs", "6791.4", path)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    j = lines[0]
+    assert j["app"] == "BFS" and j["variant"] == "radar" and j["graph"] == str(path)
+    assert j["n"] == 4096 and j["m"] == len(golden["rmat12"]["adj"]) and j["degree_sorted"] is True
+    assert j["gteps"] > 0 and j["edges"] > 0 and j["peak_kind"] == "given" and j["hbm_peak_gbs"] == 6791.4
+    assert j["hbm_frac"] == pytest.approx(j["achieved_gbs"] / 6791.4, rel=1e-3)
+    assert j["gpu"]

@@ -1,7 +1,7 @@
 """Batched execution on the GPU: 64-source bitmask BFS on one resident graph
 and the persistent many-graph launch.  Every batched result must equal the
 corresponding single-query result (and the oracle): BFS depths bit-exact,
-PageRank ranks identical to rg_pagerank (same integer arithmetic) and within
+PageRank ranks identical to rg_pagerank (same exact-sum arithmetic) and within
 1e-9 relative of the oracle."""
 
 import numpy as np
@@ -88,5 +88,5 @@ def test_batch_persistent_matches_single_queries():
         if len(adj):
             with rg.Graph.from_csr(off, adj) as G:
                 r1, it1, _ = G.pagerank("push-pull", 10)
-                assert np.array_equal(ranks[i], r1)  # same integer arithmetic, bit for bit
+                assert np.array_equal(ranks[i], r1)  # same exact sums, bit for bit
     B.free()

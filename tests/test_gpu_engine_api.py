@@ -189,3 +189,24 @@ def test_radii_loop_through_edgemap(golden, name, mode):
             for d in (d_vis, d_next, d_radii):
                 d.free()
             fr.free()
+
+
+def test_level_trace_records_every_edgemap(golden):
+    """rg_set_trace: one record per edgeMap, as Ligra's frontierStats prints
+    PUSH/PULL and the frontier size per iteration -- BFS on rmat12 goes sparse,
+    dense, then sparse again, and every dense level passes the m/20 test."""
+    g = golden["rmat12"]
+    with rg.Graph.from_csr(g["off"], g["adj"]) as G:
+        rg.set_trace(True)
+        try:
+            _, _, rounds, _ = G.bfs("push-pull", int(g["bfs_roots"][0]))
+            tr = rg.take_trace()
+        finally:
+            rg.set_trace(False)
+        assert len(tr) == rounds or len(tr) == rounds - 1
+        assert {t["mode"] for t in tr} >= {"sparse-push", "pull"}
+        for t in tr:
+            dense = t["frontier"] + t["degsum"] > t["threshold"]
+            assert (t["mode"] != "sparse-push") == dense
+            assert t["threshold"] == G.m // 20
+        assert rg.take_trace() == []  # taken and cleared

@@ -4,8 +4,9 @@ Each calling thread has its own stream and scratch (the library's
 per-thread context), so PageRank, PageRankDelta, BFS, BC and Radii calls --
 single-query and batched -- made from four threads at the same time on one
 graph handle return what the same calls return one at a time: BFS depths,
-Radii and fixed-point PageRank ranks bit-exact, BC and PageRankDelta within
-1e-9 relative (their double reductions run in a different order).
+Radii and pulled PageRank ranks (exact sums) bit-exact; pushed PageRank, BC
+and PageRankDelta within 1e-9 relative (their FP64 atomics add in a
+different order).
 """
 
 import threading
@@ -29,6 +30,7 @@ def _jobs(g, off):
     jobs = []
     for v in ("radar", "push"):
         jobs.append(("pagerank", v, lambda v=v: g.pagerank(v, 20)[0]))
+    jobs.append(("pagerank_pull", "push-pull", lambda: g.pagerank("push-pull", 20)[0]))
     jobs.append(("pagerank_delta", "radar", lambda: g.pagerank_delta("radar", 30)[0]))
     for r in roots:
         jobs.append(("bfs", int(r), lambda r=r: g.bfs("radar", int(r), parents=False)[1]))
@@ -42,7 +44,7 @@ def _jobs(g, off):
 
 
 def _same(kind, got, want, what):
-    if kind in ("bc", "bc_multi", "pagerank_delta"):
+    if kind in ("bc", "bc_multi", "pagerank_delta", "pagerank"):
         assert_close(got, want, what=what)
     else:
         assert np.array_equal(got, want), what

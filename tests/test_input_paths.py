@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import radar_graph as rg
+from conftest import assert_close
 
 
 def _write_sg(path, off, adj, directed=False, bad_size=False, inverse=None):
@@ -96,10 +97,16 @@ def test_device_build_equals_host_cleanup(case):
         assert np.array_equal(o2, off)
         assert np.array_equal(a2, adj)
         if len(adj):  # and the apps run on it like on an uploaded graph
-            r, it, _ = g.pagerank("push", 5)
             with rg.Graph.from_csr(off, adj) as g2:
+                # pulls sum exactly: identical; pushes add with FP64 atomics in
+                # any order, as the reference does: within rounding
+                r, it, _ = g.pagerank("push-pull", 5)
+                r2, it2, _ = g2.pagerank("push-pull", 5)
+                assert it == it2 and np.array_equal(r, r2)
+                r, it, _ = g.pagerank("push", 5)
                 r2, it2, _ = g2.pagerank("push", 5)
-            assert it == it2 and np.array_equal(r, r2)
+                assert it == it2
+                assert_close(r, r2, what="push PageRank on the device-built graph")
 
 
 @pytest.mark.gpu
@@ -133,7 +140,11 @@ def test_directed_device_build_equals_cleanup(case):
                 for v in ("push", "push-pull"):
                     r, it, _ = g.pagerank(v, 5)
                     r2, it2, _ = g2.pagerank(v, 5)
-                    assert it == it2 and np.array_equal(r, r2)
+                    assert it == it2
+                    if v == "push-pull":  # exact sums
+                        assert np.array_equal(r, r2)
+                    else:  # FP64 atomics in any order
+                        assert_close(r, r2, what="directed push PageRank")
 
 
 @pytest.mark.gpu
@@ -155,9 +166,12 @@ def test_create_sorted_equals_upload_then_sort(case, pinned):
         wo, wa, wi = want.download()
         go, ga, gi = got.download()
         assert np.array_equal(wo, go) and np.array_equal(wa, ga) and np.array_equal(wi, gi)
+        r1, _, _ = want.pagerank("push-pull", 10)
+        r2, _, _ = got.pagerank("push-pull", 10)
+        assert np.array_equal(r1, r2)  # exact sums: identical
         r1, _, _ = want.pagerank("radar", 10)
         r2, _, _ = got.pagerank("radar", 10)
-        assert np.array_equal(r1, r2)
+        assert_close(r1, r2, what="RADAR PageRank on the fused create+sort graph")
 
 
 @pytest.mark.gpu
