@@ -813,6 +813,7 @@ def main():
             print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
                               "config": bench_config(args.scale, n, m), "gpu_launches": int(launches),
+                              "apps_ms": {k: round(v["ms"] / args.steps, 3) for k, v in stats.items()},
                               "note": "--step-only: the timed step alone, for profiler captures"}), flush=True)
         gs.free()
         return 0

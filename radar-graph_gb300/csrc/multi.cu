@@ -201,7 +201,7 @@ struct BatchDesc {
   int32_t* depth;           // per graph: k rows of n_g depths at 64 * vbase[g]
   double* p;                // PageRank ranks
   double* acc;              // the iteration's new ranks
-  double* contrib;          // p / deg
+  U128* contrib;            // p / deg, exact 128-bit fixed point
   double* ranks;            // results
   int32_t* pr_iters;        // per graph: iterations run (PageRank.C's iter)
   const int32_t* task;      // task list: graph * 2 + kind (0 BFS, 1 PageRank), largest first
@@ -297,6 +297,21 @@ __device__ void batch_msbfs(const BatchDesc& D, int gi) {
 // vertex's sum formed exactly (128-bit fixed point) and rounded once,
 // p' = fma(0.85, sum, 0.15/n), exact L1.  Sums do not depend on the order of
 // the additions, so the ranks equal rg_pagerank's bit for bit.
+// p'/deg by degree class, as pagerank.cu's pr_quotient: no out-edges, a
+// power of two (exact exponent shift) or the IEEE division.  Every branch
+// gives the correctly rounded quotient.
+__device__ __forceinline__ double batch_quotient(double pn, uint32_t d) {
+  if (d == 0) return 0.0;
+  if ((d & (d - 1)) == 0) return double_of(bits_of(pn) - ((unsigned long long)(31 - __clz(d)) << 52));
+  return pn / (double)d;
+}
+
+// One graph's PageRank inside the persistent kernel, with the arithmetic of
+// pagerank.cu's pull (pr_exact.cuh): FP64 contributions p/deg, kept as their
+// exact 128-bit fixed-point values, each vertex's sum formed exactly and
+// rounded once, p' = fma(0.85, sum, 0.15/n), exact L1.  Sums do not depend on
+// the order of the additions, so the ranks equal rg_pagerank's bit for bit.
+// Rows are pulled by groups of 8 lanes (the batched graphs' rows are short).
 __device__ void batch_pagerank(const BatchDesc& D, int gi) {
   const uint64_t vb = D.vbase[gi];
   const uint32_t n = D.nv[gi];
@@ -304,8 +319,11 @@ __device__ void batch_pagerank(const BatchDesc& D, int gi) {
   const uint32_t* adj = D.adj + D.ebase[gi];
   double* p = D.p + vb;
   double* acc = D.acc + vb;
-  double* contrib = D.contrib + vb;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kBatchThreads / 32;
+  U128* contrib = D.contrib + vb;
+  constexpr int kG = 8;  // lanes per row
+  const int lane = threadIdx.x & 31, gl = lane & (kG - 1);
+  const unsigned gmask = 0xFFu << (lane & ~(kG - 1));
+  const uint32_t group = threadIdx.x / kG, ngroups = kBatchThreads / kG;
   // the reference's constants (PageRank.C:126-138)
   const double p0 = 1 / (double)n;
   const double added = (1 - kDamp) * (1 / (double)n);
@@ -313,8 +331,7 @@ __device__ void batch_pagerank(const BatchDesc& D, int gi) {
   __shared__ U128 s_l1;
   for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) {
     p[v] = p0;
-    const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? p0 / (double)d : 0.0;
+    contrib[v] = fx_from_double(batch_quotient(p0, off[v + 1] - off[v]));
   }
   __syncthreads();
   int64_t it = 0;
@@ -324,16 +341,17 @@ __device__ void batch_pagerank(const BatchDesc& D, int gi) {
     if (threadIdx.x == 0) s_l1 = U128{0ull, 0ull};
     __syncthreads();
     U128 l1{0ull, 0ull};
-    for (uint32_t v = warp; v < n; v += nw) {  // pull: a warp per row
+    for (uint32_t v = group; v < n; v += ngroups) {  // pull: a group of lanes per row
       U128 s{0ull, 0ull};
-      for (uint32_t j = off[v] + lane; j < off[v + 1]; j += 32) add128(s, fx_from_double(contrib[adj[j]]));
+      for (uint32_t j = off[v] + gl; j < off[v + 1]; j += kG) add128(s, contrib[adj[j]]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        add128(s, U128{__shfl_xor_sync(0xffffffffu, s.lo, o), __shfl_xor_sync(0xffffffffu, s.hi, o)});
+      for (int o = kG / 2; o > 0; o >>= 1) {
+        add128(s, U128{__shfl_xor_sync(gmask, s.lo, o), __shfl_xor_sync(gmask, s.hi, o)});
       }
-      if (lane == 0) {
-        const double pn = fma(kDamp, fx_to_double(s), added);
-        add128(l1, fx_from_double(fabs(p[v] - pn)));
+      if (gl == 0) {
+        const double pn = (s.lo | s.hi) ? fma(kDamp, fx_to_double(s), added) : added;
+        const double po = p[v];
+        if (po != pn) add128(l1, fx_from_double(fabs(po - pn)));
         acc[v] = pn;
       }
     }
@@ -350,8 +368,7 @@ __device__ void batch_pagerank(const BatchDesc& D, int gi) {
     for (uint32_t v = threadIdx.x; v < n; v += kBatchThreads) {
       const double pn = acc[v];
       p[v] = pn;
-      const uint32_t d = off[v + 1] - off[v];
-      contrib[v] = d ? pn / (double)d : 0.0;
+      contrib[v] = fx_from_double(batch_quotient(pn, off[v + 1] - off[v]));
     }
     __syncthreads();
     const bool conv = less128(s_l1, eps);
@@ -433,7 +450,7 @@ extern "C" rg_status rg_batch_create(int ngraphs, const int64_t* ns, const int64
       (s = b->d_F.reserve(8 * V)) != RG_OK || (s = b->d_N.reserve(8 * V)) != RG_OK ||
       (s = b->d_seen.reserve(8 * V)) != RG_OK || (s = b->d_depth.reserve(4 * 64 * V)) != RG_OK ||
       (s = b->d_p.reserve(8 * V)) != RG_OK || (s = b->d_acc.reserve(8 * V)) != RG_OK ||
-      (s = b->d_contrib.reserve(8 * V)) != RG_OK || (s = b->d_ranks.reserve(8 * V)) != RG_OK ||
+      (s = b->d_contrib.reserve(16 * V)) != RG_OK || (s = b->d_ranks.reserve(8 * V)) != RG_OK ||
       (s = b->d_iters.reserve(4 * ngraphs)) != RG_OK || (s = b->d_task.reserve(4 * 2 * ngraphs)) != RG_OK ||
       (s = b->d_counter.reserve(64)) != RG_OK) {
     delete b;
@@ -503,7 +520,7 @@ extern "C" rg_status rg_batch_run(rg_batch* b, const uint32_t* h_sources, int k,
   D.depth = b->d_depth.as<int32_t>();
   D.p = b->d_p.as<double>();
   D.acc = b->d_acc.as<double>();
-  D.contrib = b->d_contrib.as<double>();
+  D.contrib = b->d_contrib.as<U128>();
   D.ranks = b->d_ranks.as<double>();
   D.pr_iters = b->d_iters.as<int32_t>();
   D.task = b->d_task.as<int32_t>();

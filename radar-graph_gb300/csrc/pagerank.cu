@@ -83,12 +83,26 @@ __device__ __forceinline__ U128 block_sum128(U128 v) {
   return t;  // valid in thread 0
 }
 
-// p = 1/n, contrib = p/deg (PageRank.C:126-138); the accumulators start at 0.
-__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p, double* contrib, double p0) {
+// p'/deg, the IEEE quotient of PR_F (PageRank.C:48), by degree class: 0 for
+// no out-edges, an exact exponent shift for a power-of-two degree (the
+// quotient is exact; p' >= 0.15/n keeps it normal), else div_by_recip.
+// Degree-sorted graphs keep whole warps in one class, so the FP64 work runs
+// only in the warps of other degrees.
+__device__ __forceinline__ double pr_quotient(double pn, uint32_t d, const double* __restrict__ rdeg, int64_t v) {
+  if (d == 0) return 0.0;
+  if ((d & (d - 1)) == 0) return double_of(bits_of(pn) - ((unsigned long long)(31 - __clz(d)) << 52));
+  return div_by_recip(pn, (double)d, rdeg[v]);
+}
+
+// p = 1/n, contrib = p/deg (PageRank.C:126-138), rdeg = RN(1/deg) for the
+// later iterations' quotients; the accumulators start at 0.
+__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p, double* contrib, double* rdeg,
+                        double p0) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     p[v] = p0;
     const uint32_t d = off[v + 1] - off[v];
     contrib[v] = d ? p0 / (double)d : 0.0;
+    rdeg[v] = d ? 1.0 / (double)d : 0.0;
   }
 }
 
@@ -321,29 +335,36 @@ PullFn pull_variant(int64_t shape) {
 
 // vertexMap(PR_Vertex_F) + the L1 step + the reset, fused:
 //   p' = fma(0.85, sum, 0.15/n);  L1 += |p - p'| (exact);  p = p';
-//   acc = 0 (the next iteration's accumulator);  contrib = p'/deg.
-// kExact: acc holds the pull's exact 128-bit sums; else the push's doubles.
+//   acc = 0 where the next sweep adds instead of storing;  contrib = p'/deg.
+// kExact: acc holds the pull's exact 128-bit sums; the pull stores every
+// row that lies inside one warp step of `step` edges (pull_off: the rows it
+// reads) and adds with atomics only into rows that cross a step, so only
+// those are zeroed.  Else acc holds the push's FP64 sums, all zeroed.
 template <bool kExact>
-__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off, U128* acc, double* p,
-                                                   double* contrib, double added, U128* l1_out,
-                                                   const U128* l1_prev) {
+__global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ pull_off, uint32_t step, U128* acc,
+                                                   double* p, double* contrib, const double* __restrict__ rdeg,
+                                                   double added, U128* l1_out, const U128* l1_prev) {
   if (converged(l1_prev)) return;
   U128 local{0ull, 0ull};
   double* accd = reinterpret_cast<double*>(acc);
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     double sum;
     if (kExact) {
-      sum = fx_to_double(acc[v]);
-      acc[v] = U128{0ull, 0ull};
+      const U128 a = acc[v];
+      sum = (a.lo | a.hi) ? fx_to_double(a) : 0.0;
+      const uint32_t b = pull_off[v], e = pull_off[v + 1];
+      if (e > b && b / step != (e - 1) / step) acc[v] = U128{0ull, 0ull};
     } else {
       sum = accd[v];
       accd[v] = 0.0;
     }
-    const double pn = fma(kDamp, sum, added);
-    add128(local, fx_from_double(fabs(p[v] - pn)));
+    // fma(0.85, 0, added) is `added` exactly: vertices without in-edges skip it
+    const double pn = sum != 0.0 ? fma(kDamp, sum, added) : added;
+    const double po = p[v];
+    if (po != pn) add128(local, fx_from_double(fabs(po - pn)));
     p[v] = pn;
-    const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? pn / (double)d : 0.0;
+    contrib[v] = pr_quotient(pn, off[v + 1] - off[v], rdeg, v);  // = pn / deg, correctly rounded
   }
   const U128 t = block_sum128(local);
   if (threadIdx.x == 0 && (t.lo | t.hi)) atomic_add128(l1_out, t);
@@ -358,7 +379,7 @@ __global__ void pr_gather(const double* __restrict__ p, const uint32_t* __restri
 }
 
 struct PrState {
-  DevBuf acc, p, contrib, l1, out;
+  DevBuf acc, p, contrib, rdeg, l1, out;
 };
 
 }  // namespace
@@ -377,6 +398,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   RG_TRY(S.acc.reserve(sizeof(U128) * n));
   RG_TRY(S.p.reserve(8 * n));
   RG_TRY(S.contrib.reserve(8 * n));
+  RG_TRY(S.rdeg.reserve(8 * n));
   RG_TRY(S.l1.reserve(sizeof(U128) * (max_iters + 1)));
   RG_TRY(S.out.reserve(8 * n));
   // the reference's constants (PageRank.C:126-138)
@@ -413,6 +435,8 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
                   : push_hm == kHubMap  ? pr_push_sweep<kHubMap>
                                         : pr_push_sweep<kHubNone>;
   PullFn pull_fn = cache ? pull_variant<true>(g_opts.sweep_shape) : pull_variant<false>(g_opts.sweep_shape);
+  // edges per warp step of the chosen pull (32 lanes x 4 or 8 edges, pull_variant's shapes)
+  const uint32_t pull_step = (g_opts.sweep_shape / 10 == 8) ? 256u : 128u;
   const int pull_threads = cache ? 1024 : kPullThreads;
   const size_t pull_dyn = sizeof(double) * cacheH;
   const int sms = device_sms();
@@ -444,6 +468,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   U128* A = S.acc.as<U128>();
   double* P = S.p.as<double>();
   double* C = S.contrib.as<double>();
+  double* R = S.rdeg.as<double>();
   U128* L1 = S.l1.as<U128>();
   // The whole run (init + every iteration) is enqueued without host round
   // trips; it is captured once as a CUDA graph and replayed on later calls
@@ -454,7 +479,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     cudaError_t e = cudaMemsetAsync(L1, 0, sizeof(U128) * (max_iters + 1), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(A, 0, sizeof(U128) * n, st);
     if (e != cudaSuccess) return e;
-    pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), P, C, p0);
+    pr_init<<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), P, C, R, p0);
     launches++;
     // iteration i's kernels return at once when iteration i-1 already
     // reached L1 < 1e-7
@@ -463,22 +488,23 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
       if (g->m > 0) {
         kt_begin(st);
         if (pull) {
-          pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->in_view(), g->in_chunks(),
-                                                              (uint32_t)g->nchunks, C, A, cacheH, prev);
+          pull_fn<<<sweep_grid, pull_threads, pull_dyn, st>>>(g->in_view(), g->in_chunks(), (uint32_t)g->nchunks, C,
+                                                              A, cacheH, prev);
         } else {
           sweep_fn<<<sweep_grid, kSweepThreads, dyn, st>>>(g->view(), g->chunk_v.as<uint32_t>(),
-                                                           (uint32_t)g->nchunks, C, reinterpret_cast<double*>(A),
-                                                           hub, prev);
+                                                           (uint32_t)g->nchunks, C, reinterpret_cast<double*>(A), hub,
+                                                           prev);
         }
         kt_end(st);
         launches++;
         edge_launches++;
       }
       if (pull) {
-        pr_finalize<true><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, P, C, added, L1 + it, prev);
+        pr_finalize<true><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), g->in_view().off, pull_step,
+                                                   A, P, C, R, added, L1 + it, prev);
       } else {
-        pr_finalize<false><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), A, P, C, added, L1 + it,
-                                                    prev);
+        pr_finalize<false><<<vblocks, 256, 0, st>>>((uint32_t)n, g->off.as<uint32_t>(), g->off.as<uint32_t>(), 1u,
+                                                    A, P, C, R, added, L1 + it, prev);
       }
       launches++;
     }
@@ -488,7 +514,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   // a new graph whose buffers reuse a freed graph's addresses from matching
   struct GraphKey {
     uint64_t uid;
-    const void *off, *adj, *chunk_v, *hub_bits, *hub_slot, *hub_vertex, *a, *p, *c, *l1;
+    const void *off, *adj, *chunk_v, *hub_bits, *hub_slot, *hub_vertex, *a, *p, *c, *r, *l1;
     int64_t n, m, iters;
     int variant, grid, pull, cacheH, hubH, hubmode, shape;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof *this) == 0; }
@@ -508,6 +534,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   key.a = A;
   key.p = P;
   key.c = C;
+  key.r = R;
   key.l1 = L1;
   key.n = n;
   key.m = g->m;

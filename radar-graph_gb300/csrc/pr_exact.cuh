@@ -19,6 +19,7 @@
 // work is per vertex (the quotient, the damping step, |p - p'|).
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 
 namespace rg {
@@ -106,6 +107,27 @@ __host__ __device__ __forceinline__ double fx_to_double(const U128& s) {
   }
   const unsigned long long ex = (unsigned long long)(t - kPrFrac + 1023);
   return double_of((ex << 52) | (M & 0xFFFFFFFFFFFFFull));
+}
+
+// a / b rounded to nearest (the IEEE quotient) from y = RN(1/b), for a
+// positive normal double a and a positive integer b held exactly as a double,
+// with every intermediate value normal (PageRank: a = p' >= 0.15/n, b = a
+// degree below 2^32).  Five FP64 operations instead of a division.
+// Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1), 1990): if y is
+// the correctly rounded 1/b, q lies within one ulp of a/b and r = a - b*q is
+// exact, then RN(q + r*y) = RN(a/b).  q0 = RN(a*y) lies within 1.5 ulp of
+// a/b; one correction q1 = RN(q0 + RN(a - b*q0)*y) has error
+// |q0 - a/b| * O(2^-52) before its single rounding, so q1 lies within
+// 0.5 ulp + tiny < 1 ulp, its residual a - b*q1 is exactly representable
+// (computed exactly by the FMA), and the second correction is the theorem's
+// step.  tests/test_pr_exact_host.py compares it with IEEE division on
+// random and adversarial samples.
+__host__ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
+  const double q0 = a * y;
+  const double r0 = fma(-b, q0, a);
+  const double q1 = fma(r0, y, q0);
+  const double r1 = fma(-b, q1, a);
+  return fma(r1, y, q1);
 }
 
 // The L1 threshold of PageRank.C:172 (epsilon = 1e-7, the double) scaled
