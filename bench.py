@@ -535,7 +535,7 @@ def bench_batched(rg, ngraphs=512, k=64, pr_iters=10, plain_graphs=24, seed=7):
 # served stream: 3 resident graphs, Poisson arrivals, BFS 60% / BC 25% / Radii 15%
 # ---------------------------------------------------------------------------
 
-def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=5, workers=4):
+def bench_serving(rg, graphs, rates=(200, 400, 800, 1600, 3200, 12800), per_rate=600, seed=5, workers=4, slo_ms=100.0):
     rng = np.random.default_rng(seed)
 
     def draw(nq):
@@ -556,6 +556,7 @@ def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=
     plain_qs = draw(60)
     plain_out = []
     plain_s = 0.0
+    per_kind = {}
     for gi, kind, src in plain_qs:
         G, buf = graphs[gi], bufs[(gi, kind)]
         t0 = time.perf_counter()
@@ -565,11 +566,18 @@ def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=
             G.bc_sources(np.array([src], np.uint32), "push", out=buf)
         else:
             G.radii_seeds(rg.radii_query_seeds(src, G.n), "push", out=buf)
-        plain_s += time.perf_counter() - t0
+        dt = time.perf_counter() - t0
+        plain_s += dt
+        k = per_kind.setdefault(f"{kind}_s{int(G.n).bit_length() - 1}", [0, 0.0])
+        k[0] += 1
+        k[1] += dt
         plain_out.append(np.array(buf))  # kept for the identity check, outside the timed span
     plain_qps = len(plain_qs) / plain_s
     out = {"graphs": [int(g.n) for g in graphs], "mix": "BFS 60% / BC 25% / Radii 15%",
-           "plain_queries_per_s": round(plain_qps, 1), "rates": []}
+           "plain_queries_per_s": round(plain_qps, 1),
+           "plain_ms_per_query": {k: {"queries": c, "ms": round(1e3 * t / c, 3), "share_of_plain_time":
+                                      round(t / plain_s, 3)} for k, (c, t) in sorted(per_kind.items())},
+           "rates": []}
     with rg.Server(graphs, workers=workers, max_batch=64) as S:
         # identical results: the plain sample served in one burst
         ts = [S.submit(gi, kind, src) for gi, kind, src in plain_qs]
@@ -612,6 +620,10 @@ def bench_serving(rg, graphs, rates=(200, 800, 3200, 12800), per_rate=600, seed=
                                  "queries": st["completed"], "coalesced": st["batched"]})
         out["best_qps"] = round(best, 1)
         out["speedup_vs_plain"] = round(best / plain_qps, 2)
+        # the highest offered rate served with p99 within the latency objective
+        ok = [r for r in out["rates"] if r["p99_ms"] <= slo_ms]
+        out["slo"] = {"p99_ms": slo_ms, "max_offered_qps_within": max((r["offered_qps"] for r in ok), default=None),
+                      "served_qps_there": max((r["qps"] for r in ok), default=None)}
     return out
 
 
