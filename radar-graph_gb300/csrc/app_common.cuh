@@ -214,8 +214,10 @@ rg_status launch_push(rg_graph* g, const DevGraph& pg, const FView& in, const Op
 
 // One dense bitmask round over every edge (mask_pull_sweep): next_bits must be
 // cleared; the caller compacts it afterwards.
+// `full`: the bits a vertex can still receive (mask_pull_sweep skips rows
+// that hold them all; 0 = gather every row).
 static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
-                                          uint32_t* next_bits, cudaStream_t st) {
+                                          uint32_t* next_bits, cudaStream_t st, unsigned long long full = 0ull) {
   static std::atomic<uint64_t> carveout_set{0};  // one copy per translation unit, like the kernel
   RG_TRY(once_per_device(carveout_set, [] {
     RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
@@ -231,7 +233,8 @@ static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long*
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);
   mask_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(),
-                                                                         (uint32_t)g->nchunks, visited, next, next_bits);
+                                                                         (uint32_t)g->nchunks, visited, next, next_bits,
+                                                                         full);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
   g_timing.kernel_launches++;

@@ -572,15 +572,18 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
   RG_TRY(frontier_alloc(g, S.f[1]));
   // seeding loop (Radii.C:162-169): NextVisited[v] = 1<<i is a plain store, so
   // on a collision the largest i wins (the single-thread order)
-  std::vector<uint32_t> starts(k), uv;
+  std::vector<uint32_t> starts(k), sdeg(k), uv, udeg;
   std::vector<unsigned long long> um;
-  RG_TRY(lookup_ids(g, seeds_orig, k, true, starts.data(), nullptr));
+  RG_TRY(lookup_ids(g, seeds_orig, k, true, starts.data(), sdeg.data()));
   for (int i = 0; i < k; i++) {
     const uint32_t v = starts[i];
     auto it = std::find(uv.begin(), uv.end(), v);
-    if (it == uv.end()) { uv.push_back(v); um.push_back(1ull << i); }
+    if (it == uv.end()) { uv.push_back(v); um.push_back(1ull << i); udeg.push_back(sdeg[i]); }
     else um[it - uv.begin()] = 1ull << i;
   }
+  // the bits that can spread: seeded at a vertex with out-edges
+  unsigned long long full = 0ull;
+  for (size_t j = 0; j < uv.size(); j++) full |= udeg[j] ? um[j] : 0ull;
   CallTimer timer(g);
   unsigned long long* vis = S.visited.as<unsigned long long>();
   unsigned long long* nvis = S.next_visited.as<unsigned long long>();
@@ -611,7 +614,7 @@ rg_status radii_run(rg_graph* g, int variant, const uint32_t* seeds_orig, int k,
       // dense round: pull over every edge (same next masks and frontier)
       RG_CUDA(cudaMemsetAsync(nxt.bits, 0, 4 * ((n + 31) / 32), st));
       g_timing.edges_traversed += cur.degsum;
-      RG_TRY(launch_mask_sweep(g, vis, nvis, nxt.bits, st));
+      RG_TRY(launch_mask_sweep(g, vis, nvis, nxt.bits, st, full));
       Frontier shell;  // non-owning view of nxt for the compaction
       shell.bits.p = nxt.bits;
       RG_TRY(compact_bits(g, shell, st, true, radii, round, nullptr, nxt.queue, nxt.qoff));

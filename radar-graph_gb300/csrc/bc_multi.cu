@@ -404,8 +404,10 @@ rg_status bc_multi_run(rg_graph* g, const uint32_t* src_orig, int k, double* h_o
   if (g->directed) RG_TRY(inq.reserve(4 * (n + 66)));
   Levels L(st);
   RG_TRY(L.ensure(2 * n + 64, 0, 0, st));
-  std::vector<uint32_t> s_int(k), uniq;
-  RG_TRY(lookup_ids(g, src_orig, k, true, s_int.data(), nullptr));
+  std::vector<uint32_t> s_int(k), s_deg(k), uniq;
+  RG_TRY(lookup_ids(g, src_orig, k, true, s_int.data(), s_deg.data()));
+  unsigned long long full = 0ull;  // the bits that can spread: sources with out-edges
+  for (int q = 0; q < k; q++) full |= s_deg[q] ? (1ull << q) : 0ull;
   for (int q = 0; q < k; q++) {
     if (std::find(uniq.begin(), uniq.end(), s_int[q]) == uniq.end()) uniq.push_back(s_int[q]);
   }
@@ -462,7 +464,7 @@ rg_status bc_multi_run(rg_graph* g, const uint32_t* src_orig, int k, double* h_o
     if (cur.count + cur.degsum > threshold && cur.degsum > 0) {
       RG_CUDA(cudaMemsetAsync(nxt.bits, 0, 4 * nwords, st));
       g_timing.edges_traversed += cur.degsum;
-      RG_TRY(launch_mask_sweep(g, pS, pN, nxt.bits, st));
+      RG_TRY(launch_mask_sweep(g, pS, pN, nxt.bits, st, full));
       Frontier shell;
       shell.bits.p = nxt.bits;
       RG_TRY(compact_bits(g, shell, st, true, nullptr, 0, nullptr, nxt.queue, nxt.qoff));

@@ -108,8 +108,10 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
   RG_TRY(S.src.reserve(4 * 64));
   RG_TRY(frontier_alloc(g, S.f[0]));
   RG_TRY(frontier_alloc(g, S.f[1]));
-  std::vector<uint32_t> src(k), uniq;
-  RG_TRY(lookup_ids(g, src_orig, k, true, src.data(), nullptr));
+  std::vector<uint32_t> src(k), sdeg(k), uniq;
+  RG_TRY(lookup_ids(g, src_orig, k, true, src.data(), sdeg.data()));
+  unsigned long long full = 0ull;  // the bits that can spread: sources with out-edges
+  for (int q = 0; q < k; q++) full |= sdeg[q] ? (1ull << q) : 0ull;
   for (int q = 0; q < k; q++) {
     if (std::find(uniq.begin(), uniq.end(), src[q]) == uniq.end()) uniq.push_back(src[q]);
   }
@@ -139,7 +141,7 @@ rg_status bfs_multi_run(rg_graph* g, const uint32_t* src_orig, int k, int32_t* h
       g_timing.edges_traversed += cur.degsum;
       // dense level: the bitmask pull over every edge (seen is stable during
       // the level; N receives only the new bits)
-      RG_TRY(launch_mask_sweep(g, seen, N, nxt.bits, st));
+      RG_TRY(launch_mask_sweep(g, seen, N, nxt.bits, st, full));
       Frontier shell;
       shell.bits.p = nxt.bits;
       RG_TRY(compact_bits(g, shell, st, true, nullptr, 0, nullptr, nxt.queue, nxt.qoff));
