@@ -125,16 +125,28 @@ __device__ __forceinline__ void rq_flush(const unsigned long long* __restrict__ 
   if (grew) bit_set(next_bits, row);
 }
 
+// The bits each word can still receive (a query's samples with out-edges):
+// a row whose W words hold them all cannot grow, and its edges are not
+// gathered -- as in mask_pull_sweep, this skips most of the graph in the
+// last dense rounds.  All zero: every row is gathered.
+template <int W>
+struct RowFull {
+  unsigned long long w[W];
+};
+
 // Dense round, W words: next[v] |= (OR of vis[u] over every neighbour u) &
 // ~vis[v] per word.  Edge-balanced like mask_pull_sweep: a warp takes a
 // 512-edge chunk, kItems edges per lane, row pieces combined by a segmented
-// OR scan, one flush per row piece.
+// OR scan, one flush per row piece; rows that cannot grow are not gathered.
 template <int W, int kItems>
 __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                      uint32_t nchunks, const unsigned long long* __restrict__ vis,
-                                                     unsigned long long* nvis, uint32_t* next_bits) {
+                                                     unsigned long long* nvis, uint32_t* next_bits, RowFull<W> full) {
   constexpr int kStep = 32 * kItems;
   static_assert(kSweepChunk % kStep == 0, "chunk must hold whole steps");
+  bool skipping = false;
+#pragma unroll
+  for (int w = 0; w < W; w++) skipping |= full.w[w] != 0ull;
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -152,10 +164,39 @@ __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t*
         uint32_t u[kItems];
 #pragma unroll
         for (int i = 0; i < kItems; i++) u[i] = (e + i < g.m) ? g.adj[e + i] : 0u;
+        // the rows of the lane's edges, and which of them can still grow
+        uint32_t rowi[kItems];
+        unsigned need = 0;
+        {
+          auto open_row = [&](uint32_t rv) {
+            if (!skipping) return true;
+            unsigned long long rw[W];
+            load_row<W>(vis + (size_t)rv * W, rw);
+            bool open = false;
+#pragma unroll
+            for (int w = 0; w < W; w++) open |= (rw[w] & full.w[w]) != full.w[w];
+            return open;
+          };
+          uint32_t rv = v, rn = nxt;
+          bool open = open_row(rv);
+#pragma unroll
+          for (int i = 0; i < kItems; i++) {
+            const uint32_t ee = e + i;
+            if (ee < g.m && ee >= rn) {
+              do {
+                rv++;
+                rn = g.off[rv + 1];
+              } while (ee >= rn);
+              open = open_row(rv);
+            }
+            rowi[i] = rv;
+            if (ee < g.m && open) need |= 1u << i;
+          }
+        }
         unsigned long long x[kItems][W];
 #pragma unroll
         for (int i = 0; i < kItems; i++) {
-          if (e + i < g.m) {
+          if ((need >> i) & 1u) {
             load_row<W>(vis + (size_t)u[i] * W, x[i]);
           } else {
 #pragma unroll
@@ -167,15 +208,11 @@ __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t*
         for (int i = 0; i < kItems; i++) {
           const uint32_t ee = e + i;
           if (ee >= g.m) break;
-          if (ee >= nxt) {  // a row piece that ends in this lane
+          if (rowi[i] != row) {  // a row piece that ends in this lane
             rq_flush<W>(vis, nvis, next_bits, row, part);
 #pragma unroll
             for (int w = 0; w < W; w++) part[w] = 0ull;
-            do {
-              v++;
-              nxt = g.off[v + 1];
-            } while (ee >= nxt);
-            row = v;
+            row = rowi[i];
           }
 #pragma unroll
           for (int w = 0; w < W; w++) part[w] |= x[i][w];
@@ -198,7 +235,9 @@ __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t*
 
 template <int W>
 rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned long long* nvis, uint32_t* bits,
-                          cudaStream_t st) {
+                          cudaStream_t st, const unsigned long long* full_words) {
+  RowFull<W> full;
+  for (int w = 0; w < W; w++) full.w[w] = full_words[w];
   constexpr int kItems = W <= 2 ? 8 : 16 / W;  // about 16 mask words in flight per lane
   auto kern = rq_pull_sweep<W, kItems>;
   static std::atomic<int> resident{0};
@@ -211,7 +250,7 @@ rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned l
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);
   kern<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(), (uint32_t)g->nchunks, vis,
-                                                             nvis, bits);
+                                                             nvis, bits, full);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
   g_timing.kernel_launches++;
@@ -220,13 +259,13 @@ rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned l
 }
 
 rg_status rq_sweep(int W, rg_graph* g, const unsigned long long* vis, unsigned long long* nvis, uint32_t* bits,
-                   cudaStream_t st) {
+                   cudaStream_t st, const unsigned long long* full_words) {
   switch (W) {
-    case 1: return launch_rq_sweep<1>(g, vis, nvis, bits, st);
-    case 2: return launch_rq_sweep<2>(g, vis, nvis, bits, st);
-    case 4: return launch_rq_sweep<4>(g, vis, nvis, bits, st);
-    case 8: return launch_rq_sweep<8>(g, vis, nvis, bits, st);
-    default: return launch_rq_sweep<16>(g, vis, nvis, bits, st);
+    case 1: return launch_rq_sweep<1>(g, vis, nvis, bits, st, full_words);
+    case 2: return launch_rq_sweep<2>(g, vis, nvis, bits, st, full_words);
+    case 4: return launch_rq_sweep<4>(g, vis, nvis, bits, st, full_words);
+    case 8: return launch_rq_sweep<8>(g, vis, nvis, bits, st, full_words);
+    default: return launch_rq_sweep<16>(g, vis, nvis, bits, st, full_words);
   }
 }
 
@@ -250,10 +289,10 @@ rg_status radii_multi_run(rg_graph* g, const uint32_t* seeds_orig, int k, int nq
   while (W < nq) W *= 2;
   // per query: seeding loop (Radii.C:162-169), NextVisited[v] = 1<<i is a
   // plain store, so on a collision the largest i wins
-  std::vector<uint32_t> all(k * (size_t)nq), sv, frontier;
+  std::vector<uint32_t> all(k * (size_t)nq), adeg(k * (size_t)nq), sv, sdeg, frontier;
   std::vector<unsigned long long> sm;
   std::vector<int> sw;
-  RG_TRY(lookup_ids(g, seeds_orig, (int64_t)k * nq, true, all.data(), nullptr));
+  RG_TRY(lookup_ids(g, seeds_orig, (int64_t)k * nq, true, all.data(), adeg.data()));
   for (int q = 0; q < nq; q++) {
     const size_t first = sv.size();
     for (int i = 0; i < k; i++) {
@@ -263,11 +302,15 @@ rg_status radii_multi_run(rg_graph* g, const uint32_t* seeds_orig, int k, int nq
         sv.push_back(v);
         sm.push_back(1ull << i);
         sw.push_back(q);
+        sdeg.push_back(adeg[(size_t)q * k + i]);
       } else {
         sm[it - sv.begin()] = 1ull << i;
       }
     }
   }
+  // per word, the bits that can spread: samples seeded at vertices with out-edges
+  std::vector<unsigned long long> full(16, 0ull);
+  for (size_t j = 0; j < sv.size(); j++) full[sw[j]] |= sdeg[j] ? sm[j] : 0ull;
   frontier = sv;
   std::sort(frontier.begin(), frontier.end());
   frontier.erase(std::unique(frontier.begin(), frontier.end()), frontier.end());
@@ -310,7 +353,7 @@ rg_status radii_multi_run(rg_graph* g, const uint32_t* seeds_orig, int k, int nq
     if (cur.degsum > 0) {
       g_timing.edges_traversed += cur.degsum;
       if (cur.count + cur.degsum > threshold) {
-        RG_TRY(rq_sweep(W, g, pv, pn, nxt.bits, st));
+        RG_TRY(rq_sweep(W, g, pv, pn, nxt.bits, st, full.data()));
       } else {
         RG_TRY(launch_push<OpRadiiW, kHubNone>(g, g->view(), cur, OpRadiiW{pv, pn, W}, HubInfo{}, nxt.bits, st));
       }
