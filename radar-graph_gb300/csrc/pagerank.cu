@@ -83,26 +83,27 @@ __device__ __forceinline__ U128 block_sum128(U128 v) {
   return t;  // valid in thread 0
 }
 
-// p'/deg, the IEEE quotient of PR_F (PageRank.C:48), by degree class: 0 for
-// no out-edges, an exact exponent shift for a power-of-two degree (the
-// quotient is exact; p' >= 0.15/n keeps it normal), else div_by_recip.
-// Degree-sorted graphs keep whole warps in one class, so the FP64 work runs
-// only in the warps of other degrees.
-__device__ __forceinline__ double pr_quotient(double pn, uint32_t d, const double* __restrict__ rdeg, int64_t v) {
+// p'/deg, the IEEE quotient of PR_F (PageRank.C:48), by degree class (the
+// deg_quotient classes): the integer reciprocal is read only for degrees
+// that need it, and degree-sorted graphs keep whole warps in one class.
+__device__ __forceinline__ double pr_quotient(double pn, uint32_t d, const unsigned long long* __restrict__ rmag,
+                                              int64_t v) {
   if (d == 0) return 0.0;
   if ((d & (d - 1)) == 0) return double_of(bits_of(pn) - ((unsigned long long)(31 - __clz(d)) << 52));
-  return div_by_recip(pn, (double)d, rdeg[v]);
+  return div_by_magic(pn, d, rmag[v]);
 }
 
-// p = 1/n, contrib = p/deg (PageRank.C:126-138), rdeg = RN(1/deg) for the
-// later iterations' quotients; the accumulators start at 0.
-__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p, double* contrib, double* rdeg,
-                        double p0) {
+// p = 1/n, contrib = p/deg (PageRank.C:126-138), rmag = the integer
+// reciprocal of each degree that is neither 0, 1 nor a power of two (for the
+// later iterations' quotients); the accumulators start at 0.
+__global__ void pr_init(uint32_t n, const uint32_t* __restrict__ off, double* p, double* contrib,
+                        unsigned long long* rmag, double p0) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     p[v] = p0;
     const uint32_t d = off[v + 1] - off[v];
-    contrib[v] = d ? p0 / (double)d : 0.0;
-    rdeg[v] = d ? 1.0 / (double)d : 0.0;
+    const unsigned long long R = (d & (d - 1)) ? recip_magic(d) : 0ull;
+    contrib[v] = deg_quotient(p0, d, R);
+    rmag[v] = R;
   }
 }
 
@@ -343,28 +344,34 @@ PullFn pull_variant(int64_t shape) {
 template <bool kExact>
 __global__ void __launch_bounds__(256) pr_finalize(uint32_t n, const uint32_t* __restrict__ off,
                                                    const uint32_t* __restrict__ pull_off, uint32_t step, U128* acc,
-                                                   double* p, double* contrib, const double* __restrict__ rdeg,
-                                                   double added, U128* l1_out, const U128* l1_prev) {
+                                                   double* p, double* contrib,
+                                                   const unsigned long long* __restrict__ rmag, double added,
+                                                   U128* l1_out, const U128* l1_prev) {
   if (converged(l1_prev)) return;
   U128 local{0ull, 0ull};
   double* accd = reinterpret_cast<double*>(acc);
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    // the tests of zero and equality are integer compares (the FP64 pipe is
+    // the scarce one): every value here is a nonnegative double, not NaN
     double sum;
+    bool has;
     if (kExact) {
       const U128 a = acc[v];
-      sum = (a.lo | a.hi) ? fx_to_double(a) : 0.0;
+      has = (a.lo | a.hi) != 0ull;
+      sum = has ? fx_to_double(a) : 0.0;
       const uint32_t b = pull_off[v], e = pull_off[v + 1];
       if (e > b && b / step != (e - 1) / step) acc[v] = U128{0ull, 0ull};
     } else {
       sum = accd[v];
+      has = (bits_of(sum) << 1) != 0ull;
       accd[v] = 0.0;
     }
     // fma(0.85, 0, added) is `added` exactly: vertices without in-edges skip it
-    const double pn = sum != 0.0 ? fma(kDamp, sum, added) : added;
+    const double pn = has ? fma(kDamp, sum, added) : added;
     const double po = p[v];
-    if (po != pn) add128(local, fx_from_double(fabs(po - pn)));
+    if (bits_of(po) != bits_of(pn)) add128(local, fx_from_double(fabs(po - pn)));
     p[v] = pn;
-    contrib[v] = pr_quotient(pn, off[v + 1] - off[v], rdeg, v);  // = pn / deg, correctly rounded
+    contrib[v] = pr_quotient(pn, off[v + 1] - off[v], rmag, v);  // = pn / deg, correctly rounded
   }
   const U128 t = block_sum128(local);
   if (threadIdx.x == 0 && (t.lo | t.hi)) atomic_add128(l1_out, t);
@@ -379,7 +386,7 @@ __global__ void pr_gather(const double* __restrict__ p, const uint32_t* __restri
 }
 
 struct PrState {
-  DevBuf acc, p, contrib, rdeg, l1, out;
+  DevBuf acc, p, contrib, rmag, l1, out;
 };
 
 }  // namespace
@@ -398,7 +405,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   RG_TRY(S.acc.reserve(sizeof(U128) * n));
   RG_TRY(S.p.reserve(8 * n));
   RG_TRY(S.contrib.reserve(8 * n));
-  RG_TRY(S.rdeg.reserve(8 * n));
+  RG_TRY(S.rmag.reserve(8 * n));
   RG_TRY(S.l1.reserve(sizeof(U128) * (max_iters + 1)));
   RG_TRY(S.out.reserve(8 * n));
   // the reference's constants (PageRank.C:126-138)
@@ -468,7 +475,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   U128* A = S.acc.as<U128>();
   double* P = S.p.as<double>();
   double* C = S.contrib.as<double>();
-  double* R = S.rdeg.as<double>();
+  unsigned long long* R = S.rmag.as<unsigned long long>();
   U128* L1 = S.l1.as<U128>();
   // The whole run (init + every iteration) is enqueued without host round
   // trips; it is captured once as a CUDA graph and replayed on later calls

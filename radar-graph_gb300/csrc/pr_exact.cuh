@@ -14,9 +14,9 @@
 // with n, m < 2^32, so every sum is exact.  Smaller terms would be truncated
 // below 2^-124.
 //
-// GB300 issues one FP64 instruction per 16 lane-operations of an integer
-// instruction, so the per-edge additions stay on the integer pipes; the FP64
-// work is per vertex (the quotient, the damping step, |p - p'|).
+// GB300 issues FP64 at a small fraction of its integer rate, so the per-edge
+// additions and the per-vertex quotient p/deg stay on the integer pipes; the
+// FP64 work is the damping step and |p - p'|.
 #pragma once
 
 #include <math.h>
@@ -109,25 +109,79 @@ __host__ __device__ __forceinline__ double fx_to_double(const U128& s) {
   return double_of((ex << 52) | (M & 0xFFFFFFFFFFFFFull));
 }
 
-// a / b rounded to nearest (the IEEE quotient) from y = RN(1/b), for a
-// positive normal double a and a positive integer b held exactly as a double,
-// with every intermediate value normal (PageRank: a = p' >= 0.15/n, b = a
-// degree below 2^32).  Five FP64 operations instead of a division.
-// Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1), 1990): if y is
-// the correctly rounded 1/b, q lies within one ulp of a/b and r = a - b*q is
-// exact, then RN(q + r*y) = RN(a/b).  q0 = RN(a*y) lies within 1.5 ulp of
-// a/b; one correction q1 = RN(q0 + RN(a - b*q0)*y) has error
-// |q0 - a/b| * O(2^-52) before its single rounding, so q1 lies within
-// 0.5 ulp + tiny < 1 ulp, its residual a - b*q1 is exactly representable
-// (computed exactly by the FMA), and the second correction is the theorem's
-// step.  tests/test_pr_exact_host.py compares it with IEEE division on
-// random and adversarial samples.
-__host__ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
-  const double q0 = a * y;
-  const double r0 = fma(-b, q0, a);
-  const double q1 = fma(r0, y, q0);
-  const double r1 = fma(-b, q1, a);
-  return fma(r1, y, q1);
+__host__ __device__ __forceinline__ int clz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __clz((int)x);
+#else
+  return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+__host__ __device__ __forceinline__ unsigned long long mulhi64(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// The integer reciprocal of a degree d >= 3 that is not a power of two:
+// R = floor(2^(63+l) / d) with 2^(l-1) < d < 2^l, so R lies in [2^63, 2^64).
+// Long division in two 64-by-32-bit steps.
+__host__ __device__ __forceinline__ unsigned long long recip_magic(uint32_t d) {
+  const int l = 32 - clz32(d);
+  const unsigned long long hi = 1ull << (31 + l);  // 2^(63+l) = hi * 2^32
+  const unsigned long long q1 = hi / d, r1 = hi % d;
+  return (q1 << 32) | ((r1 << 32) / d);
+}
+
+// a / d rounded to nearest, ties to even (the IEEE quotient), on the integer
+// pipes: GB300 issues FP64 at a small fraction of its integer rate, and the
+// FP64 route (a reciprocal and two Markstein correction steps, or a
+// division) cost five or more FP64 operations per vertex.
+//   a = Ma * 2^(E-1075), A = Ma * 2^11 in [2^63, 2^64), N = A * 2^(l-1):
+//   a / d = (N / d) * 2^(E-1085-l), and N / d lies in (2^62, 2^64).
+//   Q = mulhi(A, R) is floor(N / d) or one less (R undershoots 2^(63+l)/d by
+//   less than one, so A*R/2^64 undershoots N/d by less than one); the
+//   remainder N - Q*d is below 2d, so it is exact modulo 2^64 and one
+//   comparison corrects Q.  The 53 leading bits of Q, its next bit and a
+//   sticky bit (lower bits of Q or a nonzero remainder) round to nearest even.
+// Preconditions: d >= 3 not a power of two, R = recip_magic(d), a a
+// positive normal double with a >= 2^-990 (so the quotient is normal).
+__host__ __device__ __forceinline__ double div_by_magic(double a, uint32_t d, unsigned long long R) {
+  const unsigned long long b = bits_of(a);
+  const int E = (int)(b >> 52);
+  const unsigned long long A = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11;
+  const int l = 32 - clz32(d);
+  unsigned long long Q = mulhi64(A, R);
+  unsigned long long r = (A << (l - 1)) - Q * (unsigned long long)d;
+  if (r >= d) {
+    Q++;
+    r -= d;
+  }
+  const int k = (Q >> 63) ? 11 : 10;  // bits of Q below the 53 kept
+  unsigned long long M = Q >> k;
+  const bool guard = (Q >> (k - 1)) & 1ull;
+  const bool sticky = (Q & ((1ull << (k - 1)) - 1ull)) != 0ull || r != 0ull;
+  unsigned long long ex = (unsigned long long)(E - 10 - l + k);  // biased exponent of M * 2^(k+E-1085-l)
+  if (guard && (sticky || (M & 1ull))) {
+    M++;
+    if (M == (1ull << 53)) {
+      M >>= 1;
+      ex++;
+    }
+  }
+  return double_of((ex << 52) | (M & 0xFFFFFFFFFFFFFull));
+}
+
+// p / deg(v), the IEEE quotient of PR_F (PageRank.C:48), by degree class: 0
+// for no out-edges, an exact exponent shift for a power of two, else
+// div_by_magic with R = recip_magic(d) (a >= 2^-990: PageRank values are at
+// least 0.15/n).
+__host__ __device__ __forceinline__ double deg_quotient(double a, uint32_t d, unsigned long long R) {
+  if (d == 0) return 0.0;
+  if ((d & (d - 1)) == 0) return double_of(bits_of(a) - ((unsigned long long)(31 - clz32(d)) << 52));
+  return div_by_magic(a, d, R);
 }
 
 // The L1 threshold of PageRank.C:172 (epsilon = 1e-7, the double) scaled
