@@ -455,9 +455,10 @@ typedef enum rg_option {
   RG_OPT_HUB_SMEM_KB = 2,
   /* dense iteration when |F| + outdeg(F) > m / value (default 20, ligra.h:283) */
   RG_OPT_DENSE_DIV = 3,
-  /* shape of the full-graph PageRank pull sweep: 10 * (edges per lane, 4 or 8)
-   * + cache mode (0 plain loads; 1 streamed edge array; 2 streamed edge array
-   * and gathers kept in L1/L2).  Default 81.  Never changes a result. */
+  /* shape of the full-graph PageRank pull sweep: 10 * (edges per lane, 4, 8
+   * or 16) + cache mode (0 plain loads; 1 streamed edge array; 2 streamed
+   * edge array and gathers kept in L1/L2).  Default 161.  Never changes a
+   * result. */
   RG_OPT_SWEEP_SHAPE = 4,
   /* BC's forward (path counting) pushes use hub copies too: 1 (default) or
    * 0 (only the backward pushes do).  The backward phase pushes into the

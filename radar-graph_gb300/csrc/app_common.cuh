@@ -215,31 +215,38 @@ rg_status launch_push(rg_graph* g, const DevGraph& pg, const FView& in, const Op
 // One dense bitmask round over every edge (mask_pull_sweep): next_bits must be
 // cleared; the caller compacts it afterwards.
 // `full`: the bits a vertex can still receive (mask_pull_sweep skips rows
-// that hold them all; 0 = gather every row).
-static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
-                                          uint32_t* next_bits, cudaStream_t st, unsigned long long full = 0ull) {
-  static std::atomic<uint64_t> carveout_set{0};  // one copy per translation unit, like the kernel
+// that hold them all; 0 = gather every row).  Edges per lane follow the
+// thread's sweep shape (16 for shapes 160..162, else 8).
+template <int kItems>
+rg_status launch_mask_sweep_k(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
+                              uint32_t* next_bits, cudaStream_t st, unsigned long long full) {
+  static std::atomic<uint64_t> carveout_set{0};  // one copy per translation unit and instance, like the kernel
   RG_TRY(once_per_device(carveout_set, [] {
-    RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+    RG_CUDA(cudaFuncSetAttribute(mask_pull_sweep<kItems>, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
     return RG_OK;
   }));
   static std::atomic<int> resident{0};
   int per_sm = resident.load(std::memory_order_relaxed);
   if (!per_sm) {
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mask_pull_sweep, 256, 0));
+    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mask_pull_sweep<kItems>, 256, 0));
     per_sm = std::max(per_sm, 1);
     resident.store(per_sm, std::memory_order_relaxed);
   }
   const int64_t grid = std::min<int64_t>((int64_t)device_sms() * per_sm, (g->nchunks * 32 + 255) / 256);
   kt_begin(st);
-  mask_pull_sweep<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(g->in_view(), g->in_chunks(),
-                                                                         (uint32_t)g->nchunks, visited, next, next_bits,
-                                                                         full);
+  mask_pull_sweep<kItems><<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(
+      g->in_view(), g->in_chunks(), (uint32_t)g->nchunks, visited, next, next_bits, full);
   kt_end(st);
   RG_CUDA(cudaGetLastError());
   g_timing.kernel_launches++;
   g_timing.edge_launches++;
   return RG_OK;
+}
+
+static inline rg_status launch_mask_sweep(rg_graph* g, const unsigned long long* visited, unsigned long long* next,
+                                          uint32_t* next_bits, cudaStream_t st, unsigned long long full = 0ull) {
+  return g_opts.sweep_shape / 10 == 16 ? launch_mask_sweep_k<16>(g, visited, next, next_bits, st, full)
+                                       : launch_mask_sweep_k<8>(g, visited, next, next_bits, st, full);
 }
 
 // One edgeMap.  `out` (may be null for no_output ops) receives the next

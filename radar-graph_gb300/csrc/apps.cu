@@ -719,8 +719,8 @@ rg_status rg_set_option(rg_option opt, int64_t value) {
       g_opts.dense_div = value;
       return RG_OK;
     case RG_OPT_SWEEP_SHAPE:
-      if ((value / 10 != 4 && value / 10 != 8) || value % 10 > 2) {
-        return fail(RG_EINVAL, "sweep shape must be 40..42 or 80..82");
+      if ((value / 10 != 4 && value / 10 != 8 && value / 10 != 16) || value % 10 > 2) {
+        return fail(RG_EINVAL, "sweep shape must be 40..42, 80..82 or 160..162");
       }
       g_opts.sweep_shape = value;
       return RG_OK;

@@ -517,11 +517,14 @@ static __device__ __forceinline__ void mask_flush(const unsigned long long* __re
 // gathered: in the last dense rounds that is most of the graph (RMAT s22,
 // 64 samples: 64 % of the edges in round 4, 99.8 % in round 5), and the hub
 // rows, which hold the most edges, fill first.  full = 0 gathers every row.
+template <int kItems>
 static __global__ void __launch_bounds__(256) mask_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                         uint32_t nchunks, const unsigned long long* __restrict__ visited,
                                                         unsigned long long* next_visited, uint32_t* next_bits,
                                                         unsigned long long full) {
-  constexpr int kItems = 8, kStep = 32 * kItems;
+  static_assert(kItems == 8 || kItems == 16, "8 or 16 edges per lane");
+  constexpr int kStep = 32 * kItems;
+  constexpr int kBatch = 8;  // gathers in flight per lane at a time
   const int lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -533,12 +536,14 @@ static __global__ void __launch_bounds__(256) mask_pull_sweep(DevGraph g, const 
       uint32_t row = kNone;
       unsigned long long part = 0;
       if (e < g.m) {
-        const U32x8 w = ld_stream_v8(g.adj + e);  // in bounds: adj is padded by 8 entries
         uint32_t v = upper_index(g.off, vlo, vhi, e);
         uint32_t nxt = g.off[v + 1];
         // the rows of the lane's edges first, then gathers only for rows
-        // that can still grow
-        uint32_t rowi[kItems];
+        // that can still grow.  8 edges per lane keep the rows in registers;
+        // 16 walk them again while accumulating (the offsets hit L1), which
+        // keeps the kernel at 8 gathers and 8 row ids per lane
+        constexpr bool kKeepRows = kItems <= 8;
+        uint32_t rowi[kKeepRows ? kItems : 1];
         unsigned need = 0;
         {
           uint32_t rv = v, rn = nxt;
@@ -550,24 +555,38 @@ static __global__ void __launch_bounds__(256) mask_pull_sweep(DevGraph g, const 
               do { rv++; rn = g.off[rv + 1]; } while (ee >= rn);
               open = full == 0ull || (__ldg(visited + rv) & full) != full;
             }
-            rowi[i] = rv;
+            if (kKeepRows) rowi[kKeepRows ? i : 0] = rv;
             if (ee < g.m && open) need |= 1u << i;
           }
         }
-        unsigned long long x[kItems];
-#pragma unroll
-        for (int i = 0; i < kItems; i++) x[i] = ((need >> i) & 1u) ? __ldg(visited + w.v[i]) : 0ull;
         row = v;
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (rowi[i] != row) {
-            mask_flush(visited, next_visited, next_bits, row, part);  // a row piece that ends in this lane
-            part = 0;
-            row = rowi[i];
+        for (int b = 0; b < kItems; b += kBatch) {
+          if (e + b >= g.m) break;
+          // this batch's neighbour ids (in bounds: adj is padded by 8
+          // entries and the batch starts before m)
+          const U32x8 w = ld_stream_v8(g.adj + e + b);
+          unsigned long long x[kBatch];
+#pragma unroll
+          for (int j = 0; j < kBatch; j++) x[j] = ((need >> (b + j)) & 1u) ? __ldg(visited + w.v[j]) : 0ull;
+#pragma unroll
+          for (int j = 0; j < kBatch; j++) {
+            const int i = b + j;
+            const uint32_t ee = e + i;
+            if (ee >= g.m) break;
+            const bool ends = kKeepRows ? rowi[kKeepRows ? i : 0] != row : ee >= nxt;
+            if (ends) {
+              mask_flush(visited, next_visited, next_bits, row, part);  // a row piece that ends in this lane
+              part = 0;
+              if (kKeepRows) {
+                row = rowi[kKeepRows ? i : 0];
+              } else {
+                do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+                row = v;
+              }
+            }
+            part |= x[j];
           }
-          part |= x[i];
         }
       }
 #pragma unroll

@@ -189,7 +189,7 @@ template <bool kCache, int kItems, int kMode>
 __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
     pr_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v, uint32_t nchunks,
                   const double* __restrict__ contrib, U128* acc, uint32_t H, const U128* l1_prev) {
-  static_assert(kItems == 4 || kItems == 8, "4 or 8 edges per lane");
+  static_assert(kItems == 4 || kItems == 8 || kItems == 16, "4, 8 or 16 edges per lane");
   if (converged(l1_prev)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* hc = reinterpret_cast<double*>(smem_raw);
@@ -215,55 +215,77 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
       bool cont = false;      // the lane's last row continues past the lane
       if (e < g.m) {
         // in bounds: adj is padded by 8 entries and 32-byte aligned
-        uint32_t uu[kItems];
-        if (kItems == 8 && kMode >= 1) {
+        // neighbour ids: 16 edges per lane load each batch's 8 ids with its
+        // gathers (fewer live registers), narrower shapes load them here
+        constexpr bool kIdsPerBatch = kItems > 8;
+        uint32_t uu[kIdsPerBatch ? 1 : kItems];
+        if (kIdsPerBatch) {
+        } else if (kItems == 8 && kMode >= 1) {
           const U32x8 w = ld_stream_v8(g.adj + e);
 #pragma unroll
-          for (int i = 0; i < kItems; i++) uu[i] = w.v[i];
+          for (int i = 0; i < kItems; i++) uu[kIdsPerBatch ? 0 : i] = w.v[i];
         } else {
 #pragma unroll
           for (int h = 0; h < kItems / 4; h++) {
             const uint4 w = kMode >= 1 ? ld_stream_v4(g.adj + e + 4 * h, first)
                                        : __ldg(reinterpret_cast<const uint4*>(g.adj + e + 4 * h));
-            uu[4 * h] = w.x;
-            uu[4 * h + 1] = w.y;
-            uu[4 * h + 2] = w.z;
-            uu[4 * h + 3] = w.w;
+            uu[kIdsPerBatch ? 0 : 4 * h] = w.x;
+            uu[kIdsPerBatch ? 0 : 4 * h + 1] = w.y;
+            uu[kIdsPerBatch ? 0 : 4 * h + 2] = w.z;
+            uu[kIdsPerBatch ? 0 : 4 * h + 3] = w.w;
           }
         }
         uint32_t v = upper_index(g.off, vlo, vhi, e);
         uint32_t nxt = g.off[v + 1];
         const bool first_started_before = g.off[v] < e;
-        double x[kItems];
-#pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          const uint32_t u = uu[i];
-          x[i] = (e + i < g.m) ? ((kCache && u < H) ? hc[u]
-                                  : kMode == 2      ? __longlong_as_double((long long)ld_keep_u64(contrib_bits + u, keep))
-                                                    : __ldg(contrib + u))
-                               : 0.0;
-        }
         row = v;
         bool at_first = true;
+        // the gathers in batches of at most 8 per lane (16 edges per lane
+        // halve the warp scans per edge without holding 16 values at once)
+        constexpr int kBatch = kItems > 8 ? 8 : kItems;
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (ee >= nxt) {
-            // row `row` ends inside this lane: it is the lane's head piece if
-            // it began in an earlier lane, else complete and stored here
-            if (at_first && first_started_before) {
-              head = part;
-              head_row = row;
+        for (int b = 0; b < kItems; b += kBatch) {
+          if (e + b >= g.m) break;
+          U32x8 ids{};
+          if (kIdsPerBatch) {
+            // in bounds: adj is padded by 8 entries and the batch starts before m
+            if (kMode >= 1) {
+              ids = ld_stream_v8(g.adj + e + b);
             } else {
-              store128(acc + row, part);
+              const uint4 lo = __ldg(reinterpret_cast<const uint4*>(g.adj + e + b));
+              const uint4 hi = __ldg(reinterpret_cast<const uint4*>(g.adj + e + b + 4));
+              ids = U32x8{{lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w}};
             }
-            at_first = false;
-            part = U128{0ull, 0ull};
-            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
-            row = v;
           }
-          add128(part, fx_from_double(x[i]));
+          double x[kBatch];
+#pragma unroll
+          for (int j = 0; j < kBatch; j++) {
+            const uint32_t u = kIdsPerBatch ? ids.v[j] : uu[kIdsPerBatch ? 0 : b + j];
+            x[j] = (e + b + j < g.m) ? ((kCache && u < H) ? hc[u]
+                                        : kMode == 2 ? __longlong_as_double((long long)ld_keep_u64(contrib_bits + u, keep))
+                                                     : __ldg(contrib + u))
+                                     : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < kBatch; j++) {
+            const uint32_t ee = e + b + j;
+            if (ee >= g.m) break;
+            if (ee >= nxt) {
+              // row `row` ends inside this lane: it is the lane's head piece
+              // if it began in an earlier lane, else complete and stored here
+              if (at_first && first_started_before) {
+                head = part;
+                head_row = row;
+              } else {
+                store128(acc + row, part);
+              }
+              at_first = false;
+              part = U128{0ull, 0ull};
+              do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+              row = v;
+            }
+            add128(part, fx_from_double(x[j]));
+          }
         }
         cont = nxt > e + kItems;
       }
@@ -330,6 +352,9 @@ PullFn pull_variant(int64_t shape) {
     case 80: return pr_pull_sweep<kCache, 8, 0>;
     case 81: return pr_pull_sweep<kCache, 8, 1>;
     case 82: return pr_pull_sweep<kCache, 8, 2>;
+    case 160: return pr_pull_sweep<kCache, 16, 0>;
+    case 161: return pr_pull_sweep<kCache, 16, 1>;
+    case 162: return pr_pull_sweep<kCache, 16, 2>;
     default: return pr_pull_sweep<kCache, 4, 0>;
   }
 }
@@ -443,7 +468,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
                                         : pr_push_sweep<kHubNone>;
   PullFn pull_fn = cache ? pull_variant<true>(g_opts.sweep_shape) : pull_variant<false>(g_opts.sweep_shape);
   // edges per warp step of the chosen pull (32 lanes x 4 or 8 edges, pull_variant's shapes)
-  const uint32_t pull_step = (g_opts.sweep_shape / 10 == 8) ? 256u : 128u;
+  const uint32_t pull_step = 32u * (uint32_t)(g_opts.sweep_shape / 10);
   const int pull_threads = cache ? 1024 : kPullThreads;
   const size_t pull_dyn = sizeof(double) * cacheH;
   const int sms = device_sms();

@@ -118,7 +118,7 @@ struct Options {
   int64_t hub_slots = 0;     // RG_OPT_HUB_SLOTS
   int64_t hub_smem_kb = 48;  // RG_OPT_HUB_SMEM_KB (0 = no hub copies in the frontier push)
   int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
-  int64_t sweep_shape = 81;  // RG_OPT_SWEEP_SHAPE
+  int64_t sweep_shape = 161;  // RG_OPT_SWEEP_SHAPE
   int64_t bc_fwd_hubs = 1;   // RG_OPT_BC_FWD_HUBS
 };
 

@@ -1,6 +1,7 @@
 // Autotuner: for one graph and variant, times candidate schedules of each
 // app (push/pull direction, the dense threshold m/x of ligra.h:283, hub
-// copies on/off and their shared-memory budget) and keeps the fastest per app
+// copies on/off and their shared-memory budget, PageRank's sweep shape) and
+// keeps the fastest per app
 // in the graph.  Later app calls on that graph use the choice.  No schedule
 // changes any result, so tuning is safe to run on live graphs.
 
@@ -30,10 +31,17 @@ std::vector<Options> candidates(int app, bool hubs, const Options& base) {
   // resident CTAs
   const std::vector<int64_t> kbs = hubs ? std::vector<int64_t>{0, 4, 16, 48} : std::vector<int64_t>{0};
   switch (app) {
-    case kAppPagerank:  // push (with or without hub copies) against pull (with or without cached hubs)
+    case kAppPagerank:  // push (with or without hub copies) against pull (with or without cached
+                        // hubs, 8 or 16 edges per lane: fewer warp scans per edge against more registers)
       for (int64_t kb : kbs) add(0, 20, kb);
-      add(1, 20, 0);
-      if (hubs) add(1, 20, 48);
+      for (int64_t shape : {81, 161}) {
+        add(1, 20, 0);
+        out.back().sweep_shape = shape;
+        if (hubs) {
+          add(1, 20, 48);
+          out.back().sweep_shape = shape;
+        }
+      }
       break;
     case kAppBfs:
       for (int64_t div : {10, 20, 40, 80}) add(1, div, 0);

@@ -54,7 +54,7 @@ def graph(request):
     return G(request.param)
 
 
-@pytest.mark.parametrize("shape", [40, 41, 42, 80, 81, 82])
+@pytest.mark.parametrize("shape", [40, 41, 42, 80, 81, 82, 160, 161, 162])
 @pytest.mark.parametrize("direction,kb", [(0, 0), (0, 16), (0, 48), (1, 0), (1, 16), (1, 64)])
 @pytest.mark.parametrize("variant", ["radar", "hubdup", "push-pull"])
 def test_pagerank_schedules(graph, shape, direction, kb, variant):
@@ -118,7 +118,7 @@ def test_pull_schedules_are_bit_identical(graph):
     G_ = graph.gs
     G_.clear_tuning()  # the thread's options below, not an earlier test's tuning
     ref = None
-    for shape in (40, 41, 42, 80, 81, 82):
+    for shape in (40, 41, 42, 80, 81, 82, 160, 161, 162):
         for kb in (0, 48):
             with options(direction=1, sweep_shape=shape, hub_smem_kb=kb):
                 r, it, _ = G_.pagerank("radar", 20)
