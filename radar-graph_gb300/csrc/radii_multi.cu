@@ -85,46 +85,6 @@ __global__ void rq_mark(const uint32_t* __restrict__ q, int64_t count, int W, in
   }
 }
 
-// One vertex's W mask words with as few requests as possible: gathers are
-// bound by the L1TEX request rate, not by bytes, so a 32-byte row costs one
-// 256-bit load rather than four 64-bit ones.  Rows are W*8-byte aligned.
-template <int W>
-__device__ __forceinline__ void load_row(const unsigned long long* p, unsigned long long (&x)[W]) {
-  if constexpr (W == 1) {
-    x[0] = __ldg(p);
-  } else if constexpr (W == 2) {
-    const ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p));
-    x[0] = t.x;
-    x[1] = t.y;
-  } else {
-#pragma unroll
-    for (int b = 0; b < W; b += 4) {
-      uint32_t r[8];
-      asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-          : "l"(p + b));
-#pragma unroll
-      for (int h = 0; h < 4; h++) x[b + h] = ((unsigned long long)r[2 * h + 1] << 32) | r[2 * h];
-    }
-  }
-}
-
-template <int W>
-__device__ __forceinline__ void rq_flush(const unsigned long long* __restrict__ vis, unsigned long long* nvis,
-                                         uint32_t* next_bits, uint32_t row, const unsigned long long (&part)[W]) {
-  bool grew = false;
-#pragma unroll
-  for (int w = 0; w < W; w++) {
-    if (!part[w]) continue;
-    const unsigned long long x = part[w] & ~__ldg(vis + (size_t)row * W + w);
-    if (x) {
-      atomicOr(nvis + (size_t)row * W + w, x);
-      grew = true;
-    }
-  }
-  if (grew) bit_set(next_bits, row);
-}
-
 // The bits each word can still receive (a query's samples with out-edges):
 // a row whose W words hold them all cannot grow, and its edges are not
 // gathered -- as in mask_pull_sweep, this skips most of the graph in the
@@ -134,101 +94,98 @@ struct RowFull {
   unsigned long long w[W];
 };
 
+// One lane's word of a row piece: the new bits (not yet in vis) go into nvis,
+// and the row is marked in next_bits once per slot.  The W lanes of a slot
+// walk the same rows and so reach every flush together; slot_mask names them.
+template <int W>
+__device__ __forceinline__ void rq_flush_word(const unsigned long long* __restrict__ vis, unsigned long long* nvis,
+                                              uint32_t* next_bits, uint32_t row, int w, unsigned slot_mask,
+                                              unsigned long long part) {
+  const unsigned long long x = part ? part & ~__ldg(vis + (size_t)row * W + w) : 0ull;
+  if (x) atomicOr(nvis + (size_t)row * W + w, x);
+  const unsigned grew = __ballot_sync(slot_mask, x != 0ull);
+  if (grew && w == 0) bit_set(next_bits, row);
+}
+
 // Dense round, W words: next[v] |= (OR of vis[u] over every neighbour u) &
-// ~vis[v] per word.  Edge-balanced like mask_pull_sweep: a warp takes a
-// 512-edge chunk, kItems edges per lane, row pieces combined by a segmented
-// OR scan, one flush per row piece; rows that cannot grow are not gathered.
-template <int W, int kItems>
+// ~vis[v] per word.  Word lanes: the warp is 32/W slots of W lanes; a slot
+// walks 16*W consecutive edges of the warp's 512-edge chunk and lane w of the
+// slot gathers word w of each neighbour's row, so one gather instruction
+// reads whole W-word rows (64 bytes at W = 8) of 32/W edges.  A lane skips
+// the gather where its own word of the row already holds every bit its query
+// can spread (`full`), and flushes a row piece where the row ends; the
+// slots' last pieces are combined by a segmented OR scan across slots once
+// per chunk.
+template <int W>
 __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                      uint32_t nchunks, const unsigned long long* __restrict__ vis,
                                                      unsigned long long* nvis, uint32_t* next_bits, RowFull<W> full) {
-  constexpr int kStep = 32 * kItems;
-  static_assert(kSweepChunk % kStep == 0, "chunk must hold whole steps");
-  bool skipping = false;
-#pragma unroll
-  for (int w = 0; w < W; w++) skipping |= full.w[w] != 0ull;
+  static_assert(W >= 1 && W <= 16 && (W & (W - 1)) == 0, "1..16 words, a power of two");
+  constexpr int kSlots = 32 / W;
+  constexpr int kPer = kSweepChunk / kSlots;  // edges per slot per chunk
+  constexpr int kBatch = 8;                   // gathers in flight per lane at a time
+  static_assert(kPer % kBatch == 0, "whole batches per slot");
   const int lane = threadIdx.x & 31;
+  const int w = lane % W, slot = lane / W;
+  const unsigned slot_mask = ((1u << W) - 1u) << (slot * W);  // W <= 16
+  unsigned long long fw = 0ull;  // the bits word w can still receive
+#pragma unroll
+  for (int i = 0; i < W; i++) fw = i == w ? full.w[i] : fw;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t c = warp; c < nchunks; c += nwarps) {
     const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
-    for (int r = 0; r < kSweepChunk / kStep; r++) {
-      const uint32_t e = c * kSweepChunk + r * kStep + lane * kItems;
-      uint32_t row = kNone;
-      unsigned long long part[W];
-#pragma unroll
-      for (int w = 0; w < W; w++) part[w] = 0ull;
-      if (e < g.m) {
-        uint32_t v = upper_index(g.off, vlo, vhi, e);
-        uint32_t nxt = g.off[v + 1];
-        uint32_t u[kItems];
-#pragma unroll
-        for (int i = 0; i < kItems; i++) u[i] = (e + i < g.m) ? g.adj[e + i] : 0u;
-        // the rows of the lane's edges, and which of them can still grow
-        uint32_t rowi[kItems];
+    const uint32_t e0 = c * kSweepChunk + slot * kPer;  // the slot's first edge
+    uint32_t row = kNone;
+    unsigned long long part = 0ull;
+    if (e0 < g.m) {
+      uint32_t v = upper_index(g.off, vlo, vhi, e0);
+      uint32_t nxt = g.off[v + 1];
+      auto word_open = [&](uint32_t r) { return fw != 0ull && (__ldg(vis + (size_t)r * W + w) & fw) != fw; };
+      bool open = word_open(v);
+      row = v;
+      for (int b = 0; b < kPer; b += kBatch) {
+        if (e0 + b >= g.m) break;
+        // the batch's rows and which gathers this lane needs
+        uint32_t rowj[kBatch];
         unsigned need = 0;
-        {
-          auto open_row = [&](uint32_t rv) {
-            if (!skipping) return true;
-            unsigned long long rw[W];
-            load_row<W>(vis + (size_t)rv * W, rw);
-            bool open = false;
 #pragma unroll
-            for (int w = 0; w < W; w++) open |= (rw[w] & full.w[w]) != full.w[w];
-            return open;
-          };
-          uint32_t rv = v, rn = nxt;
-          bool open = open_row(rv);
-#pragma unroll
-          for (int i = 0; i < kItems; i++) {
-            const uint32_t ee = e + i;
-            if (ee < g.m && ee >= rn) {
-              do {
-                rv++;
-                rn = g.off[rv + 1];
-              } while (ee >= rn);
-              open = open_row(rv);
-            }
-            rowi[i] = rv;
-            if (ee < g.m && open) need |= 1u << i;
+        for (int j = 0; j < kBatch; j++) {
+          const uint32_t ee = e0 + b + j;
+          if (ee < g.m && ee >= nxt) {
+            do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
+            open = word_open(v);
           }
+          rowj[j] = v;
+          if (ee < g.m && open) need |= 1u << j;
         }
-        unsigned long long x[kItems][W];
+        // in bounds: adj is padded by 8 entries and the batch starts before m
+        const U32x8 ids = ld_stream_v8(g.adj + e0 + b);
+        unsigned long long x[kBatch];
 #pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          if ((need >> i) & 1u) {
-            load_row<W>(vis + (size_t)u[i] * W, x[i]);
-          } else {
+        for (int j = 0; j < kBatch; j++) x[j] = ((need >> j) & 1u) ? __ldg(vis + (size_t)ids.v[j] * W + w) : 0ull;
 #pragma unroll
-            for (int w = 0; w < W; w++) x[i][w] = 0ull;
+        for (int j = 0; j < kBatch; j++) {
+          if (e0 + b + j >= g.m) break;
+          if (rowj[j] != row) {  // a row piece that ends in this slot
+            rq_flush_word<W>(vis, nvis, next_bits, row, w, slot_mask, part);
+            part = 0ull;
+            row = rowj[j];
           }
-        }
-        row = v;
-#pragma unroll
-        for (int i = 0; i < kItems; i++) {
-          const uint32_t ee = e + i;
-          if (ee >= g.m) break;
-          if (rowi[i] != row) {  // a row piece that ends in this lane
-            rq_flush<W>(vis, nvis, next_bits, row, part);
-#pragma unroll
-            for (int w = 0; w < W; w++) part[w] = 0ull;
-            row = rowi[i];
-          }
-#pragma unroll
-          for (int w = 0; w < W; w++) part[w] |= x[i][w];
+          part |= x[j];
         }
       }
+    }
+    // segmented OR scan of the slots' last pieces (lanes of one word)
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o);
-#pragma unroll
-        for (int w = 0; w < W; w++) {
-          const unsigned long long t = __shfl_up_sync(0xffffffffu, part[w], o);
-          if (lane >= o && tr == row) part[w] |= t;
-        }
-      }
-      const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, 1);
-      if (row != kNone && (lane == 31 || next_row != row)) rq_flush<W>(vis, nvis, next_bits, row, part);
+    for (int o = 1; o < kSlots; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o * W);
+      const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o * W);
+      if (slot >= o && tr == row) part |= t;
+    }
+    const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, W);
+    if (row != kNone && (slot == kSlots - 1 || next_row != row)) {
+      rq_flush_word<W>(vis, nvis, next_bits, row, w, slot_mask, part);
     }
   }
 }
@@ -238,8 +195,7 @@ rg_status launch_rq_sweep(rg_graph* g, const unsigned long long* vis, unsigned l
                           cudaStream_t st, const unsigned long long* full_words) {
   RowFull<W> full;
   for (int w = 0; w < W; w++) full.w[w] = full_words[w];
-  constexpr int kItems = W <= 2 ? 8 : 16 / W;  // about 16 mask words in flight per lane
-  auto kern = rq_pull_sweep<W, kItems>;
+  auto kern = rq_pull_sweep<W>;
   static std::atomic<int> resident{0};
   int per_sm = resident.load(std::memory_order_relaxed);
   if (!per_sm) {
