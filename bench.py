@@ -309,7 +309,7 @@ def bench_batched_sources(rg, gs, reps=2, plain_sample=8):
     cases = {
         "bfs": (64, lambda s: gs.bfs_multi(s), lambda s: gs.bfs("radar", int(s))[1]),
         "bc": (64, lambda s: gs.bc_multi(s), lambda s: gs.bc_sources(np.array([s], np.uint32), "radar")[0]),
-        "radii": (8, lambda s: gs.radii_multi(s), lambda s: gs.radii_seeds(s, "radar")[0]),
+        "radii": (16, lambda s: gs.radii_multi(s), lambda s: gs.radii_seeds(s, "radar")[0]),
     }
     for kind, (k, multi, single) in cases.items():
         if kind == "radii":
@@ -774,6 +774,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served legs")
     ap.add_argument("--only", default="", help="comma list of extra legs to run (default all): " + ",".join(EXTRA_LEGS))
     ap.add_argument("--cpu-pr-iters", type=int, default=2)
+    ap.add_argument("--pr-shape", type=int, default=0,
+                    help="pin PageRank's pull sweep shape (RG_OPT_SWEEP_SHAPE, e.g. 81 or 161) after autotuning "
+                         "(for profiler captures of one shape); 0 keeps the tuned choice")
     ap.add_argument("--step-only", action="store_true",
                     help="stop after the timed step (for profiler captures of it): no e2e, legs or CPU baseline")
     args = ap.parse_args()
@@ -798,6 +801,9 @@ def main():
     root = int(gs.pick_roots(1)[0])  # GAP SourcePicker, as the reference arm picks it
     bc_src = gs.bc_pick_sources(1)
     tuning = gs.autotune("radar")
+    if args.pr_shape:
+        tuning["pagerank"][1]["sweep_shape"] = args.pr_shape
+        gs.set_tuning(tuning)
     rg.set_kernel_timing(True)
     for _ in range(args.warmup):
         run_step(rg, gs, root, bc_src, {})

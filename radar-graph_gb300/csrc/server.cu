@@ -51,16 +51,12 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 // Radii queries per shared traversal: one 8-byte mask word per query and
-// vertex.  Once the masks outgrow a few times L2, every dense round streams
-// them from DRAM and the cost per query rises (measured on RMAT s24: 4.4 ms
-// per query in batches of 4, 4.9 in batches of 8), so the batch is the
-// largest power of two <= 8 whose masks fit 600 MB.
-constexpr int kRadiiBatch = 8;
-int radii_batch(const rg_graph* g) {
-  int w = kRadiiBatch;
-  while (w > 1 && (size_t)8 * w * (size_t)g->n > (size_t)600 << 20) w /= 2;
-  return w;
-}
+// vertex, up to rg_radii_multi's 16.  The dense rounds gather whole W-word
+// rows, so the cost per query falls as the batch grows even where the masks
+// stream from DRAM (RMAT s24: 3.32 ms per query in batches of 4, 2.92 in 8,
+// 2.80 in 16; s22: 1.17, 0.91, 0.81); HBM admission bounds the memory.
+constexpr int kRadiiBatch = 16;
+int radii_batch(const rg_graph*) { return kRadiiBatch; }
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(Clock::now().time_since_epoch()).count();
