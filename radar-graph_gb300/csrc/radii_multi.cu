@@ -94,98 +94,180 @@ struct RowFull {
   unsigned long long w[W];
 };
 
-// One lane's word of a row piece: the new bits (not yet in vis) go into nvis,
-// and the row is marked in next_bits once per slot.  The W lanes of a slot
-// walk the same rows and so reach every flush together; slot_mask names them.
+// Words per lane in the dense rounds: up to four (one 32-byte load), so the
+// row walk and bookkeeping a lane repeats per item are shared by its words.
 template <int W>
-__device__ __forceinline__ void rq_flush_word(const unsigned long long* __restrict__ vis, unsigned long long* nvis,
-                                              uint32_t* next_bits, uint32_t row, int w, unsigned slot_mask,
-                                              unsigned long long part) {
-  const unsigned long long x = part ? part & ~__ldg(vis + (size_t)row * W + w) : 0ull;
-  if (x) atomicOr(nvis + (size_t)row * W + w, x);
-  const unsigned grew = __ballot_sync(slot_mask, x != 0ull);
-  if (grew && w == 0) bit_set(next_bits, row);
+__host__ __device__ constexpr int rq_words_per_lane() {
+  return W < 4 ? W : 4;
+}
+
+// A lane's kWL consecutive mask words (kWL*8-byte aligned) in one load.
+template <int kWL>
+__device__ __forceinline__ void rq_load_words(const unsigned long long* p, unsigned long long (&x)[kWL]) {
+  if constexpr (kWL == 1) {
+    x[0] = __ldg(p);
+  } else if constexpr (kWL == 2) {
+    const ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p));
+    x[0] = t.x;
+    x[1] = t.y;
+  } else {
+    uint32_t r[8];
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "l"(p));
+#pragma unroll
+    for (int h = 0; h < 4; h++) x[h] = ((unsigned long long)r[2 * h + 1] << 32) | r[2 * h];
+  }
+}
+
+// One lane's words of a row piece: the new bits (not yet in vis) go into
+// nvis, and the row is marked in next_bits once per slot.  The lanes of a
+// slot walk the same rows and so reach every flush together; slot_mask names
+// them.
+template <int W, int kWL>
+__device__ __forceinline__ void rq_flush_words(const unsigned long long* __restrict__ vis, unsigned long long* nvis,
+                                               uint32_t* next_bits, uint32_t row, int w0, unsigned slot_mask,
+                                               const unsigned long long (&part)[kWL]) {
+  bool any = false;
+#pragma unroll
+  for (int i = 0; i < kWL; i++) any |= part[i] != 0ull;
+  bool grew = false;
+  if (any) {
+    unsigned long long have[kWL];
+    rq_load_words<kWL>(vis + (size_t)row * W + w0, have);
+#pragma unroll
+    for (int i = 0; i < kWL; i++) {
+      const unsigned long long x = part[i] & ~have[i];
+      if (x) {
+        atomicOr(nvis + (size_t)row * W + w0 + i, x);
+        grew = true;
+      }
+    }
+  }
+  const unsigned g = __ballot_sync(slot_mask, grew);
+  if (g && w0 == 0) bit_set(next_bits, row);
 }
 
 // Dense round, W words: next[v] |= (OR of vis[u] over every neighbour u) &
-// ~vis[v] per word.  Word lanes: the warp is 32/W slots of W lanes; a slot
-// walks 16*W consecutive edges of the warp's 512-edge chunk and lane w of the
-// slot gathers word w of each neighbour's row, so one gather instruction
-// reads whole W-word rows (64 bytes at W = 8) of 32/W edges.  A lane skips
-// the gather where its own word of the row already holds every bit its query
-// can spread (`full`), and flushes a row piece where the row ends; the
-// slots' last pieces are combined by a segmented OR scan across slots once
-// per chunk.
+// ~vis[v] per word.  Word lanes: a slot of W/kWL lanes walks 512*W/(32*kWL)
+// consecutive edges of the warp's 512-edge chunk, and each lane gathers its
+// kWL consecutive words of every neighbour's row in one load, so one gather
+// instruction reads whole W-word rows (64 bytes at W = 8) of several edges.
+// A lane skips the gather where its words of the row already hold every bit
+// their queries can spread (`full`), and flushes a row piece where the row
+// ends; the slots' last pieces are combined by a segmented OR scan across
+// slots once per chunk.
 template <int W>
 __global__ void __launch_bounds__(256) rq_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                      uint32_t nchunks, const unsigned long long* __restrict__ vis,
                                                      unsigned long long* nvis, uint32_t* next_bits, RowFull<W> full) {
   static_assert(W >= 1 && W <= 16 && (W & (W - 1)) == 0, "1..16 words, a power of two");
-  constexpr int kSlots = 32 / W;
-  constexpr int kPer = kSweepChunk / kSlots;  // edges per slot per chunk
-  constexpr int kBatch = 8;                   // gathers in flight per lane at a time
-  static_assert(kPer % kBatch == 0, "whole batches per slot");
+  constexpr int kWL = rq_words_per_lane<W>();
+  constexpr int kLanes = W / kWL;              // lanes per slot
+  constexpr int kSlots = 32 / kLanes;
+  constexpr int kPer = kSweepChunk / kSlots;   // edges per slot per chunk
+  constexpr int kGroup = kWL == 4 ? 4 : 8;     // edges per id load
+  constexpr int kBatch = 8 / kWL;              // gathers in flight per lane at a time
+  static_assert(kPer % kGroup == 0, "whole id groups per slot");
   const int lane = threadIdx.x & 31;
-  const int w = lane % W, slot = lane / W;
-  const unsigned slot_mask = ((1u << W) - 1u) << (slot * W);  // W <= 16
-  unsigned long long fw = 0ull;  // the bits word w can still receive
+  const int slot = lane / kLanes;
+  const int w0 = (lane % kLanes) * kWL;
+  const unsigned slot_mask = (kLanes == 32 ? 0xffffffffu : ((1u << kLanes) - 1u)) << (slot * kLanes);
+  unsigned long long fw[kWL];  // the bits each of the lane's words can still receive
 #pragma unroll
-  for (int i = 0; i < W; i++) fw = i == w ? full.w[i] : fw;
+  for (int i = 0; i < kWL; i++) {
+    fw[i] = 0ull;
+#pragma unroll
+    for (int j = 0; j < W; j++) fw[i] = j == w0 + i ? full.w[j] : fw[i];
+  }
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t c = warp; c < nchunks; c += nwarps) {
     const uint32_t vlo = chunk_v[c], vhi = chunk_v[c + 1];
     const uint32_t e0 = c * kSweepChunk + slot * kPer;  // the slot's first edge
     uint32_t row = kNone;
-    unsigned long long part = 0ull;
+    unsigned long long part[kWL];
+#pragma unroll
+    for (int i = 0; i < kWL; i++) part[i] = 0ull;
     if (e0 < g.m) {
       uint32_t v = upper_index(g.off, vlo, vhi, e0);
       uint32_t nxt = g.off[v + 1];
-      auto word_open = [&](uint32_t r) { return fw != 0ull && (__ldg(vis + (size_t)r * W + w) & fw) != fw; };
-      bool open = word_open(v);
+      auto words_open = [&](uint32_t r) {
+        unsigned long long have[kWL];
+        rq_load_words<kWL>(vis + (size_t)r * W + w0, have);
+        bool open = false;
+#pragma unroll
+        for (int i = 0; i < kWL; i++) open |= fw[i] != 0ull && (have[i] & fw[i]) != fw[i];
+        return open;
+      };
+      bool open = words_open(v);
       row = v;
-      for (int b = 0; b < kPer; b += kBatch) {
+      for (int b = 0; b < kPer; b += kGroup) {
         if (e0 + b >= g.m) break;
-        // the batch's rows and which gathers this lane needs
-        uint32_t rowj[kBatch];
+        // the group's rows and which gathers this lane needs
+        uint32_t rowj[kGroup];
         unsigned need = 0;
 #pragma unroll
-        for (int j = 0; j < kBatch; j++) {
+        for (int j = 0; j < kGroup; j++) {
           const uint32_t ee = e0 + b + j;
           if (ee < g.m && ee >= nxt) {
             do { v++; nxt = g.off[v + 1]; } while (ee >= nxt);
-            open = word_open(v);
+            open = words_open(v);
           }
           rowj[j] = v;
           if (ee < g.m && open) need |= 1u << j;
         }
-        // in bounds: adj is padded by 8 entries and the batch starts before m
-        const U32x8 ids = ld_stream_v8(g.adj + e0 + b);
-        unsigned long long x[kBatch];
+        // in bounds: adj is padded by 8 entries and the group starts before m
+        U32x8 ids;
+        if constexpr (kGroup == 8) {
+          ids = ld_stream_v8(g.adj + e0 + b);
+        } else {
+          const uint4 q = ld_stream_v4(g.adj + e0 + b, policy_evict_first());
+          ids.v[0] = q.x;
+          ids.v[1] = q.y;
+          ids.v[2] = q.z;
+          ids.v[3] = q.w;
+        }
 #pragma unroll
-        for (int j = 0; j < kBatch; j++) x[j] = ((need >> j) & 1u) ? __ldg(vis + (size_t)ids.v[j] * W + w) : 0ull;
+        for (int h = 0; h < kGroup; h += kBatch) {
+          unsigned long long x[kBatch][kWL];
 #pragma unroll
-        for (int j = 0; j < kBatch; j++) {
-          if (e0 + b + j >= g.m) break;
-          if (rowj[j] != row) {  // a row piece that ends in this slot
-            rq_flush_word<W>(vis, nvis, next_bits, row, w, slot_mask, part);
-            part = 0ull;
-            row = rowj[j];
+          for (int j = 0; j < kBatch; j++) {
+            if ((need >> (h + j)) & 1u) {
+              rq_load_words<kWL>(vis + (size_t)ids.v[h + j] * W + w0, x[j]);
+            } else {
+#pragma unroll
+              for (int i = 0; i < kWL; i++) x[j][i] = 0ull;
+            }
           }
-          part |= x[j];
+#pragma unroll
+          for (int j = 0; j < kBatch; j++) {
+            if (e0 + b + h + j >= g.m) break;
+            if (rowj[h + j] != row) {  // a row piece that ends in this slot
+              rq_flush_words<W, kWL>(vis, nvis, next_bits, row, w0, slot_mask, part);
+#pragma unroll
+              for (int i = 0; i < kWL; i++) part[i] = 0ull;
+              row = rowj[h + j];
+            }
+#pragma unroll
+            for (int i = 0; i < kWL; i++) part[i] |= x[j][i];
+          }
         }
       }
     }
-    // segmented OR scan of the slots' last pieces (lanes of one word)
+    // segmented OR scan of the slots' last pieces (lanes of the same words)
 #pragma unroll
     for (int o = 1; o < kSlots; o <<= 1) {
-      const unsigned long long t = __shfl_up_sync(0xffffffffu, part, o * W);
-      const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o * W);
-      if (slot >= o && tr == row) part |= t;
+      const uint32_t tr = __shfl_up_sync(0xffffffffu, row, o * kLanes);
+#pragma unroll
+      for (int i = 0; i < kWL; i++) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, part[i], o * kLanes);
+        if (slot >= o && tr == row) part[i] |= t;
+      }
     }
-    const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, W);
+    const uint32_t next_row = __shfl_down_sync(0xffffffffu, row, kLanes);
     if (row != kNone && (slot == kSlots - 1 || next_row != row)) {
-      rq_flush_word<W>(vis, nvis, next_bits, row, w, slot_mask, part);
+      rq_flush_words<W, kWL>(vis, nvis, next_bits, row, w0, slot_mask, part);
     }
   }
 }
