@@ -97,7 +97,8 @@ class Clocks:
 
 
 def cuda_profiler(on):
-    """Marks the profiled ranges -- the timed step, and the extra legs -- for
+    """Marks the profiled ranges -- the timed step, the gather probe and the
+    extra legs -- for
     a profiler started with --profile-from-start off (cudaProfilerStart/Stop
     of the CUDA runtime the library loaded); a profiler started from the
     start stops at the end of the timed step unless the extra legs reopen
@@ -850,7 +851,9 @@ def main():
         sweep_kernel = "pr_push_sweep"
     # the graph's gather ceiling: stream the edge array and gather 8 bytes per
     # edge, nothing else -- what any pull over this graph must at least do
+    cuda_profiler(True)  # a profiled range of its own, for captures of the probe
     gather_ms = gather_ceiling_ms(gs)
+    cuda_profiler(False)
     traffic = measured_traffic(sweep_kernel, args.scale)
     apps = app_rates(stats, args.steps, hbm)
     for k in apps:
