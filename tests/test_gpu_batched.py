@@ -57,6 +57,32 @@ def test_bfs_multi_s16_dense_levels():
             assert np.array_equal(depths[q], orc.bfs_depths(off, adj, int(src[q])))
 
 
+@pytest.mark.parametrize("unsorted", [False, True], ids=["sorted", "unsorted"])
+def test_bitmask_sweep_widths_agree(unsorted):
+    """The dense bitmask rounds take 16 edges per lane with the 16x sweep
+    shapes and 8 otherwise; Radii (64 samples), 64-source BFS and the oracle's
+    depths must not depend on it, on a graph with several dense rounds and,
+    unsorted, with empty rows between nonempty ones."""
+    off, adj = rg.rmat_csr(16, 16, seed=1)
+    src = _sources(off, 64, seed=3)
+    with rg.Graph.from_csr(off, adj) as G, G.degree_sort() as S:
+        H = G if unsorted else S
+        got = {}
+        for shape in (81, 161):
+            old_shape, old_dir = rg.get_option("sweep_shape"), rg.get_option("direction")
+            try:
+                rg.set_option("sweep_shape", shape)
+                rg.set_option("direction", 1)  # pulled dense rounds
+                got[shape] = (H.radii("radar")[0], H.bfs_multi(src)[0])
+            finally:
+                rg.set_option("sweep_shape", old_shape)
+                rg.set_option("direction", old_dir)
+        assert np.array_equal(got[81][0], got[161][0])
+        assert np.array_equal(got[81][1], got[161][1])
+        for q in (0, 5, 63):
+            assert np.array_equal(got[161][1][q], orc.bfs_depths(off, adj, int(src[q])))
+
+
 def test_bfs_multi_rejects_bad_input(golden):
     g = golden["tiny"]
     with rg.Graph.from_csr(g["off"], g["adj"]) as G:

@@ -44,7 +44,7 @@ def test_golden_graphs(golden, name):
         assert np.array_equal(rows[0], G.radii_seeds(ref[0], "push")[0])
 
 
-@pytest.mark.parametrize("nq", [1, 3, 4, 9, 16])
+@pytest.mark.parametrize("nq", [1, 2, 3, 4, 5, 8, 9, 16])
 @pytest.mark.parametrize("uniform", [False, True], ids=["rmat", "er"])
 def test_many_queries(nq, uniform):
     off, adj = rg.rmat_csr(14, 16, seed=5, uniform=uniform)
