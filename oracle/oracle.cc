@@ -659,7 +659,7 @@ int orc_pagerank(int64_t n, const uint32_t* off, const uint32_t* adj, int varian
   return 0;
 }
 
-// PageRankDelta Compute (PageRankDelta.C:98-155).  Round 1 filters with
+// PageRankDelta Compute (PageRankDelta.C:98-155).  The first round filters with
 // PR_Vertex_F_FirstRound (:46-61), later rounds with PR_Vertex_F (:63-76); the
 // L1 norm is the sum of |Delta| over all vertices (:140-143) and the run stops
 // when it drops below 1e-7.  push-pull pulls its dense rounds (no
