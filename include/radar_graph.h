@@ -405,6 +405,8 @@ rg_status rg_device_alloc(size_t bytes, void** d_ptr);
 rg_status rg_device_free(void* d_ptr);
 rg_status rg_copy_to_device(void* d_dst, const void* h_src, size_t bytes);
 rg_status rg_copy_to_host(void* h_dst, const void* d_src, size_t bytes);
+/* Waits for all of the device's work, including result copies left in flight
+ * by RG_OPT_ASYNC_RESULTS. */
 rg_status rg_synchronize(void);
 /* The current device: its name (NUL-terminated, at most name_len bytes), SM
  * count and nominal HBM bandwidth in GB/s (memory clock x bus width x 2). */
@@ -464,7 +466,18 @@ typedef enum rg_option {
    * 0 (only the backward pushes do).  The backward phase pushes into the
    * levels that hold the hubs, where the reductions pile up; the forward
    * reaches the hubs in its first levels.  Never changes a result. */
-  RG_OPT_BC_FWD_HUBS = 5
+  RG_OPT_BC_FWD_HUBS = 5,
+  /* 1: rg_pagerank, rg_bfs, rg_bc, rg_bc_sources, rg_radii and
+   * rg_radii_seeds return once their results are staged on the device; the
+   * copies into the caller's host buffers run on the thread's copy stream,
+   * overlapping the next call, and are complete when rg_synchronize returns
+   * (host buffers from rg_host_alloc or otherwise page-locked let them
+   * overlap; pageable ones are copied before the call returns).  The host
+   * buffers must not be read or freed before then.  Scalar outputs (rounds,
+   * iterations, L1) are valid at return.  0 (default): every result is in
+   * the host buffers when the call returns.  Never changes a result; kept
+   * per thread, not per graph (an autotuned schedule does not change it). */
+  RG_OPT_ASYNC_RESULTS = 6
 } rg_option;
 rg_status rg_set_option(rg_option opt, int64_t value);
 rg_status rg_get_option(rg_option opt, int64_t* value);

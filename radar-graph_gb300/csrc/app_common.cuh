@@ -39,7 +39,10 @@ enum App { kAppPagerank = 0, kAppBfs = 1, kAppBc = 2, kAppRadii = 3 };
 struct OptScope {
   Options saved;
   OptScope(const rg_graph* g, int app) : saved(g_opts) {
-    if (g && g->tuned[app]) g_opts = g->topt[app];
+    if (g && g->tuned[app]) {
+      g_opts = g->topt[app];
+      g_opts.async_results = saved.async_results;  // the thread's, not the schedule's
+    }
   }
   ~OptScope() { g_opts = saved; }
 };
@@ -129,9 +132,48 @@ __global__ void gather_kernel(const T* __restrict__ in, const uint32_t* __restri
   for (; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = in[new_ids[i]];
 }
 
+// The thread's stream for asynchronous result copies (RG_OPT_ASYNC_RESULTS).
+rg_status copy_stream(cudaStream_t* out);
+
+// Result download, asynchronous form: `fill(stage)` enqueues on `st` the
+// work that writes the `count` results into a staging buffer; the copy into
+// h_out then runs on the thread's copy stream once that work is done, and the
+// staging buffer is released in stream order after the copy.  The call
+// returns without waiting, and the caller may overwrite its own buffers at
+// once.
+template <class T, class Fill>
+rg_status download_async(T* h_out, int64_t count, cudaStream_t st, Fill fill) {
+  cudaStream_t cs = nullptr;
+  RG_TRY(copy_stream(&cs));
+  DevBuf stage(true, cs);
+  RG_TRY(stage.reserve(sizeof(T) * (size_t)count));
+  RG_TRY(fill(stage.as<T>()));
+  cudaEvent_t ev = nullptr;
+  RG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev, 0);
+  cudaEventDestroy(ev);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, stage.p, sizeof(T) * (size_t)count, cudaMemcpyDeviceToHost, cs);
+  if (e != cudaSuccess) return cuda_fail(e, "asynchronous result copy", __FILE__, __LINE__);
+  return RG_OK;
+}
+
 template <class T>
 rg_status download_orig(rg_graph* g, const T* d_arr, T* h_out, DevBuf& tmp, cudaStream_t st) {
   if (!h_out) return RG_OK;
+  if (g_opts.async_results) {
+    return download_async<T>(h_out, g->n, st, [&](T* stage) -> rg_status {
+      if (g->sorted) {
+        int64_t blocks = std::min<int64_t>((g->n + 255) / 256, (int64_t)device_sms() * 32);
+        gather_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(d_arr, g->new_ids.as<uint32_t>(), g->n, stage);
+        RG_CUDA(cudaGetLastError());
+        g_timing.kernel_launches++;
+      } else {
+        RG_CUDA(cudaMemcpyAsync(stage, d_arr, sizeof(T) * g->n, cudaMemcpyDeviceToDevice, st));
+      }
+      return RG_OK;
+    });
+  }
   const T* src = d_arr;
   if (g->sorted) {
     RG_TRY(tmp.reserve(sizeof(T) * g->n));

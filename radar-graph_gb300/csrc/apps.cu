@@ -314,8 +314,7 @@ rg_status requeue_degrees(const rg_graph* g, const uint32_t* queue, int64_t coun
   RG_CUDA(cudaGetLastError());
   RG_TRY(scan_u32(ctx().ws, tmp.as<uint32_t>(), qoff, count, st));
   uint32_t total = 0;
-  RG_CUDA(cudaMemcpyAsync(&total, qoff + count, 4, cudaMemcpyDeviceToHost, st));
-  RG_CUDA(cudaStreamSynchronize(st));
+  RG_TRY(read_small(qoff + count, &total, 4, st));
   *degsum = total;
   return RG_OK;
 }
@@ -728,6 +727,10 @@ rg_status rg_set_option(rg_option opt, int64_t value) {
       if (value != 0 && value != 1) return fail(RG_EINVAL, "bc_fwd_hubs must be 0 or 1");
       g_opts.bc_fwd_hubs = value;
       return RG_OK;
+    case RG_OPT_ASYNC_RESULTS:
+      if (value != 0 && value != 1) return fail(RG_EINVAL, "async_results must be 0 or 1");
+      g_opts.async_results = value;
+      return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -741,6 +744,7 @@ rg_status rg_get_option(rg_option opt, int64_t* value) {
     case RG_OPT_DENSE_DIV: *value = g_opts.dense_div; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: *value = g_opts.sweep_shape; return RG_OK;
     case RG_OPT_BC_FWD_HUBS: *value = g_opts.bc_fwd_hubs; return RG_OK;
+    case RG_OPT_ASYNC_RESULTS: *value = g_opts.async_results; return RG_OK;
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }

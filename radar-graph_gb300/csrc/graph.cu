@@ -62,6 +62,27 @@ rg_status DevBuf::reserve(size_t b) {
 
 Workspace::~Workspace() {
   if (h_info) cudaFreeHost(h_info);
+  if (h_small) cudaFreeHost(h_small);
+}
+
+__global__ void read_small_kernel(const unsigned char* __restrict__ src, volatile unsigned char* dst, size_t bytes) {
+  for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
+  __threadfence_system();
+}
+
+rg_status read_small(const void* d_src, void* h_dst, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return RG_OK;
+  Workspace& ws = ctx().ws;
+  if (bytes > kSmallRead || !ws.h_small_dev) {
+    RG_CUDA(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, st));
+    RG_CUDA(cudaStreamSynchronize(st));
+    return RG_OK;
+  }
+  read_small_kernel<<<1, 256, 0, st>>>(static_cast<const unsigned char*>(d_src), ws.h_small_dev, bytes);
+  RG_CUDA(cudaGetLastError());
+  RG_CUDA(cudaStreamSynchronize(st));
+  memcpy(h_dst, ws.h_small, bytes);
+  return RG_OK;
 }
 
 static thread_local Ctx* t_ctx = nullptr;
@@ -94,7 +115,10 @@ rg_status get_ctx(Ctx** out) {
   }
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
-      cudaHostAlloc((void**)&c->ws.h_info, 64, cudaHostAllocDefault) != cudaSuccess ||
+      cudaHostAlloc((void**)&c->ws.h_info, 64, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&c->ws.h_info_dev, c->ws.h_info, 0) != cudaSuccess ||
+      cudaHostAlloc((void**)&c->ws.h_small, kSmallRead, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&c->ws.h_small_dev, c->ws.h_small, 0) != cudaSuccess ||
       c->ws.counters.reserve(4096) != RG_OK) {
     cudaGetLastError();
     delete c;
@@ -108,6 +132,14 @@ rg_status get_ctx(Ctx** out) {
 }
 
 Ctx& ctx() { return *t_ctx; }
+
+rg_status copy_stream(cudaStream_t* out) {
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
+  if (!c->copy_stream) RG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  *out = c->copy_stream;
+  return RG_OK;
+}
 
 }  // namespace rg
 
@@ -280,8 +312,11 @@ __global__ void comp_count(const uint32_t* __restrict__ bits, int64_t nwords, co
   }
 }
 
+// Also writes (count, degsum) straight into the caller's mapped host words
+// `host_info`, so a level's host sync needs no copy (none on a copy engine
+// another stream may be using).
 __global__ void comp_scan(uint32_t* part_c, uint32_t* part_d, int64_t nt, uint64_t* info,
-                          uint32_t* qoff_total_slot_base) {
+                          uint32_t* qoff_total_slot_base, volatile uint64_t* host_info) {
   __shared__ uint32_t cc, cd, tc, td;
   if (threadIdx.x == 0) { cc = 0; cd = 0; }
   __syncthreads();
@@ -301,6 +336,9 @@ __global__ void comp_scan(uint32_t* part_c, uint32_t* part_d, int64_t nt, uint64
     info[1] = cd;
     // qoff[count] = degsum: the slot sits right after the last queue entry
     if (qoff_total_slot_base) qoff_total_slot_base[cc] = cd;
+    host_info[0] = cc;
+    host_info[1] = cd;
+    __threadfence_system();
   }
 }
 
@@ -381,11 +419,10 @@ rg_status compact_bits(const rg_graph* g, Frontier& f, cudaStream_t st, bool syn
   uint32_t* qo = qoff_out ? qoff_out : f.qoff.as<uint32_t>();
   uint64_t* info = ws.counters.as<uint64_t>();
   comp_count<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, doff, pc, pd);
-  comp_scan<<<1, kCompThreads, 0, st>>>(pc, pd, nt, info, qo);
+  comp_scan<<<1, kCompThreads, 0, st>>>(pc, pd, nt, info, qo, ws.h_info_dev);
   comp_emit<<<(unsigned)nt, kCompThreads, 0, st>>>(f.bits.as<uint32_t>(), nwords, doff, pc, pd, q, qo, depth,
                                                    level, or_into);
   RG_CUDA(cudaGetLastError());
-  RG_CUDA(cudaMemcpyAsync(ws.h_info, info, 16, cudaMemcpyDeviceToHost, st));
   f.queue_valid = (queue_out == nullptr);
   f.bits_valid = true;
   if (sync) {
@@ -490,8 +527,7 @@ rg_status lookup_ids(const rg_graph* g, const uint32_t* ids, int64_t k, bool ori
                                                              (in_degree ? g->in_off : g->off).as<uint32_t>(), d, k,
                                                              d + k, d + 2 * k);
   RG_CUDA(cudaGetLastError());
-  RG_CUDA(cudaMemcpyAsync(back.data(), d + k, 8 * k, cudaMemcpyDeviceToHost, st));
-  RG_CUDA(cudaStreamSynchronize(st));
+  RG_TRY(read_small(d + k, back.data(), 8 * (size_t)k, st));
   for (int64_t i = 0; i < k; i++) {
     if (internal_out) internal_out[i] = back[i];
     if (deg_out) deg_out[i] = back[k + i];

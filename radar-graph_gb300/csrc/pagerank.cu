@@ -619,8 +619,7 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
   g_timing.edge_launches += edge_launches;
   RG_TRY(timer.stop());  // device work done; result copies are outside the timed span
   std::vector<U128> l1h(max_iters + 1, U128{0ull, 0ull});
-  RG_CUDA(cudaMemcpyAsync(l1h.data(), L1, sizeof(U128) * (max_iters + 1), cudaMemcpyDeviceToHost, st));
-  RG_CUDA(cudaStreamSynchronize(st));
+  RG_TRY(read_small(L1, l1h.data(), sizeof(U128) * (max_iters + 1), st));
   int64_t done = max_iters;
   bool broke = false;
   const U128 eps = pr_eps_fx();
@@ -628,7 +627,17 @@ rg_status pagerank_run(rg_graph* g, int variant, int64_t max_iters, double* h_ra
     if (less128(l1h[it], eps)) { done = it; broke = true; break; }
   }
   const int64_t last = broke ? done : max_iters - 1;
-  if (h_ranks) {
+  if (h_ranks && g_opts.async_results) {
+    RG_TRY(download_async<double>(h_ranks, n, st, [&](double* stage) -> rg_status {
+      if (g->sorted) {
+        pr_gather<<<vblocks, 256, 0, st>>>(P, g->new_ids.as<uint32_t>(), n, stage);
+        RG_CUDA(cudaGetLastError());
+      } else {
+        RG_CUDA(cudaMemcpyAsync(stage, P, 8 * n, cudaMemcpyDeviceToDevice, st));
+      }
+      return RG_OK;
+    }));
+  } else if (h_ranks) {
     // P holds the last computed ranks (p_next after a break, p_curr after
     // the final reset and swap of a run that used every iteration)
     if (g->sorted) {

@@ -105,7 +105,10 @@ struct Workspace {
   DevBuf tiles;          // push tile -> first frontier entry
   DevBuf counters;       // small device scalars
   DevBuf lookup;         // lookup_ids staging
-  uint64_t* h_info = nullptr;  // pinned host mirror of level info (count, degsum, ...)
+  uint64_t* h_info = nullptr;      // pinned, mapped host mirror of level info (count, degsum, ...)
+  uint64_t* h_info_dev = nullptr;  // the device's address of h_info (kernels write it directly)
+  unsigned char* h_small = nullptr;      // pinned, mapped scratch for small reads (read_small)
+  unsigned char* h_small_dev = nullptr;  // its device address
   ~Workspace();
 };
 
@@ -120,6 +123,7 @@ struct Options {
   int64_t dense_div = 20;    // RG_OPT_DENSE_DIV
   int64_t sweep_shape = 161;  // RG_OPT_SWEEP_SHAPE
   int64_t bc_fwd_hubs = 1;   // RG_OPT_BC_FWD_HUBS
+  int64_t async_results = 0;  // RG_OPT_ASYNC_RESULTS (per thread: a graph's tuning keeps the thread's)
 };
 
 // Per-thread execution context: the stream the calling thread's work goes
@@ -130,6 +134,7 @@ struct Ctx {
   int device = -1;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // result copies of RG_OPT_ASYNC_RESULTS (created on first use)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   Workspace ws;
 };
@@ -180,6 +185,13 @@ struct rg_frontier {
 };
 
 namespace rg {
+
+// Reads `bytes` of device memory into host memory through a kernel that
+// writes the thread's mapped scratch (up to kSmallRead bytes; larger reads
+// copy): small reads on a level's critical path then never wait behind a
+// large copy another stream has on a copy engine.  Syncs `st`.
+constexpr size_t kSmallRead = 65536;
+rg_status read_small(const void* d_src, void* h_dst, size_t bytes, cudaStream_t st);
 
 // Exclusive scan of `n` uint32 values into out[0..n] (out[n] = total).
 // Total must fit 32 bits.  Uses ws.scan_partials.  Async on `st`.

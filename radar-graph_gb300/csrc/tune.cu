@@ -126,6 +126,7 @@ extern "C" rg_status rg_graph_tuned_option(const rg_graph* g, int app, rg_option
     case RG_OPT_DENSE_DIV: *value = o.dense_div; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: *value = o.sweep_shape; return RG_OK;
     case RG_OPT_BC_FWD_HUBS: *value = o.bc_fwd_hubs; return RG_OK;
+    case RG_OPT_ASYNC_RESULTS: return fail(RG_EINVAL, "async_results is a thread option, not a schedule");
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }
@@ -144,6 +145,7 @@ extern "C" rg_status rg_graph_set_tuned_option(rg_graph* g, int app, rg_option o
     case RG_OPT_DENSE_DIV: o.dense_div = value; return RG_OK;
     case RG_OPT_SWEEP_SHAPE: o.sweep_shape = value; return RG_OK;
     case RG_OPT_BC_FWD_HUBS: o.bc_fwd_hubs = value; return RG_OK;
+    case RG_OPT_ASYNC_RESULTS: return fail(RG_EINVAL, "async_results is a thread option, not a schedule");
   }
   return fail(RG_EINVAL, "unknown option %d", (int)opt);
 }

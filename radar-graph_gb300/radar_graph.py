@@ -180,7 +180,11 @@ class ServerStats(C.Structure):
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("qps", C.c_double),
                 ("admission_waits", C.c_int64), ("cancelled", C.c_int64), ("peak_running", C.c_int32)]
 
-OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3, "sweep_shape": 4, "bc_fwd_hubs": 5}
+# RG_OPT_*: the scheduling options a graph's tuning holds, and the thread's
+# result-copy mode (RG_OPT_ASYNC_RESULTS)
+SCHEDULE_OPTIONS = {"direction": 0, "hub_slots": 1, "hub_smem_kb": 2, "dense_div": 3, "sweep_shape": 4,
+                    "bc_fwd_hubs": 5}
+OPTIONS = dict(SCHEDULE_OPTIONS, async_results=6)
 _RESTYPE = {"rg_last_error": C.c_char_p, "rg_status_str": C.c_char_p, "rg_version": C.c_char_p,
             "rg_host_free": None}
 
@@ -234,6 +238,12 @@ def get_option(name):
     v = C.c_int64()
     _check(lib().rg_get_option(OPTIONS[name], C.byref(v)))
     return v.value
+
+
+def synchronize():
+    """rg_synchronize: waits for the device, including result copies left in
+    flight by the async_results option."""
+    _check(lib().rg_synchronize())
 
 
 TRACE_MODES = {0: "sparse-push", 1: "dense-push", 2: "pull"}
@@ -585,7 +595,7 @@ def _graph_autotune(self, variant="radar"):
     out = {}
     for a, name in enumerate(("pagerank", "bfs", "bc", "radii")):
         opts = {}
-        for o, code in OPTIONS.items():
+        for o, code in SCHEDULE_OPTIONS.items():
             v = C.c_int64()
             _check(lib().rg_graph_tuned_option(self._h, a, code, C.byref(v)))
             opts[o] = v.value
@@ -601,7 +611,7 @@ def _graph_set_tuning(self, tuning):
     for a, name in enumerate(("pagerank", "bfs", "bc", "radii")):
         for o, v in tuning[name][1].items():
             if v >= 0:
-                _check(lib().rg_graph_set_tuned_option(self._h, a, OPTIONS[o], int(v)))
+                _check(lib().rg_graph_set_tuned_option(self._h, a, SCHEDULE_OPTIONS[o], int(v)))
 
 
 Graph.set_tuning = _graph_set_tuning

@@ -133,9 +133,11 @@ def test_engine_options_round_trip_and_validate():
     value, and another thread starts from the defaults."""
     import threading
     valid = {"direction": [0, 1], "hub_slots": [0, 512], "hub_smem_kb": [0, 4, 227],
-             "dense_div": [1, 1000, 20], "sweep_shape": [40, 42, 80, 82, 160, 162], "bc_fwd_hubs": [0, 1]}
+             "dense_div": [1, 1000, 20], "sweep_shape": [40, 42, 80, 82, 160, 162], "bc_fwd_hubs": [0, 1],
+             "async_results": [1, 0]}
     bad = {"direction": [2, -1], "hub_slots": [-1], "hub_smem_kb": [-1, 228], "dense_div": [0],
-           "sweep_shape": [43, 50, 91, 163, 120], "bc_fwd_hubs": [2, -1]}
+           "sweep_shape": [43, 50, 91, 163, 120], "bc_fwd_hubs": [2, -1],
+           "async_results": [2, -1]}
     assert set(valid) == set(rg.OPTIONS)
     for name in valid:
         old = rg.get_option(name)
