@@ -471,7 +471,7 @@ typedef enum rg_option {
    * rg_radii_seeds return once their results are staged on the device; the
    * copies into the caller's host buffers run on the thread's copy stream,
    * overlapping the next call, and are complete when rg_synchronize returns
-   * (host buffers from rg_host_alloc or otherwise page-locked let them
+   * (host buffers from rg_pinned_alloc or otherwise page-locked let them
    * overlap; pageable ones are copied before the call returns).  The host
    * buffers must not be read or freed before then.  Scalar outputs (rounds,
    * iterations, L1) are valid at return.  0 (default): every result is in
