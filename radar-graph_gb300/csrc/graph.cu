@@ -258,7 +258,11 @@ rg_status scan_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n, 
 // vertexSubset.h:196-211 toSparse)
 // ---------------------------------------------------------------------------
 constexpr int kCompThreads = 256;
-constexpr int kCompWords = 8;  // words per lane
+// Words per lane: a warp emits its non-zero words one after another, each
+// step waiting on its offsets, so fewer words per warp means more warps to
+// hide that latency (RMAT s24 four-app step: 8 words 50.2 ms, 2 words
+// 49.1 ms, 1 word 49.5 ms).
+constexpr int kCompWords = 2;
 constexpr int kCompTile = kCompThreads * kCompWords;  // words per block
 constexpr int kCompWarps = kCompThreads / 32;
 constexpr int kWarpWords = kCompWords * 32;  // consecutive words per warp
