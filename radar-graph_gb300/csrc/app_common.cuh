@@ -135,6 +135,10 @@ __global__ void gather_kernel(const T* __restrict__ in, const uint32_t* __restri
 // The thread's stream for asynchronous result copies (RG_OPT_ASYNC_RESULTS).
 rg_status copy_stream(cudaStream_t* out);
 
+// First vertex of a degree-sorted graph's pull lists with at most 8 entries
+// (a schedule hint, computed once per graph; any value gives the same results).
+uint32_t pull_split(const rg_graph* g, const DevGraph& pull_g, cudaStream_t st);
+
 // Result download, asynchronous form: `fill(stage)` enqueues on `st` the
 // work that writes the `count` results into a staging buffer; the copy into
 // h_out then runs on the thread's copy stream once that work is done, and the
@@ -316,13 +320,24 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
     const DevGraph push_g = tr ? g->in_view() : g->view();
     const DevGraph pull_g = tr ? g->view() : g->in_view();
     if (pull) {
-      const int64_t groups_per_block = 256 / 8;
-      int64_t blocks = std::min<int64_t>((g->n + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16);
+      // degree-sorted graphs: 8 lanes per vertex down to degree 8, then 2
+      // lanes per vertex for the tail, where a group of 8 would mostly idle
+      // through the dependent loads of a short list
+      const uint32_t split = g->sorted ? pull_split(g, pull_g, st) : (uint32_t)g->n;
+      auto blocks_for = [&](int64_t nv, int kg) {
+        const int64_t groups_per_block = 256 / kg;
+        return (unsigned)std::max<int64_t>(
+            std::min<int64_t>((nv + groups_per_block - 1) / groups_per_block, (int64_t)device_sms() * 16), 1);
+      };
       kt_begin(st);
-      pull_kernel<Op, 8><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(pull_g, in.bits, op, nb);
+      if (split > 0) pull_kernel<Op, 8><<<blocks_for(split, 8), 256, 0, st>>>(pull_g, in.bits, op, nb, 0u, split);
+      if (split < (uint32_t)g->n) {
+        pull_kernel<Op, 2><<<blocks_for(g->n - split, 2), 256, 0, st>>>(pull_g, in.bits, op, nb, split,
+                                                                          (uint32_t)g->n);
+      }
       kt_end(st);
       RG_CUDA(cudaGetLastError());
-      g_timing.kernel_launches++;
+      g_timing.kernel_launches += (split > 0 ? 1 : 0) + (split < (uint32_t)g->n ? 1 : 0);
       g_timing.edge_launches++;
     } else {
       int hm = (o.hubs && in.degsum >= kHubMinEdges && g_opts.hub_smem_kb > 0) ? hub_mode_of(o.variant) : kHubNone;

@@ -604,15 +604,16 @@ static __global__ void __launch_bounds__(256) mask_pull_sweep(DevGraph g, const 
 // ---------------------------------------------------------------------------
 // pull (edgeMapDense + decodeInNghBreakEarly), a group of kG lanes per vertex
 // ---------------------------------------------------------------------------
+// Vertices [vlo, vhi), a group of kG lanes per vertex.
 template <class Op, int kG>
 __global__ void __launch_bounds__(256) pull_kernel(DevGraph g, const uint32_t* __restrict__ fbits, Op op,
-                                                   uint32_t* __restrict__ next_bits) {
+                                                   uint32_t* __restrict__ next_bits, uint32_t vlo, uint32_t vhi) {
   const int lane = threadIdx.x & 31;
   const int gl = lane % kG;
   const unsigned gmask = (kG == 32) ? 0xffffffffu : (((1u << kG) - 1u) << (lane - gl));
   const uint64_t group = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / kG;
   const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / kG;
-  for (uint64_t vv = group; vv < g.n; vv += ngroups) {
+  for (uint64_t vv = vlo + group; vv < vhi; vv += ngroups) {
     const uint32_t v = (uint32_t)vv;
     if (!op.cond(v)) continue;
     const uint32_t b = g.off[v], e = g.off[v + 1];

@@ -133,6 +133,32 @@ rg_status get_ctx(Ctx** out) {
 
 Ctx& ctx() { return *t_ctx; }
 
+// Binary search, degrees non-increasing: the first v with at most t entries.
+__global__ void find_pull_split(const uint32_t* __restrict__ off, uint32_t n, uint32_t t, uint32_t* out) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (off[mid + 1] - off[mid] <= t) hi = mid;
+    else lo = mid + 1;
+  }
+  *out = lo;
+}
+
+uint32_t pull_split(const rg_graph* g, const DevGraph& pull_g, cudaStream_t st) {
+  int64_t v = g->pull_split.load(std::memory_order_relaxed);
+  if (v >= 0) return (uint32_t)v;
+  Workspace& ws = ctx().ws;
+  uint32_t* d = reinterpret_cast<uint32_t*>(ws.counters.as<uint64_t>() + 8);  // a free scratch word
+  find_pull_split<<<1, 1, 0, st>>>(pull_g.off, pull_g.n, 8u, d);
+  uint32_t h = pull_g.n;
+  if (cudaGetLastError() != cudaSuccess || read_small(d, &h, 4, st) != RG_OK) {
+    cudaGetLastError();
+    return pull_g.n;  // a hint only: one group size for every vertex
+  }
+  g->pull_split.store(h, std::memory_order_relaxed);
+  return h;
+}
+
 rg_status copy_stream(cudaStream_t* out) {
   Ctx* c = nullptr;
   RG_TRY(get_ctx(&c));

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <memory>
+#include <atomic>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -166,6 +167,7 @@ struct rg_graph {
   mutable bool host_ready = false;
   mutable std::mutex host_mu;
   uint32_t max_deg = 0;
+  mutable std::atomic<int64_t> pull_split{-1};  // pull_split()'s cached value, -1 = not yet known
   bool tuned[4] = {false, false, false, false};  // per app: PageRank, BFS, BC, Radii
   rg::Options topt[4];                           // the autotuner's choice per app
   rg::DevGraph view() const {
