@@ -320,9 +320,10 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
     const DevGraph push_g = tr ? g->in_view() : g->view();
     const DevGraph pull_g = tr ? g->view() : g->in_view();
     if (pull) {
-      // degree-sorted graphs: 8 lanes per vertex down to degree 8, then 2
-      // lanes per vertex for the tail, where a group of 8 would mostly idle
-      // through the dependent loads of a short list
+      // degree-sorted graphs: 8 lanes per vertex down to degree 8, then one
+      // lane per vertex for the tail, where a group would mostly idle through
+      // the dependent loads of a short list (RMAT s24 BFS: 8 lanes for every
+      // vertex 1.62 ms, 2 for the tail 1.06, 1 for the tail 0.97)
       const uint32_t split = g->sorted ? pull_split(g, pull_g, st) : (uint32_t)g->n;
       auto blocks_for = [&](int64_t nv, int kg) {
         const int64_t groups_per_block = 256 / kg;
@@ -332,7 +333,7 @@ rg_status edge_map(rg_graph* g, const FView& in, const Op& op, FView* out, const
       kt_begin(st);
       if (split > 0) pull_kernel<Op, 8><<<blocks_for(split, 8), 256, 0, st>>>(pull_g, in.bits, op, nb, 0u, split);
       if (split < (uint32_t)g->n) {
-        pull_kernel<Op, 2><<<blocks_for(g->n - split, 2), 256, 0, st>>>(pull_g, in.bits, op, nb, split,
+        pull_kernel<Op, 1><<<blocks_for(g->n - split, 1), 256, 0, st>>>(pull_g, in.bits, op, nb, split,
                                                                           (uint32_t)g->n);
       }
       kt_end(st);
