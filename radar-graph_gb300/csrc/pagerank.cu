@@ -214,25 +214,33 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
       U128 part{0ull, 0ull}, head{0ull, 0ull};
       bool cont = false;      // the lane's last row continues past the lane
       if (e < g.m) {
-        // in bounds: adj is padded by 8 entries and 32-byte aligned
-        // neighbour ids: 16 edges per lane load each batch's 8 ids with its
-        // gathers (fewer live registers), narrower shapes load them here
-        constexpr bool kIdsPerBatch = kItems > 8;
-        uint32_t uu[kIdsPerBatch ? 1 : kItems];
-        if (kIdsPerBatch) {
-        } else if (kItems == 8 && kMode >= 1) {
-          const U32x8 w = ld_stream_v8(g.adj + e);
+        // the lane's neighbour ids, all loaded up front: with 16 edges per
+        // lane the second 32 bytes come from the L2 line the first just
+        // brought in (loaded only when the second batch starts, the streamed,
+        // evict-first line was often gone: RMAT s24 read 3.53 instead of 2.79
+        // GB per sweep).  In bounds: adj is padded by 8 entries and 32-byte
+        // aligned, and a group past the first is read only when it starts
+        // before m.
+        uint32_t uu[kItems];
+        if (kItems >= 8 && kMode >= 1) {
 #pragma unroll
-          for (int i = 0; i < kItems; i++) uu[kIdsPerBatch ? 0 : i] = w.v[i];
+          for (int h = 0; h < kItems / 8; h++) {
+            const U32x8 w = (h == 0 || e + 8 * h < g.m) ? ld_stream_v8(g.adj + e + 8 * h) : U32x8{};
+#pragma unroll
+            for (int i = 0; i < 8; i++) uu[8 * h + i] = w.v[i];
+          }
         } else {
 #pragma unroll
           for (int h = 0; h < kItems / 4; h++) {
-            const uint4 w = kMode >= 1 ? ld_stream_v4(g.adj + e + 4 * h, first)
-                                       : __ldg(reinterpret_cast<const uint4*>(g.adj + e + 4 * h));
-            uu[kIdsPerBatch ? 0 : 4 * h] = w.x;
-            uu[kIdsPerBatch ? 0 : 4 * h + 1] = w.y;
-            uu[kIdsPerBatch ? 0 : 4 * h + 2] = w.z;
-            uu[kIdsPerBatch ? 0 : 4 * h + 3] = w.w;
+            uint4 w = make_uint4(0u, 0u, 0u, 0u);
+            if (h < 2 || e + 4 * h < g.m) {
+              w = kMode >= 1 ? ld_stream_v4(g.adj + e + 4 * h, first)
+                             : __ldg(reinterpret_cast<const uint4*>(g.adj + e + 4 * h));
+            }
+            uu[4 * h] = w.x;
+            uu[4 * h + 1] = w.y;
+            uu[4 * h + 2] = w.z;
+            uu[4 * h + 3] = w.w;
           }
         }
         uint32_t v = upper_index(g.off, vlo, vhi, e);
@@ -241,34 +249,15 @@ __global__ void __launch_bounds__(kCache ? 1024 : kPullThreads)
         row = v;
         bool at_first = true;
         // the gathers in batches of at most 8 per lane (16 edges per lane
-        // halve the warp scans per edge without holding 16 values at once)
+        // halve the warp scans per edge without 16 values in flight at once)
         constexpr int kBatch = kItems > 8 ? 8 : kItems;
-        // in bounds: adj is padded by 8 entries and a batch starts before m
-        auto load_ids = [&](uint32_t at) {
-          if (kMode >= 1) return ld_stream_v8(g.adj + at);
-          const uint4 lo = __ldg(reinterpret_cast<const uint4*>(g.adj + at));
-          const uint4 hi = __ldg(reinterpret_cast<const uint4*>(g.adj + at + 4));
-          return U32x8{{lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w}};
-        };
-        // both halves' ids at once: the second 32 bytes of each lane's edge
-        // ids come from the L2 line the first just brought in (loaded at the
-        // second batch, the streamed, evict-first line is often gone: RMAT
-        // s24 read 3.53 instead of 2.79 GB per sweep)
-        U32x8 ids_all[kIdsPerBatch ? kItems / kBatch : 1];
-        if (kIdsPerBatch) {
-#pragma unroll
-          for (int h = 0; h < (kIdsPerBatch ? kItems / kBatch : 1); h++) {
-            ids_all[h] = (h == 0 || e + h * kBatch < g.m) ? load_ids(e + h * kBatch) : U32x8{};
-          }
-        }
 #pragma unroll
         for (int b = 0; b < kItems; b += kBatch) {
           if (e + b >= g.m) break;
-          const U32x8 ids = ids_all[kIdsPerBatch ? b / kBatch : 0];
           double x[kBatch];
 #pragma unroll
           for (int j = 0; j < kBatch; j++) {
-            const uint32_t u = kIdsPerBatch ? ids.v[j] : uu[kIdsPerBatch ? 0 : b + j];
+            const uint32_t u = uu[b + j];
             x[j] = (e + b + j < g.m) ? ((kCache && u < H) ? hc[u]
                                         : kMode == 2 ? __longlong_as_double((long long)ld_keep_u64(contrib_bits + u, keep))
                                                      : __ldg(contrib + u))
