@@ -495,9 +495,10 @@ __global__ void __launch_bounds__(kThreads) push_lbs(DevGraph g, const uint32_t*
 // last changed two or more rounds ago and pushed its unchanged mask to v
 // then, so its bits are already in visited[v]; the new bits and the next
 // frontier are exactly those of the push over the frontier (Radii.C:51-76).
-// Edge-balanced like the PageRank sweep: 8 edges per lane (one streamed
-// 32-byte load), row pieces combined by a segmented OR scan, one atomicOr and
-// activation per row piece that adds bits.
+// Edge-balanced like the PageRank sweep: 8 or 16 edges per lane (streamed
+// 32-byte id loads, gathers in batches of 8), row pieces combined by one
+// segmented OR scan per warp step, one atomicOr and activation per row piece
+// that adds bits.
 // ---------------------------------------------------------------------------
 static __device__ __forceinline__ void mask_flush(const unsigned long long* __restrict__ visited,
                                             unsigned long long* next_visited, uint32_t* next_bits, uint32_t row,

@@ -84,8 +84,8 @@ __global__ void __launch_bounds__(256) prd_filter(uint32_t n, const uint32_t* __
 // Dense round as a pull over every edge: nghSum[v] = sum of c[u] over all
 // neighbours.  c is 0 for vertices outside the frontier (the filter writes
 // it so), so no frontier test is needed and the sum is the push's over the
-// frontier.  Edge-balanced like the PageRank sweep (8 edges per lane, edge
-// array streamed), FP64 sums in a fixed order, one add per row piece.
+// frontier.  Edge-balanced (8 edges per lane, edge array streamed), FP64
+// sums in a fixed order, one add per row piece.
 __global__ void __launch_bounds__(256) prd_pull_sweep(DevGraph g, const uint32_t* __restrict__ chunk_v,
                                                       uint32_t nchunks, const double* __restrict__ c, double* ngh) {
   constexpr int kItems = 8, kStep = 32 * kItems;
