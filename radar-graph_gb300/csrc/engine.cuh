@@ -336,6 +336,9 @@ template <> struct IsRadii<OpRadii> { static constexpr bool value = true; };
 constexpr int kPushThreads = 256;     // plain push
 constexpr int kHubPushThreads = 256;  // hub push: small CTAs with a bounded hub array keep occupancy
 constexpr int kPushItems = 4;
+// push_lbs zeroes and max-scans a thread's owner slots as one uint4: one slot
+// per edge the thread takes, so exactly four
+static_assert(kPushItems == 4, "push_lbs's owner scan handles four slots per thread");
 
 template <int kThreads>
 __device__ __forceinline__ uint32_t block_max_scan_prefix(uint32_t v) {
