@@ -72,7 +72,9 @@ __global__ void read_small_kernel(const unsigned char* __restrict__ src, volatil
 
 rg_status read_small(const void* d_src, void* h_dst, size_t bytes, cudaStream_t st) {
   if (bytes == 0) return RG_OK;
-  Workspace& ws = ctx().ws;
+  Ctx* c = nullptr;
+  RG_TRY(get_ctx(&c));
+  Workspace& ws = c->ws;
   if (bytes > kSmallRead || !ws.h_small_dev) {
     RG_CUDA(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, st));
     RG_CUDA(cudaStreamSynchronize(st));
@@ -147,7 +149,9 @@ __global__ void find_pull_split(const uint32_t* __restrict__ off, uint32_t n, ui
 uint32_t pull_split(const rg_graph* g, const DevGraph& pull_g, cudaStream_t st) {
   int64_t v = g->pull_split.load(std::memory_order_relaxed);
   if (v >= 0) return (uint32_t)v;
-  Workspace& ws = ctx().ws;
+  Ctx* c = nullptr;
+  if (get_ctx(&c) != RG_OK) return pull_g.n;  // a hint only: one group size for every vertex
+  Workspace& ws = c->ws;
   uint32_t* d = reinterpret_cast<uint32_t*>(ws.counters.as<uint64_t>() + 8);  // a free scratch word
   find_pull_split<<<1, 1, 0, st>>>(pull_g.off, pull_g.n, 8u, d);
   uint32_t h = pull_g.n;
